@@ -1,0 +1,104 @@
+"""ctypes binding of ``libgtrap_gb300.so`` (the C ABI in ``include/gtrap_gb300.h``).
+
+The library is loaded lazily on first use.  There is no CPU fallback: when the
+library is missing or cannot be loaded, every call raises ``GtrapError``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+
+from . import _build
+
+c_float_p = C.POINTER(C.c_float)
+vp = C.c_void_p
+u32 = C.c_uint32
+i32 = C.c_int32
+f32 = C.c_float
+f64 = C.c_double
+sz = C.c_size_t
+
+# status codes (enum gtrap_status)
+OK, ERR_INVALID_ARG, ERR_CUDA, ERR_WORKSPACE, ERR_UNSUPPORTED, ERR_TIMEOUT = range(6)
+
+BLS_PHASE_FP32_REF = 0x1
+BLS_REF_F0_NOFMA = 0x2
+BLS_REF_PH_FMA = 0x4
+TLS_W_NOFMA = 0x1
+TLS_T_NOFMA = 0x2
+
+_SIGNATURES = {
+    "gtrap_last_error": (C.c_char_p, []),
+    "gtrap_version": (C.c_int, []),
+    "gtrap_gfilter": (C.c_int, [vp, vp, u32, u32, u32, vp]),
+    "gtrap_offset": (C.c_int, [vp, vp, vp, u32, u32, vp]),
+    "gtrap_geebls_workspace_size": (sz, [u32, u32, u32]),
+    "gtrap_geebls": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, u32, u32, u32, u32, u32, u32, u32,
+                               f32, f32, u32, u32, vp, sz, vp]),
+    "gtrap_geebls_simple_workspace_size": (sz, [u32, u32, u32]),
+    "gtrap_geebls_simple": (C.c_int, [vp, vp, vp, vp, vp, u32, u32, u32, u32, u32, u32, u32,
+                                      f32, f32, u32, u32, vp, sz, vp]),
+    "gtrap_blsstat": (C.c_int, [vp, vp, vp, u32, u32, f64, f64, u32, vp, vp, vp, vp, vp]),
+    "gtrap_getmax": (C.c_int, [vp, vp, vp, u32, u32, u32, vp, vp, vp, vp, vp, vp, vp]),
+    "gtrap_gtls": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, i32, i32, i32, i32, i32, f32, f32, f32,
+                             f32, f32, i32, u32, vp]),
+    "gtrap_probe_fp32_peak": (C.c_int, [vp, u32, C.POINTER(C.c_double), vp]),
+}
+
+
+class GtrapError(RuntimeError):
+    """Error reported by the native library (or its absence)."""
+
+    def __init__(self, status, message):
+        super().__init__(message)
+        self.status = status
+
+
+_lib = None
+_lock = threading.Lock()
+
+
+def load(build_if_missing: bool = False):
+    """Return the loaded library, raising GtrapError when it is not available."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.library_path()
+        if not path.exists():
+            if build_if_missing:
+                _build.build()
+            else:
+                raise GtrapError(ERR_UNSUPPORTED,
+                                 "gtrap_gb300 native library not built (%s); run "
+                                 "`python -m gtrap_gb300._build` first" % path)
+        try:
+            lib = C.CDLL(str(path))
+        except OSError as exc:
+            raise GtrapError(ERR_UNSUPPORTED, "cannot load %s: %s" % (path, exc)) from exc
+        for name, (res, args) in _SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib
+
+
+def exported_symbols():
+    return sorted(_SIGNATURES)
+
+
+def call(name, *args):
+    """Call an entry point returning a status and raise on failure."""
+    lib = load()
+    st = getattr(lib, name)(*args)
+    if st != OK:
+        msg = lib.gtrap_last_error().decode(errors="replace")
+        raise GtrapError(st, "%s failed (status %d): %s" % (name, st, msg))
+    return st
+
+
+def fn(name):
+    return getattr(load(), name)

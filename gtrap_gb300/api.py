@@ -1,0 +1,207 @@
+"""Tensor-level API over the native library (the path the drop-in modules use).
+
+All functions take and return CUDA tensors, launch on the current PyTorch stream and
+return without synchronising.  Layouts follow the reference: light-curve images are
+``[n, nq]`` float32 (C order), BLS spectra ``[nq, nf]``, GTLS outputs ``[nt, nq]``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import torch
+
+from . import _native as N
+from ._dev import as_ptr, require_cuda, stream_handle, workspace
+
+MINBIN = 5  # gtrap/geebls.py:14
+
+
+def _f32(t: torch.Tensor, name: str) -> torch.Tensor:
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise TypeError("%s must be a CUDA tensor" % name)
+    if t.dtype != torch.float32:
+        raise TypeError("%s must be float32 (got %s)" % (name, t.dtype))
+    return t.contiguous()
+
+
+def _u32(t: torch.Tensor, name: str) -> torch.Tensor:
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise TypeError("%s must be a CUDA tensor" % name)
+    if t.dtype not in (torch.int32, torch.uint32):
+        raise TypeError("%s must be int32/uint32 (got %s)" % (name, t.dtype))
+    return t.contiguous()
+
+
+@dataclass(frozen=True)
+class BlsGrid:
+    """Bin-grid parameters derived from duty-cycle limits as the reference's drivers do
+    (``ipynb/example geebls  Kepler Planet.ipynb`` cell 13: kma = int(qma*nb)+1,
+    kmi = int(qmi*nb), kkmi = int(n*qmi))."""
+
+    nb: int
+    kma: int
+    kmi: int
+    kkmi: int
+
+    @staticmethod
+    def from_duty(n: int, nb: int, qmi: float, qma: float) -> "BlsGrid":
+        return BlsGrid(nb=int(nb), kma=int(qma * nb) + 1, kmi=int(qmi * nb), kkmi=int(n * qmi))
+
+
+def gfilter(x: torch.Tensor, r: int, out: torch.Tensor | None = None, stream=None) -> torch.Tensor:
+    """Residual of the running median of window 2r+1 along axis 0 of ``x[n, nq]``."""
+    require_cuda()
+    x = _f32(x, "x")
+    if x.dim() != 2:
+        raise ValueError("x must be [n, nq]")
+    n, nq = x.shape
+    if out is None:
+        out = torch.empty_like(x)
+    N.call("gtrap_gfilter", as_ptr(x), as_ptr(out), n, nq, int(r), stream_handle(stream))
+    return out
+
+
+def offset(resid: torch.Tensor, tu: torch.Tensor, out: torch.Tensor | None = None,
+           stream=None) -> torch.Tensor:
+    """Per-curve mean of ``resid[n, nq]`` with masked (tu < 0) samples counted as zero."""
+    resid = _f32(resid, "resid")
+    tu = _f32(tu, "tu")
+    n, nq = resid.shape
+    if tu.shape != resid.shape:
+        raise ValueError("tu must have the shape of resid")
+    if out is None:
+        out = torch.empty(nq, dtype=torch.float32, device=resid.device)
+    N.call("gtrap_offset", as_ptr(resid), as_ptr(tu), as_ptr(out), n, nq, stream_handle(stream))
+    return out
+
+
+def _phase_flags(phase: str, f0_fma: bool = True, ph_fma: bool = False) -> int:
+    if phase == "exact":
+        return 0
+    if phase == "fp32":
+        flags = N.BLS_PHASE_FP32_REF
+        if not f0_fma:
+            flags |= N.BLS_REF_F0_NOFMA
+        if ph_fma:
+            flags |= N.BLS_REF_PH_FMA
+        return flags
+    raise ValueError("phase must be 'exact' or 'fp32'")
+
+
+def geebls(lc, tu, offset_, ntrue, nf, nb, kma, kmi, kkmi, fmin, df, *, phase="exact",
+           ref_nthread=0, f0_fma=True, ph_fma=False, out=None, stream=None):
+    """Masked BLS with per-curve times, offsets and valid counts (geebls).
+
+    Returns ``(blsp[nq, nf], phase1[nq, nf], phase2[nq, nf])``."""
+    require_cuda()
+    lc = _f32(lc, "lc")
+    tu = _f32(tu, "tu")
+    offset_ = _f32(offset_, "offset")
+    ntrue = _u32(ntrue, "ntrue")
+    n, nq = lc.shape
+    if tu.shape != lc.shape:
+        raise ValueError("tu must be [n, nq] like lc")
+    flags = _phase_flags(phase, f0_fma, ph_fma)
+    dev = lc.device
+    if out is None:
+        out = (torch.empty((nq, nf), dtype=torch.float32, device=dev),
+               torch.empty((nq, nf), dtype=torch.int32, device=dev),
+               torch.empty((nq, nf), dtype=torch.int32, device=dev))
+    blsp, p1, p2 = out
+    need = N.fn("gtrap_geebls_workspace_size")(n, nq, flags)
+    ws = workspace(need, slot="bls")
+    N.call("gtrap_geebls", as_ptr(blsp), as_ptr(p1), as_ptr(p2), as_ptr(lc), as_ptr(tu),
+           as_ptr(offset_), as_ptr(ntrue), n, nq, int(nf), int(nb), int(kma), int(kmi), int(kkmi),
+           float(fmin), float(df), flags, int(ref_nthread), as_ptr(ws), ws.numel(),
+           stream_handle(stream))
+    return blsp, p1, p2
+
+
+def geebls_simple(lc, tu, nf, nb, kma, kmi, kkmi, fmin, df, *, phase="exact", ref_nthread=0,
+                  f0_fma=True, ph_fma=False, with_phase=False, out=None, stream=None):
+    """Plain BLS with a common time axis ``tu[n]`` (geebls_simple).
+
+    Returns ``blsp[nq, nf]`` or ``(blsp, phase1, phase2)`` when ``with_phase``."""
+    require_cuda()
+    lc = _f32(lc, "lc")
+    tu = _f32(tu, "tu").reshape(-1)
+    n, nq = lc.shape
+    if tu.numel() != n:
+        raise ValueError("tu must hold n samples")
+    flags = _phase_flags(phase, f0_fma, ph_fma)
+    dev = lc.device
+    if out is None:
+        blsp = torch.empty((nq, nf), dtype=torch.float32, device=dev)
+        p1 = torch.empty((nq, nf), dtype=torch.int32, device=dev) if with_phase else None
+        p2 = torch.empty((nq, nf), dtype=torch.int32, device=dev) if with_phase else None
+    else:
+        blsp, p1, p2 = out
+    need = N.fn("gtrap_geebls_simple_workspace_size")(n, nq, flags)
+    ws = workspace(need, slot="bls")
+    N.call("gtrap_geebls_simple", as_ptr(blsp), as_ptr(p1), as_ptr(p2), as_ptr(lc), as_ptr(tu),
+           n, nq, int(nf), int(nb), int(kma), int(kmi), int(kkmi), float(fmin), float(df), flags,
+           int(ref_nthread), as_ptr(ws), ws.numel(), stream_handle(stream))
+    return (blsp, p1, p2) if (with_phase or out is not None) else blsp
+
+
+def blsstat(blsp, phase1, phase2, df, fmin, patch=0, stream=None):
+    """Per-curve (Pest, SDE, phase1 at max, phase2 at max) as device tensors."""
+    blsp = _f32(blsp, "blsp")
+    nq, nf = blsp.shape
+    dev = blsp.device
+    pest = torch.empty(nq, dtype=torch.float64, device=dev)
+    sde = torch.empty(nq, dtype=torch.float64, device=dev)
+    b1 = torch.empty(nq, dtype=torch.int32, device=dev)
+    b2 = torch.empty(nq, dtype=torch.int32, device=dev)
+    N.call("gtrap_blsstat", as_ptr(blsp), as_ptr(phase1), as_ptr(phase2), nf, nq, float(df),
+           float(fmin), int(patch), as_ptr(pest), as_ptr(sde), as_ptr(b1), as_ptr(b2),
+           stream_handle(stream))
+    return pest, sde, b1, b2
+
+
+def getmax(blsp, phase1, phase2, patch, stream=None):
+    """Per-patch partial statistics with the reference getmax kernel's outputs."""
+    blsp = _f32(blsp, "blsp")
+    nq, nf = blsp.shape
+    npatch = nf // patch
+    dev = blsp.device
+    outs = (torch.empty(npatch * nq, dtype=torch.float32, device=dev),
+            torch.empty(npatch * nq, dtype=torch.int32, device=dev),
+            torch.empty(npatch * nq, dtype=torch.float32, device=dev),
+            torch.empty(npatch * nq, dtype=torch.float32, device=dev),
+            torch.empty(npatch * nq, dtype=torch.int32, device=dev),
+            torch.empty(npatch * nq, dtype=torch.int32, device=dev))
+    N.call("gtrap_getmax", as_ptr(blsp), as_ptr(phase1), as_ptr(phase2), nf, nq, int(patch),
+           *[as_ptr(o) for o in outs], stream_handle(stream))
+    return outs
+
+
+def gtls(lc, tu, nt, nw, nl, nsc, wmax, dw, deltat, *, mode=0, t0min=0.0, dt=0.0,
+         w_fma=True, t_fma=True, out=None, stream=None):
+    """Trapezoid least-squares epoch search; returns (sn, w, t0, l, h), each ``[nt, nq]``."""
+    require_cuda()
+    lc = _f32(lc, "lc")
+    tu = _f32(tu, "tu")
+    n, nq = lc.shape
+    if tu.shape != lc.shape:
+        raise ValueError("tu must be [n, nq] like lc")
+    if nt > n:
+        raise ValueError("nt=%d exceeds the number of samples n=%d" % (nt, n))
+    dev = lc.device
+    if out is None:
+        out = tuple(torch.empty((nt, nq), dtype=torch.float32, device=dev) for _ in range(5))
+    flags = (0 if w_fma else N.TLS_W_NOFMA) | (0 if t_fma else N.TLS_T_NOFMA)
+    sn, w, t0, l, h = out
+    N.call("gtrap_gtls", as_ptr(sn), as_ptr(w), as_ptr(t0), as_ptr(l), as_ptr(h), as_ptr(lc),
+           as_ptr(tu), int(nt), int(nq), int(nw), int(nl), int(nsc), float(t0min), float(dt),
+           float(wmax), float(dw), float(deltat), int(mode), flags, stream_handle(stream))
+    return out
+
+
+def fp32_peak_probe(iters=4096, stream=None):
+    """Launch the FP32 FMA probe; returns (sink tensor, flop count)."""
+    sink = torch.empty(1 << 20, dtype=torch.float32, device="cuda")
+    flops = C.c_double(0.0)
+    N.call("gtrap_probe_fp32_peak", as_ptr(sink), int(iters), C.byref(flops), stream_handle(stream))
+    return sink, flops.value

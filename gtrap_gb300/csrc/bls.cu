@@ -1,0 +1,586 @@
+// Box least squares: fold + Signal-Residue scan (geebls / geebls_simple).
+//
+// Reference behaviour (include/geebls.h:1-167, gtrap/geebls_simple.py:17-174): one CTA
+// per (trial frequency, curve) folds every sample into nb phase bins with shared float
+// atomics, wraps the first kma bins past nb, and for every start bin i accumulates up to
+// kma bins, keeping max s^2/(kk (N - kk)) over windows of k > kmi bins holding kk > kkmi
+// samples.  SR = sqrt(max); the start and (inclusive) end bin of the best window are the
+// phase outputs.
+//
+// GB300 design:
+//  * prep: the [n, nq] time-major image is transposed once into curve-major arrays so
+//    every later read is coalesced.  Flux is quantised to a per-curve power-of-two fixed
+//    point (|x| < 2^30) and packed with a count of one into a 64-bit word, so a single
+//    integer shared atomic updates both the bin sum and the bin count; integer sums are
+//    exact and order independent, so every result is deterministic (a curve gives the
+//    same bits alone or batched).  Phases are exact: frac(t*fmin) and frac(t*df) of the
+//    float32 inputs are formed as 64-bit fixed-point fractions (the float products are
+//    exact in 48 bits), and frac(t*(fmin + j*df)) = A + j*B mod 2^64 with no rounding at
+//    all; the bin is the top log2(nb) bits.  This removes the FP32 phase drift of the
+//    reference (about 1e-5 cycles at t*f ~ 170) without any FP64 arithmetic in the fold.
+//  * fold: one CTA per (curve, tile of F consecutive frequencies); every loaded sample is
+//    binned for all F frequencies (phase step = one 64-bit add).
+//  * scan: groups of Tg threads turn a histogram into exact integer prefix sums (rounded
+//    once to float), then each thread evaluates R consecutive start bins against every
+//    end bin with one padded, conflict-free 8-byte shared load per R candidates.  A
+//    division-free pre-test s^2 >= best' * den (best' = best*(1 - 2^-20)) admits every
+//    candidate that can tie or beat the running best; admitted candidates are compared
+//    exactly with a correctly rounded quotient and a lowest-(start, end) tie-break.
+#include "common.cuh"
+
+#include <climits>
+
+namespace {
+
+using gtrap::fail;
+
+constexpr int kThreads = 512;
+constexpr int kMaxNb = 8192;
+constexpr int32_t kMasked = INT32_MIN;
+
+// frac(t*f) * 2^64 for float32 t and f, exact whenever the product is >= 2^-17.
+__device__ __forceinline__ uint64_t frac64(float t, float f) {
+  const uint32_t bt = __float_as_uint(t), bf = __float_as_uint(f);
+  const uint32_t et = (bt >> 23) & 0xFFu, ef = (bf >> 23) & 0xFFu;
+  const uint64_t mt = (bt & 0x7FFFFFu) | (et ? 0x800000u : 0u);
+  const uint64_t mf = (bf & 0x7FFFFFu) | (ef ? 0x800000u : 0u);
+  // t*f = mt*mf * 2^(e), e = (et' - 150) + (ef' - 150) with et' = max(et, 1)
+  const int e = (int)(et ? et : 1u) + (int)(ef ? ef : 1u) - 300;
+  const uint64_t m = mt * mf;  // < 2^48
+  const int s = e + 64;        // fraction bits start 64 places below the binary point
+  uint64_t a;
+  if (s >= 64 || m == 0) a = 0;             // integer product
+  else if (s >= 0) a = m << s;              // bits above 2^0 fall off: frac
+  else if (s > -64) a = m >> (-s);          // product below 2^-16: truncated
+  else a = 0;
+  if ((bt ^ bf) >> 31) a = 0ull - a;        // frac(-x) = 1 - frac(x)
+  return a;
+}
+
+// ---------------------------------------------------------------------------
+// prep
+
+struct PrepArgs {
+  const float *lc;       // [n, nq]
+  const float *tu;       // [n, nq] (full) or [n] (simple)
+  const float *offset;   // [nq] or null
+  int32_t *sx;           // [nq] out: scale exponent
+  int32_t *X;            // [nq, n] out: quantised flux or kMasked
+  ulonglong2 *AB;        // [nq, n] (full) or [n] (simple) out: (frac(t*fmin), frac(t*df))
+  float *T;              // [nq, n] out (FP32-reference phase mode, full only) or null
+  uint32_t n, nq, n_eff;
+  float fmin, df;
+  double xq_max;         // largest allowed |quantised flux|
+  int full;              // 1: per-curve tu, mask, offset
+  int exact;             // 1: exact phase (AB), 0: FP32 reference phase (T)
+};
+
+__device__ __forceinline__ bool sample_valid(const PrepArgs &a, uint32_t i, float t, float x,
+                                             double off) {
+  if (i >= a.n_eff) return false;
+  if (!isfinite(x)) return false;
+  if (a.full && !(t >= 0.0f)) return false;  // include/geebls.h:67, INVT = 0.0
+  if (!isfinite(t)) return false;
+  return isfinite((double)x - off);
+}
+
+// Per-curve power-of-two scale: 2^sx * max|x - offset| < xq_max.
+__global__ void __launch_bounds__(1024) bls_scale_kernel(PrepArgs a) {
+  __shared__ double part[32][33];
+  const int lane = threadIdx.x, row = threadIdx.y;
+  const uint32_t q = blockIdx.x * 32 + lane;
+  double amax = 0.0;
+  if (q < a.nq) {
+    const double off = a.offset ? (double)a.offset[q] : 0.0;
+    for (uint32_t i = row; i < a.n; i += 32) {
+      const size_t idx = (size_t)i * a.nq + q;
+      const float x = __ldg(a.lc + idx);
+      const float t = a.full ? __ldg(a.tu + idx) : __ldg(a.tu + i);
+      if (sample_valid(a, i, t, x, off)) amax = fmax(amax, fabs((double)x - off));
+    }
+  }
+  part[row][lane] = amax;
+  __syncthreads();
+  if (row == 0 && q < a.nq) {
+    double m = 0.0;
+    for (int k = 0; k < 32; ++k) m = fmax(m, part[k][lane]);
+    int s = 0;
+    if (m > 0.0) s = ilogb(a.xq_max) - ilogb(m) - 1;
+    a.sx[q] = s;
+  }
+}
+
+// Transpose a 32x32 tile of the [n, nq] image into curve-major quantised flux (and,
+// for per-curve times, the exact phase pair or the raw float time).
+__global__ void __launch_bounds__(256) bls_pack_kernel(PrepArgs a) {
+  __shared__ int32_t xt[32][33];
+  __shared__ float tt[32][33];
+  const uint32_t q0 = blockIdx.x * 32, i0 = blockIdx.y * 32;
+  {
+    const uint32_t q = q0 + threadIdx.x;
+    double off = 0.0, scale = 1.0;
+    if (q < a.nq) {
+      off = a.offset ? (double)a.offset[q] : 0.0;
+      scale = ldexp(1.0, a.sx[q]);
+    }
+    for (int r = threadIdx.y; r < 32; r += 8) {
+      const uint32_t i = i0 + r;
+      int32_t v = kMasked;
+      float t = 0.0f;
+      if (q < a.nq && i < a.n) {
+        const size_t idx = (size_t)i * a.nq + q;
+        const float x = __ldg(a.lc + idx);
+        t = a.full ? __ldg(a.tu + idx) : __ldg(a.tu + i);
+        if (sample_valid(a, i, t, x, off)) v = (int32_t)__double2ll_rn(((double)x - off) * scale);
+      }
+      xt[r][threadIdx.x] = v;
+      tt[r][threadIdx.x] = t;
+    }
+  }
+  __syncthreads();
+  const uint32_t i = i0 + threadIdx.x;
+  if (i >= a.n) return;
+  for (int c = threadIdx.y; c < 32; c += 8) {
+    const uint32_t q = q0 + c;
+    if (q >= a.nq) break;
+    const size_t o = (size_t)q * a.n + i;
+    a.X[o] = xt[threadIdx.x][c];
+    if (a.full) {
+      const float t = tt[threadIdx.x][c];
+      if (a.exact) a.AB[o] = make_ulonglong2(frac64(t, a.fmin), frac64(t, a.df));
+      else a.T[o] = t;
+    }
+  }
+}
+
+// Exact phase pair of a common time axis (geebls_simple).
+__global__ void bls_common_phase_kernel(const float *__restrict__ tu, ulonglong2 *AB, uint32_t n,
+                                        float fmin, float df) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    const float t = tu[i];
+    AB[i] = make_ulonglong2(frac64(t, fmin), frac64(t, df));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// fold + scan
+
+struct BlsArgs {
+  float *blsp;
+  uint32_t *ph1, *ph2;
+  const int32_t *X;        // [nq, n]
+  const ulonglong2 *AB;    // exact phase pairs
+  const float *T;          // FP32-reference times
+  const int32_t *sx;       // [nq]
+  const uint32_t *ntrue;   // [nq] or null (use n_den)
+  uint32_t n, n_den, nq, nf, nb, kma, kmi, kkmi;
+  float fmin, df;
+  uint32_t F, tiles, region, Tg, G;
+  int lognb, CB;
+  uint32_t ab_stride, t_stride;  // elements per curve (0: shared by all curves)
+  uint32_t flags;
+};
+
+template <int R>
+__device__ __forceinline__ int padi(int e) { return e + (e >> (R == 16 ? 4 : 3)); }
+
+__device__ __forceinline__ void group_bar(int id, int nthreads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
+__device__ __forceinline__ bool better(float p, int i, int e, float bp, int bi, int be) {
+  return p > bp || (p == bp && (i < bi || (i == bi && e < be)));
+}
+
+// MODE 0: exact phase, nb power of two; 1: exact phase, any nb; 2: FP32 reference phase.
+template <int R, int MODE>
+__global__ void __launch_bounds__(kThreads, R == 8 ? 2 : 1) bls_fold_scan_kernel(const BlsArgs a) {
+  extern __shared__ __align__(16) unsigned long long sm[];
+  __shared__ long long scan_x[kThreads / 32];
+  __shared__ int scan_c[kThreads / 32];
+  __shared__ float red_p[kThreads / 32];
+  __shared__ int red_i[kThreads / 32], red_e[kThreads / 32];
+
+  const uint32_t item = blockIdx.x;
+  const uint32_t q = item / a.tiles;
+  const uint32_t tile = item - q * a.tiles;
+  if (q >= a.nq) return;
+  const uint32_t j0 = tile * a.F;
+  const uint32_t nfrem = min(a.F, a.nf - j0);
+  const int tid = threadIdx.x;
+  const int nb = (int)a.nb;
+
+  // zero the histograms
+  {
+    ulonglong2 *z = reinterpret_cast<ulonglong2 *>(sm);
+    const uint32_t nz = (a.F * a.region) / 2;
+    for (uint32_t k = tid; k < nz; k += kThreads) z[k] = make_ulonglong2(0ull, 0ull);
+  }
+  __syncthreads();
+
+  // ---- fold
+  const int32_t *Xq = a.X + (size_t)q * a.n;
+  const int CB = a.CB;
+  if (MODE != 2) {
+    const ulonglong2 *ABq = a.AB + (size_t)q * a.ab_stride;
+    const int shift = 64 - a.lognb;
+    for (uint32_t k = tid; k < a.n; k += kThreads) {
+      const int32_t xq = __ldg(Xq + k);
+      if (xq == kMasked) continue;
+      const ulonglong2 ab = ABq[k];
+      const unsigned long long inc = ((unsigned long long)(long long)xq << CB) | 1ull;
+      unsigned long long ph = ab.x + (unsigned long long)j0 * ab.y;
+      unsigned long long *h = sm;
+      for (uint32_t f = 0; f < nfrem; ++f) {
+        const uint32_t bin = MODE == 0 ? (uint32_t)(ph >> shift) : (uint32_t)__umul64hi(ph, (unsigned long long)nb);
+        atomicAdd(h + bin, inc);
+        ph += ab.y;
+        h += a.region;
+      }
+    }
+  } else {
+    const float *Tq = a.T + (size_t)q * a.t_stride;
+    const float nbf = (float)nb;
+    const bool f0_nofma = a.flags & GTRAP_BLS_REF_F0_NOFMA;
+    const bool ph_fma = a.flags & GTRAP_BLS_REF_PH_FMA;
+    for (uint32_t k = tid; k < a.n; k += kThreads) {
+      const int32_t xq = __ldg(Xq + k);
+      if (xq == kMasked) continue;
+      const float t = __ldg(Tq + k);
+      const unsigned long long inc = ((unsigned long long)(long long)xq << CB) | 1ull;
+      unsigned long long *h = sm;
+      for (uint32_t f = 0; f < nfrem; ++f) {
+        const float jf = (float)(j0 + f);
+        const float f0 = f0_nofma ? __fadd_rn(a.fmin, __fmul_rn(a.df, jf)) : __fmaf_rn(a.df, jf, a.fmin);
+        const float p = __fmul_rn(t, f0);
+        const float ip = __int2float_rn(__float2int_rz(p));
+        const float ph = ph_fma ? __fmaf_rn(t, f0, -ip) : __fsub_rn(p, ip);
+        const uint32_t bin = __float2uint_rz(__fmul_rn(nbf, ph));
+        if (bin < (uint32_t)nb) atomicAdd(h + bin, inc);  // bin == nb is overwritten by the wrap in the reference
+        h += a.region;
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---- scan, one frequency per group per round
+  const int Tg = (int)a.Tg;
+  const int g = tid / Tg;
+  const int gtid = tid - g * Tg;
+  const int warp = tid >> 5, lane = tid & 31;
+  const int gw0 = (g * Tg) >> 5;           // first warp of this group
+  const int nwg = Tg >> 5;                 // warps in the group
+  const int kma = (int)a.kma, kmi = (int)a.kmi;
+  const float kkmi_f = (float)a.kkmi;
+  const float Nf = a.ntrue ? (float)a.ntrue[q] : (float)a.n_den;
+  const unsigned long long cmask = (1ull << CB) - 1ull;
+  const int i0 = gtid * R;
+  const int rounds = (int)((nfrem + a.G - 1) / a.G);
+
+  for (int rd = 0; rd < rounds; ++rd) {
+    const uint32_t f = (uint32_t)rd * a.G + g;
+    if (f >= nfrem || g >= (int)a.G) continue;
+    unsigned long long *H = sm + (size_t)f * a.region;
+    float2 *P = reinterpret_cast<float2 *>(H);
+
+    unsigned long long hv[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) hv[r] = (i0 + r < nb) ? H[i0 + r] : 0ull;
+    group_bar(1 + g, Tg);
+
+    long long px[R];
+    int pc[R];
+    long long sxv = 0;
+    int scv = 0;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      sxv += (long long)hv[r] >> CB;
+      scv += (int)(hv[r] & cmask);
+      px[r] = sxv;
+      pc[r] = scv;
+    }
+    // inclusive warp scan of the thread totals
+    long long wx = sxv;
+    int wc = scv;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long ux = __shfl_up_sync(0xffffffffu, wx, o);
+      const int uc = __shfl_up_sync(0xffffffffu, wc, o);
+      if (lane >= o) { wx += ux; wc += uc; }
+    }
+    if (lane == 31) { scan_x[warp] = wx; scan_c[warp] = wc; }
+    group_bar(1 + g, Tg);
+    long long ex = wx - sxv, tx = 0;
+    int ec = wc - scv, tc = 0;
+    for (int w = 0; w < nwg; ++w) {
+      const long long vx = scan_x[gw0 + w];
+      const int vc = scan_c[gw0 + w];
+      if (gw0 + w < warp) { ex += vx; ec += vc; }
+      tx += vx;
+      tc += vc;
+    }
+    // exclusive prefix at the R start bins, then the padded prefix array
+    float ys[R], cs[R], ncs[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const long long xr = ex + (r ? px[r - 1] : 0);
+      const int cr = ec + (r ? pc[r - 1] : 0);
+      const bool ok = i0 + r < nb;
+      ys[r] = __ll2float_rn(xr);
+      cs[r] = ok ? (float)cr : 3.0e38f;  // start beyond nb: kk < 0, never accepted
+      ncs[r] = Nf + (float)cr;
+    }
+    if (gtid == 0) P[0] = make_float2(0.0f, 0.0f);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int e = i0 + r + 1;
+      if (e <= nb) {
+        P[padi<R>(e)] = make_float2(__ll2float_rn(ex + px[r]), (float)(ec + pc[r]));
+        if (e <= kma) P[padi<R>(nb + e)] = make_float2(__ll2float_rn(tx + ex + px[r]), (float)(tc + ec + pc[r]));
+      }
+    }
+    group_bar(1 + g, Tg);
+
+    // candidate windows [i, e): i = i0 + r, e - i in (kmi, kma]
+    float bpow = 0.0f, blo = 0.0f;
+    int bi = INT_MAX, be = INT_MAX;
+    if (i0 < nb && kma > kmi) {
+      const int ebeg = i0 + kmi + 1;
+      const int eend = min(i0 + R - 1 + kma, nb + kma);
+      for (int e = ebeg; e <= eend; ++e) {
+        const float2 Pe = P[padi<R>(e)];
+        const unsigned base = (unsigned)(e - i0 - kmi - 1);
+        bool any = false;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const float s = Pe.x - ys[r];
+          const float kk = Pe.y - cs[r];
+          const float den = kk * (ncs[r] - Pe.y);
+          const float t = fmaf(-blo, den, s * s);
+          any |= (base - (unsigned)r < (unsigned)(kma - kmi)) & (kk > kkmi_f) & (t >= 0.0f);
+        }
+        if (any) {
+#pragma unroll
+          for (int r = 0; r < R; ++r) {
+            const float s = Pe.x - ys[r];
+            const float kk = Pe.y - cs[r];
+            const float den = kk * (ncs[r] - Pe.y);
+            const float s2 = s * s;
+            const float t = fmaf(-blo, den, s2);
+            if ((base - (unsigned)r < (unsigned)(kma - kmi)) && (kk > kkmi_f) && (t >= 0.0f)) {
+              const float pw = __fdiv_rn(s2, den);
+              if (pw > 0.0f && better(pw, i0 + r, e, bpow, bi, be)) {
+                bpow = pw;
+                bi = i0 + r;
+                be = e;
+                blo = bpow * (1.0f - 1.0f / 1048576.0f);
+              }
+            }
+          }
+        }
+      }
+    }
+    // group reduction (max power, then lowest start, then lowest end)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float op = __shfl_down_sync(0xffffffffu, bpow, o);
+      const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+      const int oe = __shfl_down_sync(0xffffffffu, be, o);
+      if (better(op, oi, oe, bpow, bi, be)) { bpow = op; bi = oi; be = oe; }
+    }
+    if (lane == 0) { red_p[warp] = bpow; red_i[warp] = bi; red_e[warp] = be; }
+    group_bar(1 + g, Tg);
+    if (gtid == 0) {
+      for (int w = 1; w < nwg; ++w) {
+        const float op = red_p[gw0 + w];
+        const int oi = red_i[gw0 + w], oe = red_e[gw0 + w];
+        if (better(op, oi, oe, bpow, bi, be)) { bpow = op; bi = oi; be = oe; }
+      }
+      const size_t o = (size_t)q * a.nf + j0 + f;
+      const bool found = bi != INT_MAX;
+      a.blsp[o] = found ? ldexpf(sqrtf(bpow), -a.sx[q]) : 0.0f;
+      if (a.ph1) a.ph1[o] = found ? (uint32_t)bi : 0u;
+      if (a.ph2) a.ph2[o] = found ? (uint32_t)(be - 1) : 0u;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+
+struct Plan {
+  uint32_t F, region, Tg, G, tiles;
+  int R;
+  size_t smem;
+};
+
+int make_plan(uint32_t nb, uint32_t kma, uint32_t nf, Plan *p) {
+  const int R = nb <= 4096 ? 8 : 16;
+  const int logR = R == 16 ? 4 : 3;
+  uint32_t Tg = (nb + R - 1) / R;
+  Tg = (Tg + 31) / 32 * 32;
+  if (Tg < 64) Tg = 64;  // at most 8 groups: named barriers 1..8
+  const uint32_t last = nb + kma;
+  uint32_t region = last + (last >> logR) + 1;
+  if (region < nb) region = nb;
+  region = (region + 1) & ~1u;  // 16-byte multiple for the zero fill
+  const uint32_t G = kThreads / Tg;
+  const size_t per_f = (size_t)region * 8;
+  // Frequencies per block: fill about half an SM's shared memory so two blocks can
+  // overlap their fold and scan phases; at least one round of groups.
+  const size_t budget = 110 * 1024;
+  uint32_t F = (uint32_t)(budget / per_f);
+  if (F < G) F = G;
+  if (F > 64) F = 64;
+  F = F / G * G;
+  if (F == 0) F = G;
+  const char *env = getenv("GTRAP_BLS_F");
+  if (env && atoi(env) > 0) F = (uint32_t)atoi(env);
+  if (F > nf) F = nf;
+  if ((size_t)F * per_f > (size_t)gtrap::max_smem_optin()) {
+    F = (uint32_t)((size_t)gtrap::max_smem_optin() / per_f);
+    if (F == 0) return fail(GTRAP_ERR_INVALID_ARG, "geebls: nb=%u, kma=%u do not fit in shared memory", nb, kma);
+  }
+  p->F = F;
+  p->region = region;
+  p->Tg = Tg;
+  p->G = G;
+  p->R = R;
+  p->tiles = (nf + F - 1) / F;
+  p->smem = (size_t)F * per_f;
+  return GTRAP_OK;
+}
+
+size_t ws_size(uint32_t n, uint32_t nq, uint32_t flags, bool full) {
+  const bool exact = !(flags & GTRAP_BLS_PHASE_FP32_REF);
+  size_t s = gtrap::align256((size_t)nq * 4);                 // sx
+  s += gtrap::align256((size_t)nq * n * 4);                     // X
+  if (full) s += gtrap::align256((size_t)nq * n * (exact ? 16 : 4));
+  else if (exact) s += gtrap::align256((size_t)n * 16);
+  return s + 256;
+}
+
+int run_bls(bool full, float *blsp, uint32_t *phase1, uint32_t *phase2, const float *lc,
+            const float *tu, const float *offset, const uint32_t *ntrue, uint32_t n, uint32_t nq,
+            uint32_t nf, uint32_t nb, uint32_t kma, uint32_t kmi, uint32_t kkmi, float fmin,
+            float df, uint32_t flags, uint32_t ref_nthread, void *workspace,
+            size_t workspace_bytes, cudaStream_t stream) {
+  const char *name = full ? "geebls" : "geebls_simple";
+  if (nq == 0 || nf == 0) return GTRAP_OK;
+  if (!blsp || !lc || !tu) return fail(GTRAP_ERR_INVALID_ARG, "%s: null pointer", name);
+  if (full && (!offset || !ntrue)) return fail(GTRAP_ERR_INVALID_ARG, "%s: offset and ntrue are required", name);
+  if (n == 0 || n >= (1u << 23)) return fail(GTRAP_ERR_INVALID_ARG, "%s: n=%u must be in [1, 2^23)", name, n);
+  if (nb == 0 || nb > (uint32_t)kMaxNb) return fail(GTRAP_ERR_INVALID_ARG, "%s: nb=%u must be in [1, %d]", name, nb, kMaxNb);
+  if (kma == 0 || kma > nb) return fail(GTRAP_ERR_INVALID_ARG, "%s: kma=%u must be in [1, nb]", name, kma);
+  if ((uint64_t)nq * nf >= (1ull << 40)) return fail(GTRAP_ERR_INVALID_ARG, "%s: nq*nf too large", name);
+  const bool exact = !(flags & GTRAP_BLS_PHASE_FP32_REF);
+  if (!exact && !full) {
+    // FP32-reference phase of the plain kernel folds the common time array directly.
+  }
+  if (ref_nthread && !exact && kma > ref_nthread)
+    return fail(GTRAP_ERR_INVALID_ARG, "%s: reference wrap needs kma <= nthread (%u > %u)", name, kma, ref_nthread);
+  const uint32_t kmi_eff = kmi < 1 ? 1 : kmi;        // include/geebls.h:26-28
+  const uint32_t kkmi_eff = kkmi < 5 ? 5 : kkmi;     // MINBIN, include/geebls.h:31-33
+  const uint32_t n_eff = ref_nthread ? (n / ref_nthread) * ref_nthread : n;  // include/geebls.h:57
+
+  if (!workspace || ((uintptr_t)workspace & 255))
+    return fail(GTRAP_ERR_WORKSPACE, "%s: workspace must be a 256-byte aligned device pointer", name);
+  const size_t need = ws_size(n, nq, flags, full);
+  if (workspace_bytes < need)
+    return fail(GTRAP_ERR_WORKSPACE, "%s: workspace of %zu bytes, %zu needed", name, workspace_bytes, need);
+  gtrap::Carver cv{(char *)workspace, workspace_bytes, 0};
+  int32_t *sx = cv.take<int32_t>(nq);
+  int32_t *X = cv.take<int32_t>((size_t)nq * n);
+  ulonglong2 *AB = nullptr;
+  float *T = nullptr;
+  if (full) {
+    if (exact) AB = cv.take<ulonglong2>((size_t)nq * n);
+    else T = cv.take<float>((size_t)nq * n);
+  } else if (exact) {
+    AB = cv.take<ulonglong2>(n);
+  }
+
+  const int CB = gtrap::ilog2u(n) + 1;  // count field: counts <= n < 2^CB
+  double xq_max = ldexp(1.0, 62 - CB) / (double)n;
+  if (xq_max > 2147483647.0) xq_max = 2147483647.0;
+
+  PrepArgs pa;
+  pa.lc = lc; pa.tu = tu; pa.offset = full ? offset : nullptr;
+  pa.sx = sx; pa.X = X; pa.AB = AB; pa.T = T;
+  pa.n = n; pa.nq = nq; pa.n_eff = n_eff;
+  pa.fmin = fmin; pa.df = df; pa.xq_max = xq_max;
+  pa.full = full ? 1 : 0; pa.exact = exact ? 1 : 0;
+  bls_scale_kernel<<<(nq + 31) / 32, dim3(32, 32), 0, stream>>>(pa);
+  GTRAP_TRY(gtrap::check_launch("bls_scale_kernel"));
+  bls_pack_kernel<<<dim3((nq + 31) / 32, (n + 31) / 32), dim3(32, 8), 0, stream>>>(pa);
+  GTRAP_TRY(gtrap::check_launch("bls_pack_kernel"));
+  if (!full && exact) {
+    bls_common_phase_kernel<<<(n + 255) / 256, 256, 0, stream>>>(tu, AB, n, fmin, df);
+    GTRAP_TRY(gtrap::check_launch("bls_common_phase_kernel"));
+  }
+
+  Plan p;
+  GTRAP_TRY(make_plan(nb, kma, nf, &p));
+  BlsArgs ba;
+  ba.blsp = blsp; ba.ph1 = phase1; ba.ph2 = phase2;
+  ba.X = X; ba.AB = AB; ba.T = full ? T : tu; ba.sx = sx; ba.ntrue = full ? ntrue : nullptr;
+  ba.n = n; ba.n_den = n; ba.nq = nq; ba.nf = nf; ba.nb = nb; ba.kma = kma;
+  ba.kmi = kmi_eff; ba.kkmi = kkmi_eff; ba.fmin = fmin; ba.df = df;
+  ba.F = p.F; ba.tiles = p.tiles; ba.region = p.region; ba.Tg = p.Tg; ba.G = p.G;
+  ba.lognb = gtrap::is_pow2(nb) ? gtrap::ilog2u(nb) : 0;
+  ba.CB = CB;
+  ba.ab_stride = full ? n : 0;
+  ba.t_stride = full ? n : 0;
+  ba.flags = flags;
+  if (kmi_eff >= kma) {
+    // no admissible width: every SR is zero (reference: power stays 0)
+  }
+  const uint64_t blocks = (uint64_t)p.tiles * nq;
+  if (blocks >= (1ull << 31)) return fail(GTRAP_ERR_INVALID_ARG, "%s: grid too large", name);
+  const void *fn;
+  const int mode = !exact ? 2 : (gtrap::is_pow2(nb) ? 0 : 1);
+#define GTRAP_BLS_LAUNCH(RR, MM)                                                          \
+  fn = (const void *)bls_fold_scan_kernel<RR, MM>;                                         \
+  GTRAP_TRY(gtrap::ensure_smem(fn, p.smem, name));                                         \
+  bls_fold_scan_kernel<RR, MM><<<(unsigned)blocks, kThreads, p.smem, stream>>>(ba);
+  if (p.R == 8) {
+    if (mode == 0) { GTRAP_BLS_LAUNCH(8, 0) } else if (mode == 1) { GTRAP_BLS_LAUNCH(8, 1) } else { GTRAP_BLS_LAUNCH(8, 2) }
+  } else {
+    if (mode == 0) { GTRAP_BLS_LAUNCH(16, 0) } else if (mode == 1) { GTRAP_BLS_LAUNCH(16, 1) } else { GTRAP_BLS_LAUNCH(16, 2) }
+  }
+#undef GTRAP_BLS_LAUNCH
+  return gtrap::check_launch("bls_fold_scan_kernel");
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t gtrap_geebls_workspace_size(uint32_t n, uint32_t nq, uint32_t flags) {
+  return ws_size(n, nq, flags, true);
+}
+
+size_t gtrap_geebls_simple_workspace_size(uint32_t n, uint32_t nq, uint32_t flags) {
+  return ws_size(n, nq, flags, false);
+}
+
+int gtrap_geebls(float *blsp, uint32_t *phase1, uint32_t *phase2, const float *lc,
+                 const float *tu, const float *offset, const uint32_t *ntrue, uint32_t n,
+                 uint32_t nq, uint32_t nf, uint32_t nb, uint32_t kma, uint32_t kmi,
+                 uint32_t kkmi, float fmin, float df, uint32_t flags, uint32_t ref_nthread,
+                 void *workspace, size_t workspace_bytes, gtrap_stream_t stream) {
+  return run_bls(true, blsp, phase1, phase2, lc, tu, offset, ntrue, n, nq, nf, nb, kma, kmi,
+                 kkmi, fmin, df, flags, ref_nthread, workspace, workspace_bytes, stream);
+}
+
+int gtrap_geebls_simple(float *blsp, uint32_t *phase1, uint32_t *phase2, const float *lc,
+                        const float *tu, uint32_t n, uint32_t nq, uint32_t nf, uint32_t nb,
+                        uint32_t kma, uint32_t kmi, uint32_t kkmi, float fmin, float df,
+                        uint32_t flags, uint32_t ref_nthread, void *workspace,
+                        size_t workspace_bytes, gtrap_stream_t stream) {
+  return run_bls(false, blsp, phase1, phase2, lc, tu, nullptr, nullptr, n, nq, nf, nb, kma,
+                 kmi, kkmi, fmin, df, flags, ref_nthread, workspace, workspace_bytes, stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,111 @@
+// Library-wide C ABI pieces: error reporting, version, device attribute caches and the
+// FP32 issue-rate probe used for roofline denominators.
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+#include <mutex>
+
+#include "common.cuh"
+
+namespace gtrap {
+
+namespace {
+thread_local char g_last_error[512] = "no error";
+
+constexpr int kMaxDevices = 64;
+int g_sm_count[kMaxDevices];
+int g_smem_optin[kMaxDevices];
+std::mutex g_attr_mutex;
+
+int current_device() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  return dev < kMaxDevices ? dev : 0;
+}
+}  // namespace
+
+int fail(int code, const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+int check_launch(const char *what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(GTRAP_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  return GTRAP_OK;
+}
+
+int sm_count() {
+  int dev = current_device();
+  if (!g_sm_count[dev]) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    g_sm_count[dev] = v > 0 ? v : 1;
+  }
+  return g_sm_count[dev];
+}
+
+int max_smem_optin() {
+  int dev = current_device();
+  if (!g_smem_optin[dev]) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    g_smem_optin[dev] = v > 0 ? v : 48 * 1024;
+  }
+  return g_smem_optin[dev];
+}
+
+int ensure_smem(const void *func, size_t bytes, const char *what) {
+  if (bytes <= 48 * 1024) return GTRAP_OK;
+  if (bytes > (size_t)max_smem_optin())
+    return fail(GTRAP_ERR_INVALID_ARG, "%s: needs %zu bytes of shared memory, device allows %d",
+                what, bytes, max_smem_optin());
+  // The attribute is per function and per device; setting it again is harmless, and
+  // the call is cheap next to a launch, so it is simply repeated (also during capture).
+  std::lock_guard<std::mutex> lock(g_attr_mutex);
+  cudaError_t e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)bytes);
+  if (e != cudaSuccess)
+    return fail(GTRAP_ERR_CUDA, "%s: cudaFuncSetAttribute: %s", what, cudaGetErrorString(e));
+  return GTRAP_OK;
+}
+
+}  // namespace gtrap
+
+namespace {
+// Each thread runs 8 independent FMA chains so the FP32 pipe, not latency, limits it.
+__global__ void __launch_bounds__(256) fp32_probe_kernel(float *sink, uint32_t iters) {
+  float a0 = threadIdx.x * 1e-7f, a1 = a0 + 1e-7f, a2 = a0 + 2e-7f, a3 = a0 + 3e-7f;
+  float a4 = a0 + 4e-7f, a5 = a0 + 5e-7f, a6 = a0 + 6e-7f, a7 = a0 + 7e-7f;
+  const float m = 0.999999f, c = 1e-7f;
+  for (uint32_t it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      a0 = fmaf(a0, m, c); a1 = fmaf(a1, m, c); a2 = fmaf(a2, m, c); a3 = fmaf(a3, m, c);
+      a4 = fmaf(a4, m, c); a5 = fmaf(a5, m, c); a6 = fmaf(a6, m, c); a7 = fmaf(a7, m, c);
+    }
+  }
+  float s = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
+  if (s == 1234.5f) sink[blockIdx.x * blockDim.x + threadIdx.x] = s;  // never true; keeps the work
+}
+}  // namespace
+
+extern "C" {
+
+const char *gtrap_last_error(void) { return gtrap::g_last_error; }
+
+int gtrap_version(void) { return 100; /* 0.1.0 */ }
+
+int gtrap_probe_fp32_peak(float *sink, uint32_t iters, double *flops, gtrap_stream_t stream) {
+  if (!sink || iters == 0) return gtrap::fail(GTRAP_ERR_INVALID_ARG, "probe: bad arguments");
+  const int threads = 256;
+  const int blocks = gtrap::sm_count() * 8;
+  fp32_probe_kernel<<<blocks, threads, 0, stream>>>(sink, iters);
+  if (flops) *flops = 2.0 * 8.0 * 16.0 * (double)iters * threads * blocks;
+  return gtrap::check_launch("fp32_probe_kernel");
+}
+
+}  // extern "C"

@@ -1,0 +1,59 @@
+// Shared helpers for the gtrap_gb300 CUDA sources: status handling, launch checks,
+// device-attribute caches and small integer utilities.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+
+#include "../../include/gtrap_gb300.h"
+
+namespace gtrap {
+
+// Record a formatted message as the calling thread's last error and return `code`.
+int fail(int code, const char *fmt, ...);
+
+// Check the most recent launch on this thread; returns GTRAP_OK or GTRAP_ERR_CUDA.
+int check_launch(const char *what);
+
+// Number of SMs of the current device (cached per device).
+int sm_count();
+
+// Maximum opt-in dynamic shared memory per block of the current device (cached).
+int max_smem_optin();
+
+// Raise the dynamic shared-memory limit of `func` to `bytes` once per device.
+int ensure_smem(const void *func, size_t bytes, const char *what);
+
+// Workspace carving: returns the next 256-byte aligned slice or nullptr.
+struct Carver {
+  char *base;
+  size_t size;
+  size_t used;
+  template <typename T>
+  T *take(size_t count) {
+    size_t off = (used + 255) & ~size_t(255);
+    size_t bytes = count * sizeof(T);
+    if (off + bytes > size) return nullptr;
+    used = off + bytes;
+    return reinterpret_cast<T *>(base + off);
+  }
+};
+
+inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+inline bool is_pow2(uint32_t x) { return x && !(x & (x - 1)); }
+
+inline int ilog2u(uint32_t x) {
+  int l = 0;
+  while ((1u << (l + 1)) <= x && l < 31) ++l;
+  return l;
+}
+
+}  // namespace gtrap
+
+#define GTRAP_TRY(expr)          \
+  do {                           \
+    int _st = (expr);            \
+    if (_st != GTRAP_OK) return _st; \
+  } while (0)

@@ -1,0 +1,170 @@
+// Median-filter detrend (gfilter) and per-curve offset (get_offset).
+//
+// Reference behaviour: gtrap/gfilter.py:13-86 computes, for every sample, the exact
+// (r+1)-th order statistic of the zero-padded window x[i-r .. i+r] by bisection over
+// the window values and writes x[i] - median.  Here every warp owns 32 adjacent curves
+// (one per lane, so each row it touches is one coalesced 128-byte line of the
+// [n, nq] image) and a run of consecutive rows.  Each lane keeps its window sorted in
+// shared memory, laid out [rank][lane] so that every access is bank-conflict free, and
+// slides it one row at a time: the leaving value is located by binary search and the
+// entering value is moved into place by shifting the values between the two.  The
+// median is then the element of rank r.  Work per output is O(displacement) instead
+// of O(window * bisection steps), and the result is the same order statistic, so the
+// residual is bit-identical to the reference's and to scipy.signal.medfilt.
+#include "common.cuh"
+
+namespace {
+
+__device__ __forceinline__ float load_padded(const float *__restrict__ in, long long i, long long n,
+                                             size_t nq, int q, bool qok) {
+  return (qok && i >= 0 && i < n) ? __ldg(in + (size_t)i * nq + q) : 0.0f;
+}
+
+__global__ void __launch_bounds__(256) gfilter_kernel(const float *__restrict__ in,
+                                                      float *__restrict__ out, int n, int nq,
+                                                      int r, int rows_per_warp) {
+  extern __shared__ float sorted_windows[];
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int w = 2 * r + 1;
+  float *S = sorted_windows + (size_t)warp * w * 32 + lane;  // rank k lives at S[32 * k]
+  const int q = blockIdx.x * 32 + lane;
+  const bool qok = q < nq;
+  const long long row0 = ((long long)blockIdx.y * (blockDim.x >> 5) + warp) * rows_per_warp;
+  if (row0 >= n) return;
+  const long long row1 = min((long long)n, row0 + rows_per_warp);
+  const size_t stride = (size_t)nq;
+
+  // Sorted window of the first output row (insertion sort; amortised over the run).
+  for (int k = 0; k < w; ++k) {
+    const float v = load_padded(in, row0 - r + k, n, stride, q, qok);
+    int j = k;
+    while (j > 0) {
+      const float u = S[32 * (j - 1)];
+      if (u <= v) break;
+      S[32 * j] = u;
+      --j;
+    }
+    S[32 * j] = v;
+  }
+
+  for (long long i = row0; i < row1; ++i) {
+    const float med = S[32 * r];
+    if (qok) out[(size_t)i * stride + q] = __fsub_rn(__ldg(in + (size_t)i * stride + q), med);
+    if (i + 1 >= row1) break;
+    const float vold = load_padded(in, i - r, n, stride, q, qok);
+    const float vnew = load_padded(in, i + r + 1, n, stride, q, qok);
+    if (vnew == vold) continue;
+    // Lowest rank holding the leaving value (present in the window by construction).
+    int lo = 0, hi = w - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (S[32 * mid] < vold) lo = mid + 1; else hi = mid;
+    }
+    int j = lo;
+    if (vnew > vold) {
+      while (j + 1 < w) {
+        const float u = S[32 * (j + 1)];
+        if (!(u < vnew)) break;
+        S[32 * j] = u;
+        ++j;
+      }
+    } else {
+      while (j > 0) {
+        const float u = S[32 * (j - 1)];
+        if (!(u > vnew)) break;
+        S[32 * j] = u;
+        --j;
+      }
+    }
+    S[32 * j] = vnew;
+  }
+}
+
+// offset[q] = sum of resid over samples whose time is not negative, divided by n.
+// One block per 32 curves; each of the 32 warps sums every 32nd row with Neumaier
+// compensation; the 32 partials are combined in a fixed order (deterministic).
+__global__ void __launch_bounds__(1024) offset_kernel(const float *__restrict__ resid,
+                                                      const float *__restrict__ tu,
+                                                      float *__restrict__ offset, int n, int nq) {
+  __shared__ double part[32][33];
+  const int lane = threadIdx.x, row = threadIdx.y;
+  const int q = blockIdx.x * 32 + lane;
+  float sum = 0.0f, comp = 0.0f;
+  if (q < nq) {
+    for (long long i = row; i < n; i += 32) {
+      const size_t idx = (size_t)i * nq + q;
+      const float t = __ldg(tu + idx);
+      if (!(t < 0.0f)) {
+        const float v = __ldg(resid + idx);
+        const float s = sum + v;
+        comp += (fabsf(sum) >= fabsf(v)) ? ((sum - s) + v) : ((v - s) + sum);
+        sum = s;
+      }
+    }
+  }
+  part[row][lane] = (double)sum + (double)comp;
+  __syncthreads();
+  if (row == 0 && q < nq) {
+    double s = 0.0;
+    for (int k = 0; k < 32; ++k) s += part[k][lane];
+    offset[q] = (float)(s / (double)n);
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int gtrap_gfilter(const float *in, float *out, uint32_t n, uint32_t nq, uint32_t r,
+                  gtrap_stream_t stream) {
+  using namespace gtrap;
+  if (n == 0 || nq == 0) return GTRAP_OK;
+  if (!in || !out) return fail(GTRAP_ERR_INVALID_ARG, "gfilter: null pointer");
+  if (in == out) return fail(GTRAP_ERR_INVALID_ARG, "gfilter: in and out must not alias");
+  if (n > 0x7fffffffu || nq > 0x7fffffffu)
+    return fail(GTRAP_ERR_INVALID_ARG, "gfilter: n and nq must be below 2^31");
+  const size_t w = 2 * (size_t)r + 1;
+  const size_t per_warp = w * 32 * sizeof(float);
+  const size_t budget = (size_t)max_smem_optin();
+  if (per_warp > budget)
+    return fail(GTRAP_ERR_INVALID_ARG, "gfilter: r=%u needs %zu bytes of shared memory per warp",
+                r, per_warp);
+  int warps = (int)(budget / per_warp);
+  if (warps > 8) warps = 8;
+  // Smaller windows afford more resident blocks: keep a block's share near 1/4 SM.
+  while (warps > 1 && per_warp * warps > 56 * 1024) --warps;
+  long long rows_per_warp = 8 * (long long)w;
+  if (rows_per_warp < 256) rows_per_warp = 256;
+  if (rows_per_warp > 4096) rows_per_warp = 4096;
+  // Keep enough warps for the GPU when there are few curve groups.
+  const long long groups = (nq + 31) / 32;
+  const long long want_warps = 8LL * sm_count() * 8;
+  while (rows_per_warp > 64 && groups * ((n + rows_per_warp - 1) / rows_per_warp) < want_warps)
+    rows_per_warp /= 2;
+  const long long rows_per_block = rows_per_warp * warps;
+  const long long gy = (n + rows_per_block - 1) / rows_per_block;
+  if (gy > 65535) rows_per_warp = (n + 65535LL * warps - 1) / (65535LL * warps);
+  const long long gy2 = (n + rows_per_warp * warps - 1) / (rows_per_warp * warps);
+  const size_t smem = per_warp * warps;
+  GTRAP_TRY(ensure_smem((const void *)gfilter_kernel, smem, "gfilter"));
+  dim3 grid((unsigned)groups, (unsigned)gy2);
+  gfilter_kernel<<<grid, 32 * warps, smem, stream>>>(in, out, (int)n, (int)nq, (int)r,
+                                                     (int)rows_per_warp);
+  return check_launch("gfilter_kernel");
+}
+
+int gtrap_offset(const float *resid, const float *tu, float *offset, uint32_t n, uint32_t nq,
+                 gtrap_stream_t stream) {
+  using namespace gtrap;
+  if (nq == 0) return GTRAP_OK;
+  if (!resid || !tu || !offset) return fail(GTRAP_ERR_INVALID_ARG, "offset: null pointer");
+  if (n == 0) return fail(GTRAP_ERR_INVALID_ARG, "offset: n must be positive");
+  if (n > 0x7fffffffu || nq > 0x7fffffffu)
+    return fail(GTRAP_ERR_INVALID_ARG, "offset: n and nq must be below 2^31");
+  dim3 block(32, 32);
+  offset_kernel<<<(nq + 31) / 32, block, 0, stream>>>(resid, tu, offset, (int)n, (int)nq);
+  return check_launch("offset_kernel");
+}
+
+}  // extern "C"

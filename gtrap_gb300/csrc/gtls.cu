@@ -1,0 +1,378 @@
+// Trapezoid least-squares single-event search (gtls).
+//
+// Reference behaviour (include/gtls_simple.h:1-406, include/gtls_absolute.h:1-408): one
+// CTA per (epoch e, curve q) and one thread per trapezoid width W = wmax - dw*w gathers
+// the nsc-sample scoop around sample e, shifts times by deltat*e, and for nl ingress
+// widths L scans the scoop five times to sum the regions A (tStart, tAB], B (tAB, tBC],
+// C (tBC, tCD], D (tCD, tDE], E (tDE, tEnd] (tAB = -W/4 - L/2, tBC = -W/4 + L/2,
+// tCD = -tBC, tDE = -tAB), forms the closed-form depth H = -numB/denA and chi^2, and
+// keeps the best S/N = H/sqrt(chi^2/(N-3)) of windows whose fill factor exceeds 0.75.
+// Cost: O(nl * window) per thread, and the CTA has only nw threads.
+//
+// GB300 design: a CTA covers 32 consecutive epochs (one per lane) of one curve; its
+// warps take widths in turn, so the lanes of a warp share W and do the same amount of
+// work.  The union of the 32 scoops is staged once in shared memory (times rounded
+// through (t + 1000) - 1000 exactly as the reference's scoop gather does), with exact
+// count prefixes and double-float prefix sums of x and x^2.  For each (epoch, width):
+//  * binary searches give the window [tStart, tEnd] (mean), the A..E range and the two
+//    ingress centres; the fill factor depends only on (e, W), so failing widths are
+//    skipped whole;
+//  * as L grows, regions B and D only grow outwards from -W/4 and +W/4, so four
+//    pointers walk outwards adding each new sample once; B and D are accumulated in
+//    centred coordinates u = t + W/4, v = t - W/4, which gives denA and numB without
+//    the W^2 cancellation of the raw-moment form;
+//  * C and A+E come from the prefix sums, chi^2 from the moment expansion.
+// Region membership is decided with the reference's float32 time and boundary
+// arithmetic, so the regions are the reference's regions; the sums are more accurate
+// than its float32 running sums.
+#include "common.cuh"
+
+#include <climits>
+
+namespace {
+
+using gtrap::fail;
+
+constexpr int kWarps = 8;
+constexpr int kTlsThreads = kWarps * 32;
+constexpr int kMaxStage = 7000;  // staged samples: nsc + 31
+
+struct TlsArgs {
+  float *sn, *w, *t0, *l, *h;
+  const float *lc, *tu;
+  int nt, nq, nw, nl, nsc;
+  float wmax, dw, deltat;
+  int mode;          // 0: simple, 1: absolute
+  int w_fma, t_fma;  // float32 contraction choices (see GTRAP_TLS_*_NOFMA)
+  int tiles;         // epoch tiles per curve
+};
+
+struct DF {  // double-float value hi + lo
+  float hi, lo;
+};
+
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+  const float s = __fadd_rn(a.hi, b.hi);
+  const float v = __fsub_rn(s, a.hi);
+  float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, v)), __fsub_rn(b.hi, v));
+  e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+  const float hi = __fadd_rn(s, e);
+  return DF{hi, __fsub_rn(e, __fsub_rn(hi, s))};
+}
+
+__device__ __forceinline__ DF df_from_prod(float x) {  // x*x exactly as hi + lo
+  const float p = __fmul_rn(x, x);
+  return DF{p, __fmaf_rn(x, x, -p)};
+}
+
+// (b - a) of two prefix values, rounded to float
+__device__ __forceinline__ float df_diff(float bh, float bl, float ah, float al) {
+  return __fadd_rn(__fsub_rn(bh, ah), __fsub_rn(bl, al));
+}
+
+__device__ __forceinline__ double df_diff_d(float bh, float bl, float ah, float al) {
+  return ((double)bh - (double)ah) + ((double)bl - (double)al);
+}
+
+__global__ void __launch_bounds__(kTlsThreads) gtls_kernel(const TlsArgs a) {
+  extern __shared__ __align__(16) float st[];
+  __shared__ float red_sn[kWarps][32], red_l[kWarps][32], red_h[kWarps][32];
+  __shared__ int red_w[kWarps][32];
+  __shared__ float xref;
+
+  const int item = blockIdx.x;
+  const int tile = item / a.nq;
+  const int q = item - tile * a.nq;
+  const int e0 = tile * 32;
+  const int nsch = a.nsc / 2;
+  // staged sample range [base, base + S) in sample indices, clipped to [0, nt)
+  const int first = e0 - nsch;
+  const int last = min(e0 + 31, a.nt - 1) - nsch + a.nsc;  // exclusive
+  const int base = max(first, 0);
+  const int S = max(0, min(last, a.nt) - base);
+
+  float *tq = st;                        // [S] shifted-search time (filled over masks)
+  float *xv = tq + S;                    // [S] x - xref (0 when masked)
+  int *cnt = (int *)(xv + S);            // [S+1] valid-count prefix
+  float *pxh = (float *)(cnt + S + 1);   // [S+1] prefix of x (hi, lo)
+  float *pxl = pxh + S + 1;
+  float *pqh = pxl + S + 1;              // [S+1] prefix of x^2 (hi, lo)
+  float *pql = pqh + S + 1;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+  // ---- stage the scoop union: (t + 1000) - 1000 rounding (include/gtls_simple.h:54-65)
+  for (int s = tid; s < S; s += kTlsThreads) {
+    const size_t idx = (size_t)(base + s) * a.nq + q;
+    const float tr = __ldg(a.tu + idx);
+    const float tqv = __fadd_rn(-1000.0f, __double2float_rn((double)tr + 1000.0));
+    const float x = __ldg(a.lc + idx);
+    const bool ok = tqv >= 0.0f;
+    tq[s] = ok ? tqv : -INFINITY;
+    xv[s] = ok ? x : 0.0f;
+    cnt[s] = ok ? 1 : 0;
+  }
+  __syncthreads();
+
+  // ---- serial-per-lane prefix scan in warp 0: forward fill of masked times, the
+  //      valid count and double-float sums of x - xref and (x - xref)^2
+  if (warp == 0) {
+    // reference level: mean of the valid staged values (makes the moments well conditioned)
+    float acc = 0.0f;
+    int n = 0;
+    for (int s = lane; s < S; s += 32) { acc += xv[s]; n += cnt[s]; }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      n += __shfl_xor_sync(0xffffffffu, n, o);
+    }
+    const float ref = n ? acc / (float)n : 0.0f;
+    if (lane == 0) xref = ref;
+    const int chunk = (S + 31) / 32;
+    const int s0 = min(S, lane * chunk), s1 = min(S, s0 + chunk);
+    int c = 0;
+    DF sx{0.0f, 0.0f}, sq{0.0f, 0.0f};
+    float lastt = -INFINITY;
+    for (int s = s0; s < s1; ++s) {
+      if (cnt[s]) {
+        const float xc = __fsub_rn(xv[s], ref);
+        xv[s] = xc;
+        c += 1;
+        sx = df_add(sx, DF{xc, 0.0f});
+        sq = df_add(sq, df_from_prod(xc));
+        lastt = tq[s];
+      }
+    }
+    // exclusive scan of the lane totals (count, sx, sq) and of the last valid time
+    int ec = c;
+    DF ex = sx, eq = sq;
+    float lt = lastt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int uc = __shfl_up_sync(0xffffffffu, ec, o);
+      const float uxh = __shfl_up_sync(0xffffffffu, ex.hi, o);
+      const float uxl = __shfl_up_sync(0xffffffffu, ex.lo, o);
+      const float uqh = __shfl_up_sync(0xffffffffu, eq.hi, o);
+      const float uql = __shfl_up_sync(0xffffffffu, eq.lo, o);
+      const float ut = __shfl_up_sync(0xffffffffu, lt, o);
+      if (lane >= o) {
+        ec += uc;
+        ex = df_add(DF{uxh, uxl}, ex);
+        eq = df_add(DF{uqh, uql}, eq);
+        lt = (lt == -INFINITY) ? ut : lt;
+      }
+    }
+    // convert inclusive to exclusive
+    int pc = __shfl_up_sync(0xffffffffu, ec, 1);
+    float pxh0 = __shfl_up_sync(0xffffffffu, ex.hi, 1), pxl0 = __shfl_up_sync(0xffffffffu, ex.lo, 1);
+    float pqh0 = __shfl_up_sync(0xffffffffu, eq.hi, 1), pql0 = __shfl_up_sync(0xffffffffu, eq.lo, 1);
+    float pt = __shfl_up_sync(0xffffffffu, lt, 1);
+    if (lane == 0) { pc = 0; pxh0 = pxl0 = pqh0 = pql0 = 0.0f; pt = -INFINITY; }
+    DF rx{pxh0, pxl0}, rq{pqh0, pql0};
+    int rc = pc;
+    float ft = pt;
+    for (int s = s0; s < s1; ++s) {
+      cnt[s] = rc;  // cnt becomes the exclusive prefix
+      pxh[s] = rx.hi; pxl[s] = rx.lo; pqh[s] = rq.hi; pql[s] = rq.lo;
+      if (tq[s] != -INFINITY) {
+        const float xc = xv[s];
+        rc += 1;
+        rx = df_add(rx, DF{xc, 0.0f});
+        rq = df_add(rq, df_from_prod(xc));
+        ft = tq[s];
+      } else {
+        tq[s] = ft;  // masked: previous valid time keeps the search predicate monotone
+      }
+    }
+    // the lane owning element S-1 (the only one with s1 == S and a non-empty chunk)
+    // writes the total at index S
+    if (s1 == S && s0 < s1) {
+      cnt[S] = rc; pxh[S] = rx.hi; pxl[S] = rx.lo; pqh[S] = rq.hi; pql[S] = rq.lo;
+    }
+    if (S == 0 && lane == 0) { cnt[0] = 0; pxh[0] = pxl[0] = pqh[0] = pql[0] = 0.0f; }
+  }
+  __syncthreads();
+
+  // ---- per (epoch, width)
+  const int e = e0 + lane;
+  const bool eok = e < a.nt;
+  const float ef = (float)e;
+  const float dte = __fmul_rn(a.deltat, ef);
+  const bool t_fma = a.t_fma;
+  auto tt = [&](int s) -> float {
+    const float v = tq[s];
+    return t_fma ? __fmaf_rn(-a.deltat, ef, v) : __fsub_rn(v, dte);
+  };
+  // scoop of epoch e in staged indices
+  const int lo = max(e - nsch, 0) - base;
+  const int hi = min(e - nsch + a.nsc, a.nt) - base;
+  auto ub = [&](float tau) -> int {  // first s in [lo, hi) with tt(s) > tau
+    int x0 = lo, x1 = hi;
+    while (x0 < x1) {
+      const int mid = (x0 + x1) >> 1;
+      if (tt(mid) > tau) x1 = mid; else x0 = mid + 1;
+    }
+    return x0;
+  };
+  auto lb = [&](float tau) -> int {  // first s in [lo, hi) with tt(s) >= tau
+    int x0 = lo, x1 = hi;
+    while (x0 < x1) {
+      const int mid = (x0 + x1) >> 1;
+      if (tt(mid) >= tau) x1 = mid; else x0 = mid + 1;
+    }
+    return x0;
+  };
+
+  float best_sn = 0.0f, best_l = 0.0f, best_h = 0.0f;
+  int best_w = INT_MAX;
+  const int nl = a.nl;
+  const float crit_w = a.deltat;
+
+  for (int wi = warp; wi < a.nw && eok && lo < hi; wi += kWarps) {
+    const float wf = (float)wi;
+    const float W = a.w_fma ? __fmaf_rn(-a.dw, wf, a.wmax) : __fsub_rn(a.wmax, __fmul_rn(a.dw, wf));
+    if (!(W > 0.0f)) continue;
+    const float tStart = -0.5f * W, tEnd = 0.5f * W;
+    const int ubS = ub(tStart), lbS = lb(tStart), ubE = ub(tEnd);
+    const int N = cnt[ubE] - cnt[ubS];
+    // fill factor (include/gtls_simple.h:308-311) depends only on (e, W)
+    const float filfac = __fdiv_rn((float)N, __fdiv_rn(W, crit_w));
+    if (!(filfac > 0.75f)) continue;
+    const int Nw = cnt[ubE] - cnt[lbS];
+    const float m = Nw > 0 ? __fdiv_rn(df_diff(pxh[ubE], pxl[ubE], pxh[lbS], pxl[lbS]), (float)Nw) : 0.0f;
+    const float SxAE = df_diff(pxh[ubE], pxl[ubE], pxh[ubS], pxl[ubS]);
+    const double SS = df_diff_d(pqh[ubE], pql[ubE], pqh[ubS], pql[ubS]) -
+                      2.0 * (double)m * (double)SxAE + (double)m * (double)m * (double)N;
+    const float SSf = (float)SS;
+    const double Wd = (double)W;
+    const float dl = a.mode ? __double2float_rn(Wd / 4.0 / (double)nl)
+                            : __double2float_rn(Wd * 0.45 / (double)nl);
+    const float Wq = 0.25f * W;  // exact
+    int bL = ub(-Wq), bR = bL;
+    int dL = ub(Wq), dR = dL;
+    int nB = 0, nD = 0;
+    float xB = 0.f, uB = 0.f, xuB = 0.f, uuB = 0.f;
+    float xD = 0.f, vD = 0.f, xvD = 0.f, vvD = 0.f;
+    for (int mm = 0; mm < nl; ++mm) {
+      const float L = __fmul_rn((float)(a.mode ? mm + 1 : mm), dl);
+      const double Ld = (double)L;
+      const float tAB = __double2float_rn(-Wd * 0.25 - Ld * 0.5);
+      const float tBC = __double2float_rn(-Wd * 0.25 + Ld * 0.5);
+      const float tCD = -tBC, tDE = -tAB;
+      while (bL > lo && tt(bL - 1) > tAB) {
+        --bL;
+        if (cnt[bL + 1] != cnt[bL]) {
+          const float x = xv[bL], u = __fadd_rn(tt(bL), Wq);
+          ++nB; xB += x; uB += u; xuB = fmaf(x, u, xuB); uuB = fmaf(u, u, uuB);
+        }
+      }
+      while (bR < hi && !(tt(bR) > tBC)) {
+        if (cnt[bR + 1] != cnt[bR]) {
+          const float x = xv[bR], u = __fadd_rn(tt(bR), Wq);
+          ++nB; xB += x; uB += u; xuB = fmaf(x, u, xuB); uuB = fmaf(u, u, uuB);
+        }
+        ++bR;
+      }
+      while (dL > lo && tt(dL - 1) > tCD) {
+        --dL;
+        if (cnt[dL + 1] != cnt[dL]) {
+          const float x = xv[dL], v = __fsub_rn(tt(dL), Wq);
+          ++nD; xD += x; vD += v; xvD = fmaf(x, v, xvD); vvD = fmaf(v, v, vvD);
+        }
+      }
+      while (dR < hi && !(tt(dR) > tDE)) {
+        if (cnt[dR + 1] != cnt[dR]) {
+          const float x = xv[dR], v = __fsub_rn(tt(dR), Wq);
+          ++nD; xD += x; vD += v; xvD = fmaf(x, v, xvD); vvD = fmaf(v, v, vvD);
+        }
+        ++dR;
+      }
+      if (!(L != 0.0f)) continue;  // L = 0: H = 0/0 in the reference, never accepted
+      const int nC = cnt[dL] - cnt[bR];
+      const float SxC = df_diff(pxh[dL], pxl[dL], pxh[bR], pxl[bR]);
+      const int nACE = N - nB - nD;
+      const int nAE = nACE - nC;
+      const float xAEC = (SxAE - xB - xD) - m * (float)nACE;
+      const float XU = xuB - m * uB;
+      const float XV = xvD - m * vD;
+      const float L2 = L * L;
+      const float denA = 4.0f * L2 * (float)(nAE - nC) + 16.0f * (uuB + vvD);
+      const float numB = 8.0f * L2 * xAEC + 16.0f * L * (XV - XU);
+      const float H = -numB / denA;
+      const float SxCc = SxC - m * (float)nC;
+      const float SxAEc = xAEC - SxCc;
+      const float HL = H / L;
+      const float chi2 = SSf + H * (SxAEc - SxCc) + 0.25f * H * H * (float)nACE +
+                         2.0f * HL * (XV - XU) + HL * HL * (uuB + vvD);
+      if (chi2 > 0.0f) {
+        const float hv = a.mode ? fabsf(H) : H;
+        const float sn = hv / sqrtf(chi2 / (float)(N - 3));
+        if (sn > best_sn || (sn == best_sn && sn > 0.0f && wi < best_w)) {
+          best_sn = sn; best_w = wi; best_l = L; best_h = H;
+        }
+      }
+    }
+  }
+
+  red_sn[warp][lane] = best_sn;
+  red_w[warp][lane] = best_w;
+  red_l[warp][lane] = best_l;
+  red_h[warp][lane] = best_h;
+  __syncthreads();
+  if (warp == 0 && eok) {
+    for (int k = 1; k < kWarps; ++k) {
+      const float s = red_sn[k][lane];
+      const int w = red_w[k][lane];
+      if (s > best_sn || (s == best_sn && w < best_w)) {
+        best_sn = s; best_w = w; best_l = red_l[k][lane]; best_h = red_h[k][lane];
+      }
+    }
+    if (best_w == INT_MAX || !(best_sn > 0.0f)) { best_sn = 0.0f; best_w = 0; best_l = 0.0f; best_h = 0.0f; }
+    const float wf = (float)best_w;
+    const float W = a.w_fma ? __fmaf_rn(-a.dw, wf, a.wmax) : __fsub_rn(a.wmax, __fmul_rn(a.dw, wf));
+    const size_t k = (size_t)e * a.nq + q;
+    a.sn[k] = best_sn;
+    a.t0[k] = dte;
+    a.w[k] = W;
+    a.l[k] = best_l;
+    a.h[k] = best_h;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int gtrap_gtls(float *tlssn, float *tlsw, float *tlst0, float *tlsl, float *tlshmax,
+               const float *lc, const float *tu, int32_t nt, int32_t nq, int32_t nw,
+               int32_t nl, int32_t nsc, float t0min, float dt, float wmax, float dw,
+               float deltat, int32_t mode, uint32_t flags, gtrap_stream_t stream) {
+  (void)t0min;
+  (void)dt;
+  if (nt <= 0 || nq <= 0) return GTRAP_OK;
+  if (!tlssn || !tlsw || !tlst0 || !tlsl || !tlshmax || !lc || !tu)
+    return fail(GTRAP_ERR_INVALID_ARG, "gtls: null pointer");
+  if (nw < 1 || nw > 1024) return fail(GTRAP_ERR_INVALID_ARG, "gtls: nw=%d must be in [1, 1024]", nw);
+  if (nl < 1 || nl > 4096) return fail(GTRAP_ERR_INVALID_ARG, "gtls: nl=%d must be in [1, 4096]", nl);
+  if (nsc < 1 || nsc + 31 > kMaxStage)
+    return fail(GTRAP_ERR_INVALID_ARG, "gtls: nsc=%d must be in [1, %d]", nsc, kMaxStage - 31);
+  if (mode != 0 && mode != 1) return fail(GTRAP_ERR_INVALID_ARG, "gtls: mode must be 0 or 1");
+  if (!(deltat > 0.0f)) return fail(GTRAP_ERR_INVALID_ARG, "gtls: deltat must be positive");
+  const long long tiles = ((long long)nt + 31) / 32;
+  if (tiles * nq >= (1LL << 31)) return fail(GTRAP_ERR_INVALID_ARG, "gtls: grid too large");
+  const int S = nsc + 31;
+  const size_t smem = (size_t)S * 8 + (size_t)(S + 1) * 20 + 64;
+  GTRAP_TRY(gtrap::ensure_smem((const void *)gtls_kernel, smem, "gtls"));
+  TlsArgs ta;
+  ta.sn = tlssn; ta.w = tlsw; ta.t0 = tlst0; ta.l = tlsl; ta.h = tlshmax;
+  ta.lc = lc; ta.tu = tu;
+  ta.nt = nt; ta.nq = nq; ta.nw = nw; ta.nl = nl; ta.nsc = nsc;
+  ta.wmax = wmax; ta.dw = dw; ta.deltat = deltat; ta.mode = mode;
+  ta.w_fma = (flags & GTRAP_TLS_W_NOFMA) ? 0 : 1;
+  ta.t_fma = (flags & GTRAP_TLS_T_NOFMA) ? 0 : 1;
+  ta.tiles = (int)tiles;
+  gtls_kernel<<<(unsigned)(tiles * nq), kTlsThreads, smem, stream>>>(ta);
+  return gtrap::check_launch("gtls_kernel");
+}
+
+}  // extern "C"

@@ -1,0 +1,149 @@
+/*
+ * gtrap_gb300.h - C ABI of the GB300 (sm_103a) transit-search library.
+ *
+ * Every entry point takes raw device pointers, plain sizes and a CUDA
+ * stream, launches its kernels on that stream and returns a status code
+ * (GTRAP_OK == 0).  On failure gtrap_last_error() returns a description of
+ * the last error raised on the calling host thread.  No entry point
+ * allocates device memory: scratch space is passed in by the caller as a
+ * workspace pointer whose size is reported by the matching *_workspace_size
+ * function.
+ *
+ * Layout conventions follow the reference (gtrap):
+ *   light-curve images   lc[n, nq], tu[n, nq]  C order, element (i, q) at i*nq + q
+ *   BLS spectra          blsp[nq, nf]          element (q, j) at q*nf + j
+ *   GTLS outputs         tlssn[nt, nq]         element (e, q) at e*nq + q
+ * Masked samples are given as negative times (the reference uses -1000).
+ */
+#ifndef GTRAP_GB300_H
+#define GTRAP_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *gtrap_stream_t; /* same type as cudaStream_t */
+
+enum gtrap_status {
+  GTRAP_OK = 0,
+  GTRAP_ERR_INVALID_ARG = 1,   /* a size or parameter is out of the supported range */
+  GTRAP_ERR_CUDA = 2,          /* the CUDA runtime reported an error */
+  GTRAP_ERR_WORKSPACE = 3,     /* workspace pointer missing, misaligned or too small */
+  GTRAP_ERR_UNSUPPORTED = 4,   /* valid request this build does not implement */
+  GTRAP_ERR_TIMEOUT = 5        /* a bounded device-side wait expired */
+};
+
+/* Flags for the BLS entry points. */
+#define GTRAP_BLS_PHASE_FP32_REF 0x1u  /* fold with the reference's FP32 phase arithmetic
+                                          (include/geebls.h:68-70) instead of the exact
+                                          64-bit fixed-point phase */
+#define GTRAP_BLS_REF_F0_NOFMA   0x2u  /* FP32 phase: f0 = fmin + (df*j) with two roundings
+                                          (default: one fused multiply-add) */
+#define GTRAP_BLS_REF_PH_FMA     0x4u  /* FP32 phase: frac = fma(t, f0, -trunc(t*f0)) */
+
+/* Flags for the GTLS entry point. */
+#define GTRAP_TLS_W_NOFMA 0x1u  /* W = wmax - (dw*tid) with two roundings (default: fma) */
+#define GTRAP_TLS_T_NOFMA 0x2u  /* t - deltat*e with two roundings (default: fma) */
+
+const char *gtrap_last_error(void);
+int gtrap_version(void); /* 10000*major + 100*minor + patch */
+
+/* ---------------------------------------------------------------------------
+ * Median-filter detrend.  Replaces the gfilter kernel (gtrap/gfilter.py:13-86)
+ * launched by get_detrend (gtrap/gfilter.py:103-144):
+ *   out[i, q] = in[i, q] - median(in[i-r .. i+r, q]),  zero padded outside [0, n).
+ * The median is the exact (r+1)-th order statistic, so the result is bit-exact
+ * against scipy.signal.medfilt(x, 2r+1) followed by a float32 subtraction.
+ * Unlike the reference every row is written: n need not be a multiple of a
+ * tile height and r is not limited by one.  in and out must not alias.
+ * ------------------------------------------------------------------------- */
+int gtrap_gfilter(const float *in, float *out, uint32_t n, uint32_t nq, uint32_t r,
+                  gtrap_stream_t stream);
+
+/* Per-curve offset.  Replaces get_offset (gtrap/gfilter.py:94-101):
+ *   offset[q] = sum_{i : !(tu[i,q] < 0)} resid[i, q] / n   (masked samples count as 0). */
+int gtrap_offset(const float *resid, const float *tu, float *offset, uint32_t n, uint32_t nq,
+                 gtrap_stream_t stream);
+
+/* ---------------------------------------------------------------------------
+ * Box least squares.  Replaces the geebls kernel of gbls_module()
+ * (gtrap/geebls.py:10-22, include/geebls.h:1-167):
+ *   blsp[q, j]   = SR = sqrt(max_{i,k} s^2 / (kk (ntrue[q] - kk))),  f_j = fmin + j*df
+ *   phase1[q, j] = best start bin i, phase2[q, j] = best end bin (inclusive, may be >= nb)
+ * over start bins i < nb and widths k in (max(kmi,1), kma] bins with kk > max(kkmi,5)
+ * samples, folding samples with tu[i, q] >= 0 and flux lc - offset[q].
+ * nb in [1, 8192], kma in [1, nb].  ref_nthread > 0 reproduces the reference's
+ * tail drop (only the first floor(n/ref_nthread)*ref_nthread samples are folded);
+ * 0 folds every sample.  Ties between equal powers pick the lowest start bin,
+ * then the lowest end bin; with no accepted window SR = 0 and both bins = 0.
+ * ------------------------------------------------------------------------- */
+size_t gtrap_geebls_workspace_size(uint32_t n, uint32_t nq, uint32_t flags);
+int gtrap_geebls(float *blsp, uint32_t *phase1, uint32_t *phase2, const float *lc,
+                 const float *tu, const float *offset, const uint32_t *ntrue, uint32_t n,
+                 uint32_t nq, uint32_t nf, uint32_t nb, uint32_t kma, uint32_t kmi,
+                 uint32_t kkmi, float fmin, float df, uint32_t flags, uint32_t ref_nthread,
+                 void *workspace, size_t workspace_bytes, gtrap_stream_t stream);
+
+/* Plain BLS.  Replaces the geebls kernel of gtrap/geebls_simple.py:17-174: common
+ * time array tu[n], no mask, no offset, denominator n, no phase outputs (phase1 and
+ * phase2 may be NULL; when given they are filled as above). */
+size_t gtrap_geebls_simple_workspace_size(uint32_t n, uint32_t nq, uint32_t flags);
+int gtrap_geebls_simple(float *blsp, uint32_t *phase1, uint32_t *phase2, const float *lc,
+                        const float *tu, uint32_t n, uint32_t nq, uint32_t nf, uint32_t nb,
+                        uint32_t kma, uint32_t kmi, uint32_t kkmi, float fmin, float df,
+                        uint32_t flags, uint32_t ref_nthread, void *workspace,
+                        size_t workspace_bytes, gtrap_stream_t stream);
+
+/* ---------------------------------------------------------------------------
+ * BLS peak statistics.  Replaces getmax + combine_stat (gtrap/getstat.py:14-57,
+ * 100-123) as called by get_blsstat (gtrap/getstat.py:64-67).  Over the first
+ * floor(nf/patch)*patch frequencies of each curve (all nf when patch == 0):
+ *   pest[q] = 1/(jmax*df + fmin), sde[q] = (max - mean)/std with mean and the second
+ *   moment divided by nf, ph1best/ph2best = phase1/phase2 at jmax (lowest j on ties).
+ * Outputs are device arrays of nq elements; phase pointers may be NULL.
+ * ------------------------------------------------------------------------- */
+int gtrap_blsstat(const float *blsp, const uint32_t *phase1, const uint32_t *phase2,
+                  uint32_t nf, uint32_t nq, double df, double fmin, uint32_t patch,
+                  double *pest, double *sde, uint32_t *ph1best, uint32_t *ph2best,
+                  gtrap_stream_t stream);
+
+/* Per-patch partials with the getmax kernel's outputs (gtrap/getstat.py:14-57): for
+ * patch p of `patch` frequencies of curve q, element p + npatch*q of each output holds
+ * the patch maximum, its global index j + nf*q (lowest on ties), the patch sum and sum
+ * of squares, and phase1/phase2 at the maximum.  npatch = nf / patch. */
+int gtrap_getmax(const float *blsp, const uint32_t *phase1, const uint32_t *phase2,
+                 uint32_t nf, uint32_t nq, uint32_t patch, float *maxval, uint32_t *maxidx,
+                 float *avesum, float *varsum, uint32_t *maxphase1, uint32_t *maxphase2,
+                 gtrap_stream_t stream);
+
+/* ---------------------------------------------------------------------------
+ * Trapezoid least-squares single-event search.  Replaces the gtls kernel of
+ * gtls_module(mode) (gtrap/gtls.py:11-27; include/gtls_simple.h:1-406 for mode 0,
+ * include/gtls_absolute.h:1-408 for mode 1).  For each epoch e < nt and curve q < nq,
+ * the best signal-to-noise over nw widths W = wmax - dw*w and nl ingress widths L
+ * (mode 0: L = m*0.45W/nl; mode 1: L = (m+1)*W/(4nl)), using the samples of the scoop
+ * [e - nsc/2, e - nsc/2 + nsc) with times shifted by deltat*e.  Outputs
+ * tlssn/tlsw/tlst0/tlsl/tlshmax[e*nq + q].  t0min and dt are accepted and unused,
+ * as in the reference.  Valid times of a curve must be non-decreasing.
+ * nw in [1, 1024], nl in [1, 4096], nsc in [1, 65536].
+ * ------------------------------------------------------------------------- */
+int gtrap_gtls(float *tlssn, float *tlsw, float *tlst0, float *tlsl, float *tlshmax,
+               const float *lc, const float *tu, int32_t nt, int32_t nq, int32_t nw,
+               int32_t nl, int32_t nsc, float t0min, float dt, float wmax, float dw,
+               float deltat, int32_t mode, uint32_t flags, gtrap_stream_t stream);
+
+/* ---------------------------------------------------------------------------
+ * Measurement helpers (used by the benchmark to report roofline fractions).
+ * ------------------------------------------------------------------------- */
+/* FP32 issue peak: launches a register-resident FMA-chain kernel; *flops receives the
+ * number of FP32 floating-point operations it performs (an FMA counts as 2). */
+int gtrap_probe_fp32_peak(float *sink, uint32_t iters, double *flops, gtrap_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GTRAP_GB300_H */

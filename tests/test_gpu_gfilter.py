@@ -1,0 +1,62 @@
+"""gfilter on the GPU: bit-exact against scipy.signal.medfilt (the oracle) and the
+drop-in get_detrend / get_offset surface."""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from gtrap_gb300 import api, driver, gfilter
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("n,nq,r", [(1000, 1, 16), (777, 33, 24), (64, 5, 40), (2048, 64, 0),
+                                    (3000, 2, 128), (500, 70, 3)])
+def test_gfilter_bit_exact(cuda, n, nq, r):
+    rng = np.random.default_rng(n + nq + r)
+    x = rng.normal(1.0, 1e-3, size=(n, nq)).astype(np.float32)
+    x[n // 3: n // 3 + 20] = 1.002            # plateau (ties)
+    x[:, 0] = np.round(x[:, 0] * 1000) / 1000  # heavy duplicates
+    got = api.gfilter(torch.from_numpy(x).to(cuda), r).cpu().numpy()
+    np.testing.assert_array_equal(got, oracle.medfilt_residual(x, r))
+
+
+def test_gfilter_constant_and_zero_padding(cuda):
+    x = np.full((100, 3), 2.5, np.float32)
+    got = api.gfilter(torch.from_numpy(x).to(cuda), 10).cpu().numpy()
+    np.testing.assert_array_equal(got, oracle.medfilt_residual(x, 10))
+    # first and last rows see the zero padding exactly as medfilt does
+    assert got[50, 0] == 0.0
+
+
+def test_gfilter_large_window_vs_n(cuda):
+    rng = np.random.default_rng(1)
+    x = rng.normal(size=(30, 4)).astype(np.float32)
+    got = api.gfilter(torch.from_numpy(x).to(cuda), 40).cpu().numpy()
+    np.testing.assert_array_equal(got, oracle.medfilt_residual(x, 40))
+
+
+def test_get_detrend_dropin(cuda):
+    rng = np.random.default_rng(2)
+    lc = rng.normal(1.0, 1e-3, size=(4000, 4)).astype(np.float32)
+    out = gfilter.get_detrend(np.array(lc.T.tolist()).T, nby=1000, nbx=1, r=16, isw=0, osw=0)
+    np.testing.assert_array_equal(out, oracle.medfilt_residual(lc, 16))
+    dev = gfilter.get_detrend(lc, nby=1000, nbx=1, r=16, osw=1)
+    host = np.zeros(lc.size, np.float32)
+    driver.memcpy_dtoh(host, dev)
+    np.testing.assert_array_equal(host.reshape(lc.shape), out)
+
+
+def test_get_offset_dropin(cuda):
+    rng = np.random.default_rng(3)
+    n, nq = 5000, 7
+    resid = rng.normal(0, 1e-3, size=(n, nq)).astype(np.float32)
+    tu = np.tile(np.arange(n, dtype=np.float32)[:, None], (1, nq))
+    tu[100:900, 2] = -1000.0
+    dev = driver.mem_alloc(resid.nbytes)
+    driver.memcpy_htod(dev, resid)
+    off, img = gfilter.get_offset(n, nq, dev, tu)
+    np.testing.assert_allclose(off, oracle.offset(resid, tu), rtol=1e-5, atol=1e-10)
+    ref_img = resid.copy()
+    ref_img[tu < 0] = 0.0
+    np.testing.assert_array_equal(img, ref_img)

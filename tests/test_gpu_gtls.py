@@ -1,0 +1,100 @@
+"""gtls on the GPU against the FP64 oracle (reference region scans, FP64 sums).
+
+Tolerance: S/N relative error <= 1e-4 for S/N >= 1 (absolute 1e-4 below); the best
+(W, L) identical except where the oracle's top two templates are within that tolerance.
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from gtrap_gb300 import api, gtls as gtls_mod, synth
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4
+
+
+def _run(cuda, lc, tu, nt, g, mode=0):
+    d = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
+    out = api.gtls(d(lc), d(tu), nt, g["nw"], g["nl"], g["nsc"], g["wmax"], g["dw"], g["deltat"], mode=mode)
+    return [o.cpu().numpy() for o in out]
+
+
+def _compare(got, ref, *, tol=TOL):
+    sn, w, t0, l, h = got
+    osn, ow, ot0, ol, oh = ref
+    scale = np.maximum(np.abs(osn), 1.0)
+    err = np.abs(sn - osn) / scale
+    assert err.max() <= tol, "max S/N err %g at %s" % (err.max(), np.unravel_index(err.argmax(), err.shape))
+    np.testing.assert_array_equal(t0, ot0)
+    pos = osn > 0
+    mism = pos & ((w != ow) | (l != ol))
+    assert mism.sum() <= max(3, 0.002 * pos.sum()), "param mismatches: %d" % mism.sum()
+    ok = pos & ~mism
+    np.testing.assert_allclose(h[ok], oh[ok], rtol=1e-3, atol=1e-7)
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_gtls_tess_like(cuda, mode):
+    lc, tu, _ = synth.tess_like(nq=4, n=3000, seed=11 + mode, transit_frac=0.75)
+    g = synth.tls_grid(nw=8, nl=16)
+    got = _run(cuda, lc, tu, 3000, g, mode)
+    ref = oracle.gtls(lc, tu, 3000, g["nw"], g["nl"], g["nsc"], g["wmax"], g["dw"], g["deltat"], mode=mode)
+    _compare(got, ref)
+
+
+@pytest.mark.parametrize("nw,nl", [(1, 1), (3, 5), (13, 2), (40, 7)])
+def test_gtls_grid_shapes(cuda, nw, nl):
+    lc, tu, _ = synth.tess_like(nq=3, n=1200, seed=nw * 10 + nl)
+    g = synth.tls_grid(nw=nw, nl=nl, wmin_h=1.0, wmax_h=5.0)
+    got = _run(cuda, lc, tu, 1200, g)
+    ref = oracle.gtls(lc, tu, 1200, g["nw"], g["nl"], g["nsc"], g["wmax"], g["dw"], g["deltat"])
+    _compare(got, ref)
+
+
+def test_gtls_kepler_cadence_and_nt_below_n(cuda):
+    lc, tu, ntrue, _, _ = synth.kepler_like(nq=2, n=3000, nf=8, seed=4)
+    lc = 2.0 - lc
+    lc = (lc - np.median(lc, axis=0)).astype(np.float32)
+    g = synth.tls_grid(wmin_h=3.0, wmax_h=30.0, nw=16, nl=10, deltat=synth.KEPLER_CADENCE)
+    got = _run(cuda, lc, tu, 2500, g)
+    ref = oracle.gtls(lc, tu, 2500, g["nw"], g["nl"], g["nsc"], g["wmax"], g["dw"], g["deltat"])
+    _compare(got, ref)
+
+
+def test_gtls_dropin_module(cuda):
+    from gtrap_gb300 import driver
+    lc, tu, _ = synth.tess_like(nq=2, n=800, seed=3)
+    g = synth.tls_grid(nw=8, nl=6)
+    nt, nq = 800, 2
+    outs = [driver.mem_alloc(nt * nq * 4) for _ in range(5)]
+    d_lc, d_tu = driver.mem_alloc(lc.nbytes), driver.mem_alloc(tu.nbytes)
+    driver.memcpy_htod(d_lc, lc)
+    driver.memcpy_htod(d_tu, tu)
+    k = gtls_mod.gtls_module().get_function("gtls")
+    k(*outs, d_lc, d_tu, np.int32(nt), np.int32(g["nl"]), np.int32(g["nsc"]), np.float32(0.0),
+      np.float32(1.0), np.float32(g["wmax"]), np.float32(g["dw"]), np.float32(g["deltat"]),
+      block=(g["nw"], 1, 1), grid=(nt, nq), shared=(2 * g["nsc"] + g["nw"] + 2) * 4)
+    host = []
+    for o in outs:
+        a = np.zeros(nt * nq, np.float32)
+        driver.memcpy_dtoh(a, o)
+        host.append(a.reshape(nt, nq))
+    ref = oracle.gtls(lc, tu, nt, g["nw"], g["nl"], g["nsc"], g["wmax"], g["dw"], g["deltat"])
+    _compare(host, ref)
+
+
+def test_gtls_signal_found(cuda):
+    lc, tu, inj = synth.tess_like(nq=8, n=18000, seed=99, transit_frac=1.0)
+    g = synth.tls_grid()
+    sn = _run(cuda, lc, tu, 18000, g)[0]
+    t = np.where(tu[:, 0] > 0, tu[:, 0], np.nan)
+    hits = 0
+    strong = inj[:, 4] > 2e-3
+    for q in np.nonzero(strong)[0]:
+        e = int(np.argmax(sn[:, q]))
+        per, ep = inj[q, 1], inj[q, 2]
+        ph = (t[e] - ep + 0.5 * per) % per - 0.5 * per if np.isfinite(t[e]) else 1e9
+        hits += abs(ph) < inj[q, 3]
+    assert hits >= 0.8 * strong.sum()

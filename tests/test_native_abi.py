@@ -1,0 +1,65 @@
+"""The C-ABI library loads and exports every entry point declared in include/*.h.
+Only argument-validation paths run here (they return before any CUDA call)."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import pytest
+
+from gtrap_gb300 import _build, _native
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def _declared():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        src = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        names |= set(re.findall(r"\b(gtrap_[a-z0-9_]+)\s*\(", src))
+    return names
+
+
+@pytest.fixture(scope="module")
+def lib():
+    _build.build()
+    return _native.load()
+
+
+def test_every_declared_symbol_is_exported(lib):
+    declared = _declared()
+    assert {"gtrap_geebls", "gtrap_gtls", "gtrap_gfilter", "gtrap_blsstat"} <= declared
+    for name in sorted(declared):
+        assert hasattr(lib, name), name
+    # and the ctypes signature table covers them
+    assert declared <= set(_native.exported_symbols())
+
+
+def test_version_and_error_text(lib):
+    assert lib.gtrap_version() >= 100
+    assert isinstance(lib.gtrap_last_error(), bytes)
+
+
+def test_validation_errors_need_no_gpu(lib):
+    st = lib.gtrap_gfilter(None, None, 10, 10, 2, None)
+    assert st == _native.ERR_INVALID_ARG
+    assert b"null" in lib.gtrap_last_error()
+    # nb out of range is rejected before any launch
+    st = lib.gtrap_geebls_simple(C.c_void_p(16), None, None, C.c_void_p(16), C.c_void_p(16), 100, 2,
+                                 10, 9000, 10, 1, 5, 0.1, 0.01, 0, 0, None, 0, None)
+    assert st == _native.ERR_INVALID_ARG
+    st = lib.gtrap_gtls(*([C.c_void_p(16)] * 7), 10, 2, 2000, 4, 10, 0.0, 0.0, 1.0, 0.1, 0.01, 0, 0, None)
+    assert st == _native.ERR_INVALID_ARG
+    assert b"nw" in lib.gtrap_last_error()
+
+
+def test_workspace_sizes_are_host_side(lib):
+    a = lib.gtrap_geebls_workspace_size(65536, 1024, 0)
+    b = lib.gtrap_geebls_workspace_size(65536, 1024, _native.BLS_PHASE_FP32_REF)
+    assert a >= 1024 * 65536 * 20 and b < a
+    assert lib.gtrap_geebls_simple_workspace_size(4096, 64, 0) >= 64 * 4096 * 4 + 4096 * 16
+
+
+def test_missing_workspace_is_an_error(lib):
+    st = lib.gtrap_geebls_simple(C.c_void_p(256), None, None, C.c_void_p(256), C.c_void_p(256), 100, 2,
+                                 10, 64, 10, 1, 5, 0.1, 0.01, 0, 0, None, 0, None)
+    assert st == _native.ERR_WORKSPACE

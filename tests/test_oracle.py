@@ -1,0 +1,161 @@
+"""CPU checks of the oracle itself: known answers, the reference's own CPU code
+(golden vectors from gtrap/tls.py), and independent restatements on small inputs."""
+from fractions import Fraction
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle
+from oracle import tls_cpu
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+# ----------------------------------------------------------------------------- tls.py
+
+def test_tls_self_check_known_answer():
+    # gtrap/tls.py:113-122: noiseless trapezoid, input H = -3
+    t = np.linspace(0, 100, 132)
+    x = tls_cpu.gen_trapzoid(t, -3.0, 30.0, 5.0, 50.0)
+    assert tls_cpu.get_Hmax(t, x, 30.0, 5.0, 50.0) == pytest.approx(-3.0, abs=1e-12)
+
+
+def test_tls_restatement_matches_reference_golden():
+    g = np.load(GOLDEN / "tls_py_golden.npz")
+    for k in range(int(g["ncases"])):
+        t, x = g["t_%d" % k], g["x_%d" % k]
+        H, W, L, t0 = g["par_%d" % k]
+        np.testing.assert_array_equal(tls_cpu.gen_trapzoid(t, H, W, L, t0), g["template_%d" % k])
+        assert tls_cpu.get_Hmax(t, x, W, L, t0) == pytest.approx(float(g["hmax_%d" % k]), rel=1e-12, abs=1e-12)
+        got = tls_cpu.get_chi2Hmax(t, x, W, L, t0)
+        np.testing.assert_allclose(np.array(got, dtype=float), g["chi2_%d" % k], rtol=1e-10, atol=1e-12)
+
+
+# ----------------------------------------------------------------------------- gfilter
+
+def test_medfilt_known_answer():
+    x = np.array([[5], [1], [4], [2], [3]], np.float32)
+    med = x - oracle.medfilt_residual(x, 1)
+    np.testing.assert_array_equal(med[:, 0], [1, 4, 2, 3, 2])
+
+
+@pytest.mark.parametrize("r", [0, 1, 3, 8])
+def test_medfilt_equals_reference_bisection(r):
+    rng = np.random.default_rng(r)
+    x = rng.normal(size=(57, 3)).astype(np.float32)
+    x[10:20, 1] = 0.5           # ties
+    x[:, 2] = np.round(x[:, 2])  # many duplicates and zeros
+    np.testing.assert_array_equal(oracle.medfilt_residual(x, r), oracle.gfilter_bisection(x, r))
+
+
+# ----------------------------------------------------------------------------- BLS
+
+def _frac_bins(t, fmin, df, j, nb):
+    """Exact bins from rational arithmetic on the float32 inputs."""
+    f = Fraction(float(np.float32(fmin))) + j * Fraction(float(np.float32(df)))
+    out = []
+    for ti in t:
+        p = Fraction(float(np.float32(ti))) * f
+        fr = p - (p.numerator // p.denominator)
+        out.append(int(fr * nb))
+    return np.array(out)
+
+
+def _bls_python(lc, bins_per_freq, nb, kma, kmi, kkmi, N):
+    """Direct restatement of the reference loops (include/geebls.h:105-140) in FP64."""
+    nf = len(bins_per_freq)
+    nq = lc.shape[1]
+    sr = np.zeros((nq, nf))
+    p1 = np.zeros((nq, nf), int)
+    p2 = np.zeros((nq, nf), int)
+    kmi, kkmi = max(kmi, 1), max(kkmi, 5)
+    for q in range(nq):
+        for j, b in enumerate(bins_per_freq):
+            y = np.zeros(nb + kma)
+            c = np.zeros(nb + kma, int)
+            np.add.at(y, b, lc[:, q].astype(np.float64))
+            np.add.at(c, b, 1)
+            y[nb:] = y[:kma]
+            c[nb:] = c[:kma]
+            best, bi, bj = 0.0, 0, 0
+            for i in range(nb):
+                s, kk = 0.0, 0
+                for k in range(1, kma + 1):
+                    s += y[i + k - 1]
+                    kk += c[i + k - 1]
+                    if k > kmi and kk > kkmi:
+                        pw = s * s / (kk * (N - kk))
+                        if pw > best:
+                            best, bi, bj = pw, i, i + k - 1
+            sr[q, j], p1[q, j], p2[q, j] = np.sqrt(best), bi, bj
+    return sr, p1, p2
+
+
+def test_bls_oracle_exact_phase_matches_rational_restatement():
+    rng = np.random.default_rng(3)
+    n, nq, nb, kma, kmi, kkmi, nf = 96, 2, 32, 6, 1, 5, 5
+    t = np.sort(rng.uniform(0, 300, n)).astype(np.float32)
+    lc = rng.normal(size=(n, nq)).astype(np.float32)
+    fmin, df = np.float32(0.013), np.float32(0.0371)
+    bins = [_frac_bins(t, fmin, df, j, nb) for j in range(nf)]
+    sr_ref, p1_ref, p2_ref = _bls_python(lc, bins, nb, kma, kmi, kkmi, n)
+    sr, p1, p2, _ = oracle.bls(lc, t, nf, nb, kma, kmi, kkmi, fmin, df)
+    np.testing.assert_allclose(sr, sr_ref, rtol=1e-12)
+    np.testing.assert_array_equal(p1, p1_ref)
+    np.testing.assert_array_equal(p2, p2_ref)
+
+
+def test_bls_oracle_fp32_phase_matches_float32_emulation():
+    rng = np.random.default_rng(4)
+    n, nq, nb, kma, kmi, kkmi, nf = 128, 2, 64, 9, 2, 6, 4
+    t = np.sort(rng.uniform(0, 1400, n)).astype(np.float32)
+    lc = rng.normal(size=(n, nq)).astype(np.float32)
+    fmin, df = np.float32(0.31), np.float32(0.173)
+    bins = []
+    for j in range(nf):
+        f0 = np.float32(np.float32(fmin) + np.float32(df * np.float32(j)))  # no-fma variant
+        p = (t * f0).astype(np.float32)
+        ph = (p - p.astype(np.int32).astype(np.float32)).astype(np.float32)
+        b = (np.float32(nb) * ph).astype(np.float32).astype(np.int64)
+        bins.append(b)
+    keep = [b < nb for b in bins]
+    assert all(k.all() for k in keep)
+    sr_ref, p1_ref, p2_ref = _bls_python(lc, bins, nb, kma, kmi, kkmi, n)
+    sr, p1, p2, _ = oracle.bls(lc, t, nf, nb, kma, kmi, kkmi, fmin, df, phase="fp32", f0_fma=False)
+    np.testing.assert_allclose(sr, sr_ref, rtol=1e-12)
+    np.testing.assert_array_equal(p1, p1_ref)
+
+
+def test_bls_oracle_mask_offset_ntrue():
+    rng = np.random.default_rng(5)
+    n, nq, nb, kma, kmi, kkmi, nf = 160, 3, 32, 5, 1, 5, 3
+    tu = np.tile(np.sort(rng.uniform(0, 200, n))[:, None], (1, nq)).astype(np.float32)
+    tu[20:40, 1] = -1000.0
+    lc = rng.normal(size=(n, nq)).astype(np.float32)
+    off = np.array([0.1, -0.2, 0.0], np.float32)
+    ntrue = (tu >= 0).sum(axis=0).astype(np.uint32)
+    fmin, df = np.float32(0.05), np.float32(0.021)
+    sr, p1, p2, _ = oracle.bls(lc, tu, nf, nb, kma, kmi, kkmi, fmin, df, offset=off, ntrue=ntrue)
+    for q in range(nq):
+        valid = tu[:, q] >= 0
+        bins = [_frac_bins(tu[valid, q], fmin, df, j, nb) for j in range(nf)]
+        x = (lc[valid, q].astype(np.float64) - np.float64(off[q]))[:, None]
+        s2, a1, a2 = _bls_python(x, bins, nb, kma, kmi, kkmi, int(ntrue[q]))
+        np.testing.assert_allclose(sr[q], s2[0], rtol=1e-12)
+        np.testing.assert_array_equal(p1[q], a1[0])
+
+
+def test_bls_exact_phase_agrees_with_naive_float64_bins():
+    """Exact 64-bit phases and naive FP64 frac(t*f) give the same bins except within
+    FP64 rounding of a bin edge."""
+    rng = np.random.default_rng(9)
+    t = np.sort(rng.uniform(0, 1400, 4000)).astype(np.float32)
+    fmin, df, nb = np.float32(0.005), np.float32(1.2e-4), 2048
+    for j in (0, 777, 16383):
+        exact = _frac_bins(t[:200], fmin, df, j, nb)
+        f = np.float64(fmin) + j * np.float64(df)
+        ph = np.mod(t[:200].astype(np.float64) * f, 1.0)
+        naive = np.floor(ph * nb).astype(int)
+        diff = exact != naive
+        assert diff.sum() <= 1
