@@ -26,6 +26,7 @@ BLS_REF_F0_NOFMA = 0x2
 BLS_REF_PH_FMA = 0x4
 TLS_W_NOFMA = 0x1
 TLS_T_NOFMA = 0x2
+TLS_FIX_A = 0x4
 
 _SIGNATURES = {
     "gtrap_last_error": (C.c_char_p, []),

@@ -178,8 +178,11 @@ def getmax(blsp, phase1, phase2, patch, stream=None):
 
 
 def gtls(lc, tu, nt, nw, nl, nsc, wmax, dw, deltat, *, mode=0, t0min=0.0, dt=0.0,
-         w_fma=True, t_fma=True, out=None, stream=None):
-    """Trapezoid least-squares epoch search; returns (sn, w, t0, l, h), each ``[nt, nq]``."""
+         w_fma=True, t_fma=True, fix_a=False, out=None, stream=None):
+    """Trapezoid least-squares epoch search; returns (sn, w, t0, l, h), each ``[nt, nq]``.
+
+    ``fix_a`` forms the depth from region A's own flux instead of the flux the reference
+    kernel sums there (see GTRAP_TLS_FIX_A in include/gtrap_gb300.h)."""
     require_cuda()
     lc = _f32(lc, "lc")
     tu = _f32(tu, "tu")
@@ -191,7 +194,8 @@ def gtls(lc, tu, nt, nw, nl, nsc, wmax, dw, deltat, *, mode=0, t0min=0.0, dt=0.0
     dev = lc.device
     if out is None:
         out = tuple(torch.empty((nt, nq), dtype=torch.float32, device=dev) for _ in range(5))
-    flags = (0 if w_fma else N.TLS_W_NOFMA) | (0 if t_fma else N.TLS_T_NOFMA)
+    flags = (0 if w_fma else N.TLS_W_NOFMA) | (0 if t_fma else N.TLS_T_NOFMA) | \
+        (N.TLS_FIX_A if fix_a else 0)
     sn, w, t0, l, h = out
     N.call("gtrap_gtls", as_ptr(sn), as_ptr(w), as_ptr(t0), as_ptr(l), as_ptr(h), as_ptr(lc),
            as_ptr(tu), int(nt), int(nq), int(nw), int(nl), int(nsc), float(t0min), float(dt),

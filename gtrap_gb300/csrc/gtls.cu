@@ -24,7 +24,10 @@
 //  * C and A+E come from the prefix sums, chi^2 from the moment expansion.
 // Region membership is decided with the reference's float32 time and boundary
 // arithmetic, so the regions are the reference's regions; the sums are more accurate
-// than its float32 running sums.
+// than its float32 running sums.  The reference's region-A loop adds the flux of scoop
+// slot i - nSx while classifying slot i (include/gtls_simple.h:212-225 index cache[i]
+// with the loop counter); the depth H is formed with that sum, and so it is here unless
+// GTRAP_TLS_FIX_A asks for region A's own flux.  chi^2 uses region A's own flux in both.
 #include "common.cuh"
 
 #include <climits>
@@ -44,6 +47,7 @@ struct TlsArgs {
   float wmax, dw, deltat;
   int mode;          // 0: simple, 1: absolute
   int w_fma, t_fma;  // float32 contraction choices (see GTRAP_TLS_*_NOFMA)
+  int fix_a;         // 1: region A's own flux in H (GTRAP_TLS_FIX_A)
   int tiles;         // epoch tiles per curve
 };
 
@@ -194,6 +198,7 @@ __global__ void __launch_bounds__(kTlsThreads) gtls_kernel(const TlsArgs a) {
   __syncthreads();
 
   // ---- per (epoch, width)
+  const float xr = xref;
   const int e = e0 + lane;
   const bool eok = e < a.nt;
   const float ef = (float)e;
@@ -203,7 +208,8 @@ __global__ void __launch_bounds__(kTlsThreads) gtls_kernel(const TlsArgs a) {
     const float v = tq[s];
     return t_fma ? __fmaf_rn(-a.deltat, ef, v) : __fsub_rn(v, dte);
   };
-  // scoop of epoch e in staged indices
+  // scoop of epoch e in staged indices; c0 is scoop slot 0 (negative before the series)
+  const int c0 = e - nsch - base;
   const int lo = max(e - nsch, 0) - base;
   const int hi = min(e - nsch + a.nsc, a.nt) - base;
   auto ub = [&](float tau) -> int {  // first s in [lo, hi) with tt(s) > tau
@@ -293,11 +299,28 @@ __global__ void __launch_bounds__(kTlsThreads) gtls_kernel(const TlsArgs a) {
       const int nACE = N - nB - nD;
       const int nAE = nACE - nC;
       const float xAEC = (SxAE - xB - xD) - m * (float)nACE;
+      // the A part of xAEC as the reference forms it: flux of scoop slots [0, nAx)
+      // weighted by the validity of A's slots [nSx, nSx + nAx)
+      float xAEC_h = xAEC;
+      if (!a.fix_a) {
+        const int nA = cnt[bL] - cnt[ubS];
+        const int nAx = bL - ubS;
+        const int jlo = max(c0, 0), jhi = max(c0 + nAx, jlo);
+        float QA = df_diff(pxh[jhi], pxl[jhi], pxh[jlo], pxl[jlo]) + xr * (float)(cnt[jhi] - cnt[jlo]);
+        if (nAx > nA) {  // masked slots inside A drop their partner's flux
+          for (int i = 0; i < nAx; ++i) {
+            const int j = c0 + i;
+            if (cnt[ubS + i + 1] == cnt[ubS + i] && j >= 0 && cnt[j + 1] != cnt[j]) QA -= xv[j] + xr;
+          }
+        }
+        const float xA = df_diff(pxh[bL], pxl[bL], pxh[ubS], pxl[ubS]) - m * (float)nA;
+        xAEC_h = (xAEC - xA) + (QA - (m + xr) * (float)nA);
+      }
       const float XU = xuB - m * uB;
       const float XV = xvD - m * vD;
       const float L2 = L * L;
       const float denA = 4.0f * L2 * (float)(nAE - nC) + 16.0f * (uuB + vvD);
-      const float numB = 8.0f * L2 * xAEC + 16.0f * L * (XV - XU);
+      const float numB = 8.0f * L2 * xAEC_h + 16.0f * L * (XV - XU);
       const float H = -numB / denA;
       const float SxCc = SxC - m * (float)nC;
       const float SxAEc = xAEC - SxCc;
@@ -370,6 +393,7 @@ int gtrap_gtls(float *tlssn, float *tlsw, float *tlst0, float *tlsl, float *tlsh
   ta.wmax = wmax; ta.dw = dw; ta.deltat = deltat; ta.mode = mode;
   ta.w_fma = (flags & GTRAP_TLS_W_NOFMA) ? 0 : 1;
   ta.t_fma = (flags & GTRAP_TLS_T_NOFMA) ? 0 : 1;
+  ta.fix_a = (flags & GTRAP_TLS_FIX_A) ? 1 : 0;
   ta.tiles = (int)tiles;
   gtls_kernel<<<(unsigned)(tiles * nq), kTlsThreads, smem, stream>>>(ta);
   return gtrap::check_launch("gtls_kernel");

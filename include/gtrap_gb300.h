@@ -47,6 +47,9 @@ enum gtrap_status {
 /* Flags for the GTLS entry point. */
 #define GTRAP_TLS_W_NOFMA 0x1u  /* W = wmax - (dw*tid) with two roundings (default: fma) */
 #define GTRAP_TLS_T_NOFMA 0x2u  /* t - deltat*e with two roundings (default: fma) */
+#define GTRAP_TLS_FIX_A   0x4u  /* depth H from region A's own flux; by default H uses the
+                                   flux the reference kernel sums there (scoop slots
+                                   [0, nAx), include/gtls_simple.h:221) */
 
 const char *gtrap_last_error(void);
 int gtrap_version(void); /* 10000*major + 100*minor + patch */

@@ -60,7 +60,7 @@ def _load():
                                                 f32, f32, u32, u32]
         lib.oracle_gtls.restype = C.c_int
         lib.oracle_gtls.argtypes = [fp, fp, i32, i32, i32, i32, i32, f32, f32, f32, i32, i32, i32,
-                                    i32, dp, fp, fp, fp, dp]
+                                    i32, i32, dp, fp, fp, fp, dp]
         _lib = lib
     return _lib
 
@@ -110,8 +110,10 @@ def bls_window_power(lc, tu, q, j, i0, jend, nb, fmin, df, *, offset=None, ntrue
                                        int(jend))
 
 
-def gtls(lc, tu, nt, nw, nl, nsc, wmax, dw, deltat, *, mode=0, w_fma=True, t_fma=True, nthreads=0):
-    """FP64 gtls restatement; returns (sn, w, t0, l, h), each [nt, nq]."""
+def gtls(lc, tu, nt, nw, nl, nsc, wmax, dw, deltat, *, mode=0, w_fma=True, t_fma=True, fix_a=False,
+         nthreads=0):
+    """FP64 gtls restatement; returns (sn, w, t0, l, h), each [nt, nq].  ``fix_a`` sums
+    region A's own flux instead of the reference kernel's scoop-start slots."""
     lib = _load()
     lc = np.ascontiguousarray(lc, dtype=np.float32)
     tu = np.ascontiguousarray(tu, dtype=np.float32)
@@ -124,7 +126,7 @@ def gtls(lc, tu, nt, nw, nl, nsc, wmax, dw, deltat, *, mode=0, w_fma=True, t_fma
     lib.oracle_gtls(_ptr(lc, C.c_float), _ptr(tu, C.c_float), int(nt), int(nq), int(nw), int(nl),
                     int(nsc), float(np.float32(wmax)), float(np.float32(dw)),
                     float(np.float32(deltat)), int(mode), int(bool(w_fma)), int(bool(t_fma)),
-                    int(nthreads), _ptr(sn, C.c_double), _ptr(w, C.c_float), _ptr(t0, C.c_float),
+                    int(bool(fix_a)), int(nthreads), _ptr(sn, C.c_double), _ptr(w, C.c_float), _ptr(t0, C.c_float),
                     _ptr(l, C.c_float), _ptr(h, C.c_double))
     return sn, w, t0, l, h
 

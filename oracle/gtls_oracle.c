@@ -10,7 +10,9 @@
  *   tq = fl32(-1000 + fl32(tu + 1000)), valid when tq >= 0, then shifted by deltat*e (:122-134)
  *   W = wmax - dw*w; dl = W*0.45/nl (simple) or W/4/nl (absolute); L = m*dl or (m+1)*dl (:68-69, :167)
  *   mean over tStart <= t <= tEnd (:139-152)
- *   region scans A..E with the reference's break rules (:199-305)
+ *   region scans A..E with the reference's break rules (:199-305); region A adds the
+ *     flux of scoop slot i - nSx for the slot i it classifies (the kernel indexes cache[i]
+ *     with the loop counter, :221), unless fix_a selects the slot's own flux
  *   filfac = N/(W/deltat) > 0.75 (:308-311); denA, numB, H = -numB/denA (:314-317)
  *   chi^2 (:320-357); S/N = H/sqrt(chi^2/(N-3)), |H| in absolute mode (:361)
  *   best over (W, L) per epoch; ties keep the lowest width index, then the first L.
@@ -26,7 +28,7 @@
 
 typedef struct {
   const float *lc, *tu;
-  int nt, nq, nw, nl, nsc, mode, w_fma, t_fma;
+  int nt, nq, nw, nl, nsc, mode, w_fma, t_fma, fix_a;
   float wmax, dw, deltat;
 } tls_args;
 
@@ -75,7 +77,9 @@ static void one_epoch(const tls_args *a, int q, int e, float *tt, double *xx, do
       for (int i = 0; i < nsc; ++i) { if (tt[i] > tStart) break; ++nSx; }
       for (int i = nSx; i < nsc; ++i) {
         if (tt[i] > tAB) break;
-        if (tt[i] >= tStart) { ++nA; xAEC += xx[i] - mean; }
+        /* region A's flux is read from scoop slot i - nSx, not i, as in
+           include/gtls_simple.h:212-225 (unless fix_a is set) */
+        if (tt[i] >= tStart) { ++nA; xAEC += (a->fix_a ? xx[i] : xx[i - nSx]) - mean; }
         ++nAx;
       }
       for (int i = nSx + nAx; i < nsc; ++i) {
@@ -140,9 +144,9 @@ static void one_epoch(const tls_args *a, int q, int e, float *tt, double *xx, do
 
 /* Outputs [nt*nq], element e*nq + q. */
 int oracle_gtls(const float *lc, const float *tu, int nt, int nq, int nw, int nl, int nsc,
-                float wmax, float dw, float deltat, int mode, int w_fma, int t_fma, int nthreads,
-                double *sn, float *w, float *t0, float *l, double *h) {
-  tls_args a = {lc, tu, nt, nq, nw, nl, nsc, mode, w_fma, t_fma, wmax, dw, deltat};
+                float wmax, float dw, float deltat, int mode, int w_fma, int t_fma, int fix_a,
+                int nthreads, double *sn, float *w, float *t0, float *l, double *h) {
+  tls_args a = {lc, tu, nt, nq, nw, nl, nsc, mode, w_fma, t_fma, fix_a, wmax, dw, deltat};
   const long total = (long)nt * nq;
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
