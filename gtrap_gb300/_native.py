@@ -6,7 +6,9 @@ library is missing or cannot be loaded, every call raises ``GtrapError``.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import threading
+from pathlib import Path
 
 from . import _build
 
@@ -67,7 +69,8 @@ def load(build_if_missing: bool = False):
     with _lock:
         if _lib is not None:
             return _lib
-        path = _build.library_path()
+        override = os.environ.get("GTRAP_GB300_LIB")  # a tuning variant built by _build.build
+        path = Path(override) if override else _build.library_path()
         if not path.exists():
             if build_if_missing:
                 _build.build()

@@ -35,8 +35,14 @@ namespace {
 using gtrap::fail;
 
 constexpr int kThreads = 512;
+#ifndef GTRAP_BLS_MINB
+#define GTRAP_BLS_MINB 2  // resident blocks per SM the R = 8 scan is compiled for
+#endif
 constexpr int kMaxNb = 8192;
 constexpr int32_t kMasked = INT32_MIN;
+// Pre-test slack: candidates within 2^-15 of the running best are evaluated exactly, which
+// covers the rounding of the expanded denominator form (error <= ~5 ulp of blo*den).
+constexpr float kSlack = 1.0f - 1.0f / 32768.0f;
 
 // frac(t*f) * 2^64 for float32 t and f, exact whenever the product is >= 2^-17.
 __device__ __forceinline__ uint64_t frac64(float t, float f) {
@@ -195,7 +201,7 @@ __device__ __forceinline__ bool better(float p, int i, int e, float bp, int bi, 
 
 // MODE 0: exact phase, nb power of two; 1: exact phase, any nb; 2: FP32 reference phase.
 template <int R, int MODE>
-__global__ void __launch_bounds__(kThreads, R == 8 ? 2 : 1) bls_fold_scan_kernel(const BlsArgs a) {
+__global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1) bls_fold_scan_kernel(const BlsArgs a) {
   extern __shared__ __align__(16) unsigned long long sm[];
   __shared__ long long scan_x[kThreads / 32];
   __shared__ int scan_c[kThreads / 32];
@@ -342,43 +348,85 @@ __global__ void __launch_bounds__(kThreads, R == 8 ? 2 : 1) bls_fold_scan_kernel
     }
     group_bar(1 + g, Tg);
 
-    // candidate windows [i, e): i = i0 + r, e - i in (kmi, kma]
+    // candidate windows [i, e): i = i0 + r, k = e - i in (kmi, kma], kk > kkmi
     float bpow = 0.0f, blo = 0.0f;
     int bi = INT_MAX, be = INT_MAX;
+    // exact evaluation of (r, e): pre-test s^2 >= blo*den, then the rounded quotient
+    auto consider = [&](int r, float2 Pe, int e) {
+      const float s = Pe.x - ys[r];
+      const float kk = Pe.y - cs[r];
+      const float den = kk * (ncs[r] - Pe.y);
+      const float s2 = s * s;
+      if (kk > kkmi_f && fmaf(-blo, den, s2) >= 0.0f) {
+        const float pw = __fdiv_rn(s2, den);
+        if (pw > 0.0f && better(pw, i0 + r, e, bpow, bi, be)) {
+          bpow = pw;
+          bi = i0 + r;
+          be = e;
+          blo = bpow * kSlack;
+        }
+      }
+    };
     if (i0 < nb && kma > kmi) {
       const int ebeg = i0 + kmi + 1;
       const int eend = min(i0 + R - 1 + kma, nb + kma);
-      for (int e = ebeg; e <= eend; ++e) {
-        const float2 Pe = P[padi<R>(e)];
-        const unsigned base = (unsigned)(e - i0 - kmi - 1);
-        bool any = false;
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-          const float s = Pe.x - ys[r];
-          const float kk = Pe.y - cs[r];
-          const float den = kk * (ncs[r] - Pe.y);
-          const float t = fmaf(-blo, den, s * s);
-          any |= (base - (unsigned)r < (unsigned)(kma - kmi)) & (kk > kkmi_f) & (t >= 0.0f);
+      // Body: every start has k in range and kk > kkmi, so no per-candidate checks.
+      // kk is smallest for the last start; find the first end where it passes kkmi.
+      int fa = i0 + R + kmi, fb = i0 + kma;
+      {
+        int x0 = fa, x1 = fb + 1;
+        const float need = cs[R - 1] + kkmi_f;
+        while (x0 < x1) {
+          const int mid = (x0 + x1) >> 1;
+          if (P[padi<R>(mid)].y > need) x1 = mid; else x0 = mid + 1;
         }
-        if (any) {
+        fa = x0;
+      }
+      // head and tail with full checks
+      auto checked = [&](int e_from, int e_to) {
+        for (int e = e_from; e <= e_to; ++e) {
+          const float2 Pe = P[padi<R>(e)];
+          const unsigned base = (unsigned)(e - i0 - kmi - 1);
+#pragma unroll
+          for (int r = 0; r < R; ++r)
+            if (base - (unsigned)r < (unsigned)(kma - kmi)) consider(r, Pe, e);
+        }
+      };
+      if (fa > fb) {
+        checked(ebeg, eend);
+      } else {
+        checked(ebeg, fa - 1);
+        // -blo*den = blo*u^2 + beta_r*u + gamma_r in counts u centred on the first start
+        const float c0 = cs[0];
+        float beta[R], gamma[R];
+        auto coeffs = [&]() {
+#pragma unroll
+          for (int r = 0; r < R; ++r) {
+            const float ar = cs[r] - c0, br = ncs[r] - c0;
+            beta[r] = -blo * (ar + br);
+            gamma[r] = (blo * ar) * br;
+          }
+        };
+        coeffs();
+        for (int e = fa; e <= fb; ++e) {
+          const float2 Pe = P[padi<R>(e)];
+          const float u = Pe.y - c0;
+          const float G = (blo * u) * u;
+          unsigned neg = 0xffffffffu;
 #pragma unroll
           for (int r = 0; r < R; ++r) {
             const float s = Pe.x - ys[r];
-            const float kk = Pe.y - cs[r];
-            const float den = kk * (ncs[r] - Pe.y);
-            const float s2 = s * s;
-            const float t = fmaf(-blo, den, s2);
-            if ((base - (unsigned)r < (unsigned)(kma - kmi)) && (kk > kkmi_f) && (t >= 0.0f)) {
-              const float pw = __fdiv_rn(s2, den);
-              if (pw > 0.0f && better(pw, i0 + r, e, bpow, bi, be)) {
-                bpow = pw;
-                bi = i0 + r;
-                be = e;
-                blo = bpow * (1.0f - 1.0f / 1048576.0f);
-              }
-            }
+            const float t = fmaf(s, s, fmaf(u, beta[r], G + gamma[r]));
+            neg &= __float_as_uint(t);
+          }
+          if (!(neg >> 31)) {  // some candidate may reach the running best
+            const float before = blo;
+#pragma unroll
+            for (int r = 0; r < R; ++r) consider(r, Pe, e);
+            if (blo != before) coeffs();
           }
         }
+        checked(fb + 1, eend);
       }
     }
     // group reduction (max power, then lowest start, then lowest end)

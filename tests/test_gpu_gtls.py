@@ -34,7 +34,7 @@ def _compare(got, ref, *, tol=TOL):
     ok = pos & ~mism
     # depth: within 1e-3 except where denA nearly cancels (masked wings), at most 0.2%
     herr = np.abs(h[ok] - oh[ok]) / np.maximum(np.abs(oh[ok]), 1e-6)
-    assert (herr > 1e-3).mean() <= 0.002, "depth mismatches: %d" % (herr > 1e-3).sum()
+    assert (herr > 1e-3).sum() <= 0.002 * max(herr.size, 1), "depth mismatches: %d" % (herr > 1e-3).sum()
 
 
 @pytest.mark.parametrize("mode", [0, 1])
