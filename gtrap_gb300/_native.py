@@ -38,6 +38,9 @@ _SIGNATURES = {
     "gtrap_geebls_workspace_size": (sz, [u32, u32, u32]),
     "gtrap_geebls": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, u32, u32, u32, u32, u32, u32, u32,
                                f32, f32, u32, u32, vp, sz, vp]),
+    "gtrap_geebls_noalloc_max_scratch": (sz, []),
+    "gtrap_geebls_noalloc": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, u32, u32, u32, u32, u32, u32,
+                                       u32, f32, f32, u32, u32, vp]),
     "gtrap_geebls_simple_workspace_size": (sz, [u32, u32, u32]),
     "gtrap_geebls_simple": (C.c_int, [vp, vp, vp, vp, vp, u32, u32, u32, u32, u32, u32, u32,
                                       f32, f32, u32, u32, vp, sz, vp]),

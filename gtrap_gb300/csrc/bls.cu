@@ -29,6 +29,14 @@
 #include "common.cuh"
 
 #include <climits>
+#include <mutex>
+
+// Fixed scratch for gtrap_geebls_noalloc.  A file-scope device array: every GPU that
+// loads this library holds it until the process exits.  Host code must not use the
+// symbol's name as an address (it names a host-side stand-in); the device address is
+// looked up per device with cudaGetSymbolAddress.
+constexpr size_t kNoallocScratchBytes = size_t(64) << 20;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
 
 namespace {
 
@@ -601,9 +609,54 @@ int run_bls(bool full, float *blsp, uint32_t *phase1, uint32_t *phase2, const fl
   return gtrap::check_launch("bls_fold_scan_kernel");
 }
 
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void *g_noalloc_ptr[kMaxDevices];  // device address of g_noalloc_scratch, per device
+
+// Device address of the fixed scratch on the current device.  The first call on a device
+// looks it up (cudaGetSymbolAddress with that device current) and caches it.
+int noalloc_scratch(void **out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return fail(GTRAP_ERR_CUDA, "geebls_noalloc: cudaGetDevice: %s", cudaGetErrorString(e));
+  if (dev < 0 || dev >= kMaxDevices) return fail(GTRAP_ERR_UNSUPPORTED, "geebls_noalloc: device %d out of range", dev);
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      return fail(GTRAP_ERR_CUDA, "geebls_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return GTRAP_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+size_t gtrap_geebls_noalloc_max_scratch(void) { return kNoallocScratchBytes; }
+
+int gtrap_geebls_noalloc(float *blsp, uint32_t *phase1, uint32_t *phase2, const float *lc,
+                         const float *tu, const float *offset, const uint32_t *ntrue, uint32_t n,
+                         uint32_t nq, uint32_t nf, uint32_t nb, uint32_t kma, uint32_t kmi,
+                         uint32_t kkmi, float fmin, float df, uint32_t flags,
+                         uint32_t ref_nthread, gtrap_stream_t stream) {
+  if (nq == 0 || nf == 0) return GTRAP_OK;
+  const size_t need = ws_size(n, nq, flags, true);
+  if (need > kNoallocScratchBytes)
+    return fail(GTRAP_ERR_INVALID_ARG,
+                "geebls_noalloc: n=%u x nq=%u needs %zu bytes of scratch, the fixed scratch holds %zu; "
+                "use gtrap_geebls with a workspace for larger batches",
+                n, nq, need, kNoallocScratchBytes);
+  void *scratch = nullptr;
+  GTRAP_TRY(noalloc_scratch(&scratch));
+  // Every scratch element the kernels read is written earlier in the same call (per-curve
+  // scale, quantised flux, phase pairs), so nothing is cleared between calls.
+  return run_bls(true, blsp, phase1, phase2, lc, tu, offset, ntrue, n, nq, nf, nb, kma, kmi,
+                 kkmi, fmin, df, flags, ref_nthread, scratch, kNoallocScratchBytes, stream);
+}
 
 size_t gtrap_geebls_workspace_size(uint32_t n, uint32_t nq, uint32_t flags) {
   return ws_size(n, nq, flags, true);

@@ -7,7 +7,7 @@
  * the last error raised on the calling host thread.  No entry point
  * allocates device memory: scratch space is passed in by the caller as a
  * workspace pointer whose size is reported by the matching *_workspace_size
- * function.
+ * function (gtrap_geebls_noalloc uses a fixed scratch array instead).
  *
  * Layout conventions follow the reference (gtrap):
  *   light-curve images   lc[n, nq], tu[n, nq]  C order, element (i, q) at i*nq + q
@@ -89,6 +89,26 @@ int gtrap_geebls(float *blsp, uint32_t *phase1, uint32_t *phase2, const float *l
                  uint32_t nq, uint32_t nf, uint32_t nb, uint32_t kma, uint32_t kmi,
                  uint32_t kkmi, float fmin, float df, uint32_t flags, uint32_t ref_nthread,
                  void *workspace, size_t workspace_bytes, gtrap_stream_t stream);
+
+/* Masked BLS for callers that cannot allocate device memory.  No counterpart in the
+ * reference: it is gtrap_geebls without the workspace arguments.  Some hosts hand a
+ * library only the input and output buffers (as the reference's kernels receive them)
+ * and own every other allocation, and latency-critical callers may not call cudaMalloc,
+ * which can synchronise the device or fail under memory pressure.  This entry point
+ * allocates nothing: its scratch is a fixed device array of
+ * gtrap_geebls_noalloc_max_scratch() bytes (64 MiB) compiled into the library, which every
+ * GPU that loads the library holds until exit.  Batches needing more scratch than that
+ * (gtrap_geebls_workspace_size(n, nq, flags) bytes) are rejected with
+ * GTRAP_ERR_INVALID_ARG.  The first call on a device looks up the array's device address
+ * and should come before any stream capture.  All calls share the one array and every call
+ * rewrites what it reads, so calls that overlap on the GPU (different streams, threads or
+ * processes sharing the context) race and must be serialised by the caller. */
+size_t gtrap_geebls_noalloc_max_scratch(void);
+int gtrap_geebls_noalloc(float *blsp, uint32_t *phase1, uint32_t *phase2, const float *lc,
+                         const float *tu, const float *offset, const uint32_t *ntrue, uint32_t n,
+                         uint32_t nq, uint32_t nf, uint32_t nb, uint32_t kma, uint32_t kmi,
+                         uint32_t kkmi, float fmin, float df, uint32_t flags,
+                         uint32_t ref_nthread, gtrap_stream_t stream);
 
 /* Plain BLS.  Replaces the geebls kernel of gtrap/geebls_simple.py:17-174: common
  * time array tu[n], no mask, no offset, denominator n, no phase outputs (phase1 and
