@@ -48,6 +48,8 @@ constexpr int kThreads = 512;
 #endif
 constexpr int kMaxNb = 8192;
 constexpr int32_t kMasked = INT32_MIN;
+// Largest bin count for which the 32-bit fold format is exact (see the fold).
+constexpr int kFastMaxCount = 512;
 // Pre-test slack: candidates within 2^-15 of the running best are evaluated exactly, which
 // covers the rounding of the expanded denominator form (error <= ~5 ulp of blo*den).
 constexpr float kSlack = 1.0f - 1.0f / 32768.0f;
@@ -79,6 +81,7 @@ struct PrepArgs {
   const float *tu;       // [n, nq] (full) or [n] (simple)
   const float *offset;   // [nq] or null
   int32_t *sx;           // [nq] out: scale exponent
+  uint32_t *nv;          // [nq] out: number of valid samples
   int32_t *X;            // [nq, n] out: quantised flux or kMasked
   ulonglong2 *AB;        // [nq, n] (full) or [n] (simple) out: (frac(t*fmin), frac(t*df))
   float *T;              // [nq, n] out (FP32-reference phase mode, full only) or null
@@ -101,23 +104,31 @@ __device__ __forceinline__ bool sample_valid(const PrepArgs &a, uint32_t i, floa
 // Per-curve power-of-two scale: 2^sx * max|x - offset| < xq_max.
 __global__ void __launch_bounds__(1024) bls_scale_kernel(PrepArgs a) {
   __shared__ double part[32][33];
+  __shared__ uint32_t pcnt[32][33];
   const int lane = threadIdx.x, row = threadIdx.y;
   const uint32_t q = blockIdx.x * 32 + lane;
   double amax = 0.0;
+  uint32_t cnt = 0;
   if (q < a.nq) {
     const double off = a.offset ? (double)a.offset[q] : 0.0;
     for (uint32_t i = row; i < a.n; i += 32) {
       const size_t idx = (size_t)i * a.nq + q;
       const float x = __ldg(a.lc + idx);
       const float t = a.full ? __ldg(a.tu + idx) : __ldg(a.tu + i);
-      if (sample_valid(a, i, t, x, off)) amax = fmax(amax, fabs((double)x - off));
+      if (sample_valid(a, i, t, x, off)) {
+        amax = fmax(amax, fabs((double)x - off));
+        ++cnt;
+      }
     }
   }
   part[row][lane] = amax;
+  pcnt[row][lane] = cnt;
   __syncthreads();
   if (row == 0 && q < a.nq) {
     double m = 0.0;
-    for (int k = 0; k < 32; ++k) m = fmax(m, part[k][lane]);
+    uint32_t c = 0;
+    for (int k = 0; k < 32; ++k) { m = fmax(m, part[k][lane]); c += pcnt[k][lane]; }
+    a.nv[q] = c;
     int s = 0;
     if (m > 0.0) s = ilogb(a.xq_max) - ilogb(m) - 1;
     a.sx[q] = s;
@@ -187,6 +198,7 @@ struct BlsArgs {
   const ulonglong2 *AB;    // exact phase pairs
   const float *T;          // FP32-reference times
   const int32_t *sx;       // [nq]
+  const uint32_t *nv;      // [nq] valid samples (the fold's total count)
   const uint32_t *ntrue;   // [nq] or null (use n_den)
   uint32_t n, n_den, nq, nf, nb, kma, kmi, kkmi;
   float fmin, df;
@@ -215,6 +227,9 @@ __global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1) bls_fol
   __shared__ int scan_c[kThreads / 32];
   __shared__ float red_p[kThreads / 32];
   __shared__ int red_i[kThreads / 32], red_e[kThreads / 32];
+  __shared__ unsigned grp_best[kThreads / 64];  // running best power of each group (float bits)
+  __shared__ int scan_m[kThreads / 32];          // per-warp maximum bin count
+  __shared__ unsigned drop_cnt[64];              // FP32-phase samples landing on bin nb
 
   const uint32_t item = blockIdx.x;
   const uint32_t q = item / a.tiles;
@@ -230,52 +245,89 @@ __global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1) bls_fol
     ulonglong2 *z = reinterpret_cast<ulonglong2 *>(sm);
     const uint32_t nz = (a.F * a.region) / 2;
     for (uint32_t k = tid; k < nz; k += kThreads) z[k] = make_ulonglong2(0ull, 0ull);
+    if (tid < 64) drop_cnt[tid] = 0u;
   }
   __syncthreads();
 
-  // ---- fold
+  // ---- fold.  Fast format: two 32-bit words per bin, S += xq >> 10 and
+  // C += ((xq & 1023) << 12) | 1, exact while every bin holds at most kFastMaxCount
+  // samples (|xq| < 2^30).  The scan verifies that and re-folds a frequency in the 64-bit
+  // format ((xq << CB) | 1, one 64-bit atomic) when it does not hold.
   const int32_t *Xq = a.X + (size_t)q * a.n;
   const int CB = a.CB;
+  unsigned *h32 = reinterpret_cast<unsigned *>(sm);
+  const int shift = 64 - a.lognb;
+  const ulonglong2 *ABq = a.AB + (size_t)q * a.ab_stride;
+  const float *Tq = a.T + (size_t)q * a.t_stride;
+  const float nbf = (float)nb;
+  const bool f0_nofma = a.flags & GTRAP_BLS_REF_F0_NOFMA;
+  const bool ph_fma = a.flags & GTRAP_BLS_REF_PH_FMA;
+  // bin of time t at frequency j0 + f with the reference's float32 arithmetic; nb means
+  // dropped (the reference's wrap overwrites that slot)
+  auto ref_bin = [&](float t, uint32_t f) -> uint32_t {
+    const float jf = (float)(j0 + f);
+    const float f0 = f0_nofma ? __fadd_rn(a.fmin, __fmul_rn(a.df, jf)) : __fmaf_rn(a.df, jf, a.fmin);
+    const float p = __fmul_rn(t, f0);
+    const float ip = __int2float_rn(__float2int_rz(p));
+    const float ph = ph_fma ? __fmaf_rn(t, f0, -ip) : __fsub_rn(p, ip);
+    return __float2uint_rz(__fmul_rn(nbf, ph));
+  };
   if (MODE != 2) {
-    const ulonglong2 *ABq = a.AB + (size_t)q * a.ab_stride;
-    const int shift = 64 - a.lognb;
     for (uint32_t k = tid; k < a.n; k += kThreads) {
       const int32_t xq = __ldg(Xq + k);
       if (xq == kMasked) continue;
       const ulonglong2 ab = ABq[k];
-      const unsigned long long inc = ((unsigned long long)(long long)xq << CB) | 1ull;
+      const unsigned wS = (unsigned)(xq >> 10);
+      const unsigned wC = ((unsigned)(xq & 1023) << 12) | 1u;
       unsigned long long ph = ab.x + (unsigned long long)j0 * ab.y;
-      unsigned long long *h = sm;
+      unsigned *h = h32;
       for (uint32_t f = 0; f < nfrem; ++f) {
         const uint32_t bin = MODE == 0 ? (uint32_t)(ph >> shift) : (uint32_t)__umul64hi(ph, (unsigned long long)nb);
-        atomicAdd(h + bin, inc);
+        atomicAdd(h + 2 * bin, wS);
+        atomicAdd(h + 2 * bin + 1, wC);
         ph += ab.y;
-        h += a.region;
+        h += 2 * a.region;
       }
     }
   } else {
-    const float *Tq = a.T + (size_t)q * a.t_stride;
-    const float nbf = (float)nb;
-    const bool f0_nofma = a.flags & GTRAP_BLS_REF_F0_NOFMA;
-    const bool ph_fma = a.flags & GTRAP_BLS_REF_PH_FMA;
     for (uint32_t k = tid; k < a.n; k += kThreads) {
       const int32_t xq = __ldg(Xq + k);
       if (xq == kMasked) continue;
       const float t = __ldg(Tq + k);
-      const unsigned long long inc = ((unsigned long long)(long long)xq << CB) | 1ull;
-      unsigned long long *h = sm;
+      const unsigned wS = (unsigned)(xq >> 10);
+      const unsigned wC = ((unsigned)(xq & 1023) << 12) | 1u;
+      unsigned *h = h32;
       for (uint32_t f = 0; f < nfrem; ++f) {
-        const float jf = (float)(j0 + f);
-        const float f0 = f0_nofma ? __fadd_rn(a.fmin, __fmul_rn(a.df, jf)) : __fmaf_rn(a.df, jf, a.fmin);
-        const float p = __fmul_rn(t, f0);
-        const float ip = __int2float_rn(__float2int_rz(p));
-        const float ph = ph_fma ? __fmaf_rn(t, f0, -ip) : __fsub_rn(p, ip);
-        const uint32_t bin = __float2uint_rz(__fmul_rn(nbf, ph));
-        if (bin < (uint32_t)nb) atomicAdd(h + bin, inc);  // bin == nb is overwritten by the wrap in the reference
-        h += a.region;
+        const uint32_t bin = ref_bin(t, f);
+        if (bin < (uint32_t)nb) {
+          atomicAdd(h + 2 * bin, wS);
+          atomicAdd(h + 2 * bin + 1, wC);
+        } else {
+          atomicAdd(drop_cnt + f, 1u);
+        }
+        h += 2 * a.region;
       }
     }
   }
+  // 64-bit re-fold of frequency j0 + f by the Tg_ threads of one group
+  auto refold64 = [&](uint32_t f, int gtid_, int Tg_) {
+    unsigned long long *Hf = sm + (size_t)f * a.region;
+    for (uint32_t k = gtid_; k < a.n; k += Tg_) {
+      const int32_t xq = __ldg(Xq + k);
+      if (xq == kMasked) continue;
+      const unsigned long long inc = ((unsigned long long)(long long)xq << CB) | 1ull;
+      uint32_t bin;
+      if (MODE != 2) {
+        const ulonglong2 ab = ABq[k];
+        const unsigned long long ph = ab.x + (unsigned long long)(j0 + f) * ab.y;
+        bin = MODE == 0 ? (uint32_t)(ph >> shift) : (uint32_t)__umul64hi(ph, (unsigned long long)nb);
+      } else {
+        bin = ref_bin(__ldg(Tq + k), f);
+        if (bin >= (uint32_t)nb) continue;
+      }
+      atomicAdd(Hf + bin, inc);
+    }
+  };
   __syncthreads();
 
   // ---- scan, one frequency per group per round
@@ -298,53 +350,80 @@ __global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1) bls_fol
     unsigned long long *H = sm + (size_t)f * a.region;
     float2 *P = reinterpret_cast<float2 *>(H);
 
-    unsigned long long hv[R];
-#pragma unroll
-    for (int r = 0; r < R; ++r) hv[r] = (i0 + r < nb) ? H[i0 + r] : 0ull;
-    group_bar(1 + g, Tg);
-
     long long px[R];
     int pc[R];
-    long long sxv = 0;
-    int scv = 0;
+    long long sxv = 0, ex = 0, tx = 0;
+    int scv = 0, ec = 0, tc = 0;
+    if (gtid == 0) grp_best[g] = 0u;
+    for (int pass = 0; pass < 2; ++pass) {
+      const bool fast = pass == 0;
+      unsigned long long hv[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
-      sxv += (long long)hv[r] >> CB;
-      scv += (int)(hv[r] & cmask);
-      px[r] = sxv;
-      pc[r] = scv;
-    }
-    // inclusive warp scan of the thread totals
-    long long wx = sxv;
-    int wc = scv;
+      for (int r = 0; r < R; ++r) hv[r] = (i0 + r < nb) ? H[i0 + r] : 0ull;
+      group_bar(1 + g, Tg);
+      sxv = 0;
+      scv = 0;
+      int cmax = 0;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const long long ux = __shfl_up_sync(0xffffffffu, wx, o);
-      const int uc = __shfl_up_sync(0xffffffffu, wc, o);
-      if (lane >= o) { wx += ux; wc += uc; }
-    }
-    if (lane == 31) { scan_x[warp] = wx; scan_c[warp] = wc; }
-    group_bar(1 + g, Tg);
-    long long ex = wx - sxv, tx = 0;
-    int ec = wc - scv, tc = 0;
-    for (int w = 0; w < nwg; ++w) {
-      const long long vx = scan_x[gw0 + w];
-      const int vc = scan_c[gw0 + w];
-      if (gw0 + w < warp) { ex += vx; ec += vc; }
-      tx += vx;
-      tc += vc;
-    }
-    // exclusive prefix at the R start bins, then the padded prefix array
-    float ys[R], cs[R], ncs[R];
+      for (int r = 0; r < R; ++r) {
+        long long xs;
+        int c;
+        if (fast) {
+          xs = (long long)(int)(unsigned)(hv[r] & 0xffffffffull) * 1024 + (long long)(hv[r] >> 44);
+          c = (int)((hv[r] >> 32) & 0xfffull);
+        } else {
+          xs = (long long)hv[r] >> CB;
+          c = (int)(hv[r] & cmask);
+        }
+        sxv += xs;
+        scv += c;
+        cmax = max(cmax, c);
+        px[r] = sxv;
+        pc[r] = scv;
+      }
+      // inclusive warp scan of the thread totals, warp maximum of the bin counts
+      long long wx = sxv;
+      int wc = scv;
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
-      const long long xr = ex + (r ? px[r - 1] : 0);
-      const int cr = ec + (r ? pc[r - 1] : 0);
-      const bool ok = i0 + r < nb;
-      ys[r] = __ll2float_rn(xr);
-      cs[r] = ok ? (float)cr : 3.0e38f;  // start beyond nb: kk < 0, never accepted
-      ncs[r] = Nf + (float)cr;
+      for (int o = 1; o < 32; o <<= 1) {
+        const long long ux = __shfl_up_sync(0xffffffffu, wx, o);
+        const int uc = __shfl_up_sync(0xffffffffu, wc, o);
+        if (lane >= o) { wx += ux; wc += uc; }
+      }
+      cmax = __reduce_max_sync(0xffffffffu, cmax);
+      if (lane == 31) { scan_x[warp] = wx; scan_c[warp] = wc; scan_m[warp] = cmax; }
+      group_bar(1 + g, Tg);
+      ex = wx - sxv;
+      tx = 0;
+      ec = wc - scv;
+      tc = 0;
+      int gmax = 0;
+      for (int w = 0; w < nwg; ++w) {
+        const long long vx = scan_x[gw0 + w];
+        const int vc = scan_c[gw0 + w];
+        if (gw0 + w < warp) { ex += vx; ec += vc; }
+        tx += vx;
+        tc += vc;
+        gmax = max(gmax, scan_m[gw0 + w]);
+      }
+      if (!fast) break;
+      const int expect = (int)a.nv[q] - (MODE == 2 ? (int)drop_cnt[f] : 0);
+      if (tc == expect && gmax <= kFastMaxCount) break;
+      // some bin may have overflowed the 32-bit format: fold this frequency again in 64 bits
+      group_bar(1 + g, Tg);  // every thread has read scan_* and H before they are rewritten
+      {
+        ulonglong2 *z = reinterpret_cast<ulonglong2 *>(H);
+        for (uint32_t k = gtid; k < a.region / 2; k += Tg) z[k] = make_ulonglong2(0ull, 0ull);
+      }
+      group_bar(1 + g, Tg);
+      refold64(f, gtid, Tg);
+      group_bar(1 + g, Tg);
     }
+    // exclusive prefix sums at the R start bins (the counts are re-read from P when needed)
+    float ys[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) ys[r] = __ll2float_rn(ex + (r ? px[r - 1] : 0));
+    const float c_last = (float)(ec + (R > 1 ? pc[R - 2] : 0));  // count prefix of the last start
     if (gtid == 0) P[0] = make_float2(0.0f, 0.0f);
 #pragma unroll
     for (int r = 0; r < R; ++r) {
@@ -361,21 +440,44 @@ __global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1) bls_fol
     int bi = INT_MAX, be = INT_MAX;
     // exact evaluation of (r, e): pre-test s^2 >= blo*den, then the rounded quotient
     auto consider = [&](int r, float2 Pe, int e) {
+      const float cr = P[padi<R>(i0 + r)].y;
       const float s = Pe.x - ys[r];
-      const float kk = Pe.y - cs[r];
-      const float den = kk * (ncs[r] - Pe.y);
+      const float kk = Pe.y - cr;
+      const float den = kk * ((Nf + cr) - Pe.y);
       const float s2 = s * s;
-      if (kk > kkmi_f && fmaf(-blo, den, s2) >= 0.0f) {
+      if (i0 + r < nb && kk > kkmi_f && fmaf(-blo, den, s2) >= 0.0f) {
         const float pw = __fdiv_rn(s2, den);
         if (pw > 0.0f && better(pw, i0 + r, e, bpow, bi, be)) {
           bpow = pw;
           bi = i0 + r;
           be = e;
-          blo = bpow * kSlack;
+          if (bpow * kSlack > blo) blo = bpow * kSlack;
         }
       }
     };
-    if (i0 < nb && kma > kmi) {
+    // The admission threshold is shared by the group: any candidate found anywhere in the
+    // group raises it, so a lane rarely leaves the fast loop.  It only ever holds powers of
+    // real candidates, so the group maximum always passes it.
+    volatile unsigned *gbest = grp_best + g;
+    auto publish = [&]() { if (bpow > 0.0f) atomicMax(grp_best + g, __float_as_uint(bpow)); };
+    auto refresh = [&]() -> bool {
+      const float gb = __uint_as_float(*gbest) * kSlack;
+      if (gb > blo) { blo = gb; return true; }
+      return false;
+    };
+    const bool active = i0 < nb && kma > kmi;
+    // seed with the widest window of every start
+    if (active) {
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int e = i0 + r + kma;
+        if (i0 + r < nb) consider(r, P[padi<R>(e)], e);
+      }
+      publish();
+    }
+    group_bar(1 + g, Tg);
+    if (active) {
+      refresh();
       const int ebeg = i0 + kmi + 1;
       const int eend = min(i0 + R - 1 + kma, nb + kma);
       // Body: every start has k in range and kk > kkmi, so no per-candidate checks.
@@ -383,7 +485,7 @@ __global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1) bls_fol
       int fa = i0 + R + kmi, fb = i0 + kma;
       {
         int x0 = fa, x1 = fb + 1;
-        const float need = cs[R - 1] + kkmi_f;
+        const float need = c_last + kkmi_f;
         while (x0 < x1) {
           const int mid = (x0 + x1) >> 1;
           if (P[padi<R>(mid)].y > need) x1 = mid; else x0 = mid + 1;
@@ -404,13 +506,15 @@ __global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1) bls_fol
         checked(ebeg, eend);
       } else {
         checked(ebeg, fa - 1);
+        refresh();
         // -blo*den = blo*u^2 + beta_r*u + gamma_r in counts u centred on the first start
-        const float c0 = cs[0];
+        const float c0 = P[padi<R>(i0)].y;
         float beta[R], gamma[R];
         auto coeffs = [&]() {
 #pragma unroll
           for (int r = 0; r < R; ++r) {
-            const float ar = cs[r] - c0, br = ncs[r] - c0;
+            const float cr = P[padi<R>(i0 + r)].y;
+            const float ar = cr - c0, br = (Nf + cr) - c0;
             beta[r] = -blo * (ar + br);
             gamma[r] = (blo * ar) * br;
           }
@@ -427,11 +531,18 @@ __global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1) bls_fol
             const float t = fmaf(s, s, fmaf(u, beta[r], G + gamma[r]));
             neg &= __float_as_uint(t);
           }
-          if (!(neg >> 31)) {  // some candidate may reach the running best
-            const float before = blo;
+          if (!(neg >> 31)) {  // some candidate may reach the shared best
+            const float before = bpow;
 #pragma unroll
-            for (int r = 0; r < R; ++r) consider(r, Pe, e);
-            if (blo != before) coeffs();
+            for (int r = 0; r < R; ++r) {
+              const float s = Pe.x - ys[r];
+              if (fmaf(s, s, fmaf(u, beta[r], G + gamma[r])) >= 0.0f) consider(r, Pe, e);
+            }
+            if (bpow != before) publish();
+            refresh();
+            coeffs();
+          } else if (!((e - fa) & 15)) {
+            if (refresh()) coeffs();
           }
         }
         checked(fb + 1, eend);
@@ -477,7 +588,8 @@ int make_plan(uint32_t nb, uint32_t kma, uint32_t nf, Plan *p) {
   uint32_t Tg = (nb + R - 1) / R;
   Tg = (Tg + 31) / 32 * 32;
   if (Tg < 64) Tg = 64;  // at most 8 groups: named barriers 1..8
-  const uint32_t last = nb + kma;
+  // prefix entries 0 .. nb + kma are written; starts read entries up to nb + R - 2
+  const uint32_t last = nb + (kma > (uint32_t)R ? kma : (uint32_t)R);
   uint32_t region = last + (last >> logR) + 1;
   if (region < nb) region = nb;
   region = (region + 1) & ~1u;  // 16-byte multiple for the zero fill
@@ -511,6 +623,7 @@ int make_plan(uint32_t nb, uint32_t kma, uint32_t nf, Plan *p) {
 size_t ws_size(uint32_t n, uint32_t nq, uint32_t flags, bool full) {
   const bool exact = !(flags & GTRAP_BLS_PHASE_FP32_REF);
   size_t s = gtrap::align256((size_t)nq * 4);                 // sx
+  s += gtrap::align256((size_t)nq * 4);                        // nv
   s += gtrap::align256((size_t)nq * n * 4);                     // X
   if (full) s += gtrap::align256((size_t)nq * n * (exact ? 16 : 4));
   else if (exact) s += gtrap::align256((size_t)n * 16);
@@ -547,6 +660,7 @@ int run_bls(bool full, float *blsp, uint32_t *phase1, uint32_t *phase2, const fl
     return fail(GTRAP_ERR_WORKSPACE, "%s: workspace of %zu bytes, %zu needed", name, workspace_bytes, need);
   gtrap::Carver cv{(char *)workspace, workspace_bytes, 0};
   int32_t *sx = cv.take<int32_t>(nq);
+  uint32_t *nv = cv.take<uint32_t>(nq);
   int32_t *X = cv.take<int32_t>((size_t)nq * n);
   ulonglong2 *AB = nullptr;
   float *T = nullptr;
@@ -559,11 +673,11 @@ int run_bls(bool full, float *blsp, uint32_t *phase1, uint32_t *phase2, const fl
 
   const int CB = gtrap::ilog2u(n) + 1;  // count field: counts <= n < 2^CB
   double xq_max = ldexp(1.0, 62 - CB) / (double)n;
-  if (xq_max > 2147483647.0) xq_max = 2147483647.0;
+  if (xq_max > 1073741823.0) xq_max = 1073741823.0;  // |xq| < 2^30 for the 32-bit fold format
 
   PrepArgs pa;
   pa.lc = lc; pa.tu = tu; pa.offset = full ? offset : nullptr;
-  pa.sx = sx; pa.X = X; pa.AB = AB; pa.T = T;
+  pa.sx = sx; pa.nv = nv; pa.X = X; pa.AB = AB; pa.T = T;
   pa.n = n; pa.nq = nq; pa.n_eff = n_eff;
   pa.fmin = fmin; pa.df = df; pa.xq_max = xq_max;
   pa.full = full ? 1 : 0; pa.exact = exact ? 1 : 0;
@@ -580,7 +694,7 @@ int run_bls(bool full, float *blsp, uint32_t *phase1, uint32_t *phase2, const fl
   GTRAP_TRY(make_plan(nb, kma, nf, &p));
   BlsArgs ba;
   ba.blsp = blsp; ba.ph1 = phase1; ba.ph2 = phase2;
-  ba.X = X; ba.AB = AB; ba.T = full ? T : tu; ba.sx = sx; ba.ntrue = full ? ntrue : nullptr;
+  ba.X = X; ba.AB = AB; ba.T = full ? T : tu; ba.sx = sx; ba.nv = nv; ba.ntrue = full ? ntrue : nullptr;
   ba.n = n; ba.n_den = n; ba.nq = nq; ba.nf = nf; ba.nb = nb; ba.kma = kma;
   ba.kmi = kmi_eff; ba.kkmi = kkmi_eff; ba.fmin = fmin; ba.df = df;
   ba.F = p.F; ba.tiles = p.tiles; ba.region = p.region; ba.Tg = p.Tg; ba.G = p.G;

@@ -138,3 +138,19 @@ def test_injected_transit_recovered(cuda):
         ratio = pest[q] / per[q]
         ok += any(abs(ratio - m) < 0.01 * m for m in (1.0, 0.5, 2.0, 1 / 3, 3.0))
     assert ok >= 0.8 * strong.sum()
+
+
+def test_concentrated_bins_use_exact_fallback(cuda):
+    """A frequency so low that each bin receives ~1000 samples exceeds the 32-bit fold
+    format's per-bin limit; the kernel must detect it and re-fold in 64 bits."""
+    rng = np.random.default_rng(12)
+    n, nq, nb = 8192, 2, 512
+    tu = (0.02 * np.arange(n)).astype(np.float32)
+    lc = rng.normal(size=(n, nq)).astype(np.float32)
+    lc -= lc.mean(axis=0)
+    fmin, df, nf = np.float32(1e-4), np.float32(2e-3), 40   # the first frequencies cover < 1 cycle
+    d = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
+    sr, p1, p2 = api.geebls_simple(d(lc), d(tu), nf, nb, 52, 2, 5, fmin, df, with_phase=True)
+    osr, op1, op2, opmax = oracle.bls(lc, tu, nf, nb, 52, 2, 5, fmin, df)
+    _check_spectrum(sr.cpu().numpy(), p1.cpu().numpy(), p2.cpu().numpy(), osr, op1, op2, opmax,
+                    lc, tu, dict(nb=nb, fmin=fmin, df=df))
