@@ -202,14 +202,21 @@ struct BlsArgs {
   const uint32_t *ntrue;   // [nq] or null (use n_den)
   uint32_t n, n_den, nq, nf, nb, kma, kmi, kkmi;
   float fmin, df;
-  uint32_t F, tiles, region, Tg, G;
+  uint32_t F, tiles, region, Tg, G, lp;
   int lognb, CB;
   uint32_t ab_stride, t_stride;  // elements per curve (0: shared by all curves)
   uint32_t flags;
 };
 
-template <int R>
-__device__ __forceinline__ int padi(int e) { return e + (e >> (R == 16 ? 4 : 3)); }
+// Start bins per scan task (one warp; its lanes take 32 end bins at a time).
+constexpr int kRS = 8;
+
+// Order-preserving key of a window: power (non-negative float bits) in the high word, then
+// the lowest (start, end) -- start < 2^17, end < 2^15 -- as the complement in the low word.
+__device__ __forceinline__ unsigned long long pack_key(float pw, int i, int e) {
+  return ((unsigned long long)__float_as_uint(pw) << 32) |
+         (unsigned long long)(0xffffffffu - (((unsigned)i << 15) | (unsigned)e));
+}
 
 __device__ __forceinline__ void group_bar(int id, int nthreads) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
@@ -225,9 +232,9 @@ __global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1) bls_fol
   extern __shared__ __align__(16) unsigned long long sm[];
   __shared__ long long scan_x[kThreads / 32];
   __shared__ int scan_c[kThreads / 32];
-  __shared__ float red_p[kThreads / 32];
-  __shared__ int red_i[kThreads / 32], red_e[kThreads / 32];
-  __shared__ unsigned grp_best[kThreads / 64];  // running best power of each group (float bits)
+  __shared__ unsigned long long best_key[64];    // per frequency: best (power, -start, -end)
+  __shared__ unsigned best_thr[64];              // per frequency: running best power (float bits)
+  __shared__ int task_ctr;                       // next scan task of this block
   __shared__ int scan_m[kThreads / 32];          // per-warp maximum bin count
   __shared__ unsigned drop_cnt[64];              // FP32-phase samples landing on bin nb
 
@@ -273,20 +280,31 @@ __global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1) bls_fol
     return __float2uint_rz(__fmul_rn(nbf, ph));
   };
   if (MODE != 2) {
-    for (uint32_t k = tid; k < a.n; k += kThreads) {
-      const int32_t xq = __ldg(Xq + k);
-      if (xq == kMasked) continue;
-      const ulonglong2 ab = ABq[k];
-      const unsigned wS = (unsigned)(xq >> 10);
-      const unsigned wC = ((unsigned)(xq & 1023) << 12) | 1u;
-      unsigned long long ph = ab.x + (unsigned long long)j0 * ab.y;
-      unsigned *h = h32;
-      for (uint32_t f = 0; f < nfrem; ++f) {
-        const uint32_t bin = MODE == 0 ? (uint32_t)(ph >> shift) : (uint32_t)__umul64hi(ph, (unsigned long long)nb);
-        atomicAdd(h + 2 * bin, wS);
-        atomicAdd(h + 2 * bin + 1, wC);
-        ph += ab.y;
-        h += 2 * a.region;
+    // kU samples per thread per step, all loads issued before any is used
+    constexpr int kU = 4;
+    for (uint32_t k0 = tid; k0 < a.n; k0 += kU * kThreads) {
+      int32_t xq[kU];
+      ulonglong2 ab[kU];
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        const uint32_t k = k0 + u * kThreads;
+        xq[u] = k < a.n ? __ldg(Xq + k) : kMasked;
+        ab[u] = k < a.n ? __ldg(ABq + k) : make_ulonglong2(0ull, 0ull);
+      }
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        if (xq[u] == kMasked) continue;
+        const unsigned wS = (unsigned)(xq[u] >> 10);
+        const unsigned wC = ((unsigned)(xq[u] & 1023) << 12) | 1u;
+        unsigned long long ph = ab[u].x + (unsigned long long)j0 * ab[u].y;
+        unsigned *h = h32;
+        for (uint32_t f = 0; f < nfrem; ++f) {
+          const uint32_t bin = MODE == 0 ? (uint32_t)(ph >> shift) : (uint32_t)__umul64hi(ph, (unsigned long long)nb);
+          atomicAdd(h + 2 * bin, wS);
+          atomicAdd(h + 2 * bin + 1, wC);
+          ph += ab[u].y;
+          h += 2 * a.region;
+        }
       }
     }
   } else {
@@ -330,7 +348,7 @@ __global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1) bls_fol
   };
   __syncthreads();
 
-  // ---- scan, one frequency per group per round
+  // ---- prefix sums: groups of Tg threads, one frequency per group per round
   const int Tg = (int)a.Tg;
   const int g = tid / Tg;
   const int gtid = tid - g * Tg;
@@ -343,6 +361,8 @@ __global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1) bls_fol
   const unsigned long long cmask = (1ull << CB) - 1ull;
   const int i0 = gtid * R;
   const int rounds = (int)((nfrem + a.G - 1) / a.G);
+  const int lp = (int)a.lp;                // prefix entries per frequency (multiple of 32)
+  const int nchunk = lp >> 5;
 
   for (int rd = 0; rd < rounds; ++rd) {
     const uint32_t f = (uint32_t)rd * a.G + g;
@@ -354,7 +374,6 @@ __global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1) bls_fol
     int pc[R];
     long long sxv = 0, ex = 0, tx = 0;
     int scv = 0, ec = 0, tc = 0;
-    if (gtid == 0) grp_best[g] = 0u;
     for (int pass = 0; pass < 2; ++pass) {
       const bool fast = pass == 0;
       unsigned long long hv[R];
@@ -419,157 +438,224 @@ __global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1) bls_fol
       refold64(f, gtid, Tg);
       group_bar(1 + g, Tg);
     }
-    // exclusive prefix sums at the R start bins (the counts are re-read from P when needed)
-    float ys[R];
-#pragma unroll
-    for (int r = 0; r < R; ++r) ys[r] = __ll2float_rn(ex + (r ? px[r - 1] : 0));
-    const float c_last = (float)(ec + (R > 1 ? pc[R - 2] : 0));  // count prefix of the last start
+    // P[e] = (flux prefix, count prefix) over bins [0, e) of the wrapped axis, e <= nb + kma
     if (gtid == 0) P[0] = make_float2(0.0f, 0.0f);
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       const int e = i0 + r + 1;
       if (e <= nb) {
-        P[padi<R>(e)] = make_float2(__ll2float_rn(ex + px[r]), (float)(ec + pc[r]));
-        if (e <= kma) P[padi<R>(nb + e)] = make_float2(__ll2float_rn(tx + ex + px[r]), (float)(tc + ec + pc[r]));
+        P[e] = make_float2(__ll2float_rn(ex + px[r]), (float)(ec + pc[r]));
+        if (e <= kma) P[nb + e] = make_float2(__ll2float_rn(tx + ex + px[r]), (float)(tc + ec + pc[r]));
       }
     }
-    group_bar(1 + g, Tg);
+  }
+  if (tid < 64) { best_key[tid] = 0ull; best_thr[tid] = 0u; }
+  if (tid == 0) task_ctr = 0;
+  __syncthreads();
 
-    // candidate windows [i, e): i = i0 + r, k = e - i in (kmi, kma], kk > kkmi
-    float bpow = 0.0f, blo = 0.0f;
-    int bi = INT_MAX, be = INT_MAX;
-    // exact evaluation of (r, e): pre-test s^2 >= blo*den, then the rounded quotient
-    auto consider = [&](int r, float2 Pe, int e) {
-      const float cr = P[padi<R>(i0 + r)].y;
-      const float s = Pe.x - ys[r];
-      const float kk = Pe.y - cr;
-      const float den = kk * ((Nf + cr) - Pe.y);
-      const float s2 = s * s;
-      if (i0 + r < nb && kk > kkmi_f && fmaf(-blo, den, s2) >= 0.0f) {
-        const float pw = __fdiv_rn(s2, den);
-        if (pw > 0.0f && better(pw, i0 + r, e, bpow, bi, be)) {
-          bpow = pw;
-          bi = i0 + r;
-          be = e;
-          if (bpow * kSlack > blo) blo = bpow * kSlack;
-        }
-      }
-    };
-    // The admission threshold is shared by the group: any candidate found anywhere in the
-    // group raises it, so a lane rarely leaves the fast loop.  It only ever holds powers of
-    // real candidates, so the group maximum always passes it.
-    volatile unsigned *gbest = grp_best + g;
-    auto publish = [&]() { if (bpow > 0.0f) atomicMax(grp_best + g, __float_as_uint(bpow)); };
-    auto refresh = [&]() -> bool {
-      const float gb = __uint_as_float(*gbest) * kSlack;
-      if (gb > blo) { blo = gb; return true; }
-      return false;
-    };
-    const bool active = i0 < nb && kma > kmi;
-    // seed with the widest window of every start
-    if (active) {
+  // ---- per 32-entry chunk of end bins: maximum and minimum of the flux prefix
+  const int elast = nb + kma;  // last written prefix entry
+  for (int item = warp; item < (int)nfrem * nchunk; item += kThreads / 32) {
+    const int f = item / nchunk, c = item - f * nchunk;
+    const float2 *P = reinterpret_cast<const float2 *>(sm + (size_t)f * a.region);
+    const int e = 32 * c + lane;
+    const float v = e <= elast ? P[e].x : 0.0f;
+    float mx = e <= elast ? v : -INFINITY, mn = e <= elast ? v : INFINITY;
 #pragma unroll
-      for (int r = 0; r < R; ++r) {
-        const int e = i0 + r + kma;
-        if (i0 + r < nb) consider(r, P[padi<R>(e)], e);
-      }
-      publish();
+    for (int o = 16; o > 0; o >>= 1) {
+      mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+      mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
     }
-    group_bar(1 + g, Tg);
-    if (active) {
-      refresh();
-      const int ebeg = i0 + kmi + 1;
-      const int eend = min(i0 + R - 1 + kma, nb + kma);
-      // Body: every start has k in range and kk > kkmi, so no per-candidate checks.
-      // kk is smallest for the last start; find the first end where it passes kkmi.
-      int fa = i0 + R + kmi, fb = i0 + kma;
-      {
-        int x0 = fa, x1 = fb + 1;
-        const float need = c_last + kkmi_f;
-        while (x0 < x1) {
-          const int mid = (x0 + x1) >> 1;
-          if (P[padi<R>(mid)].y > need) x1 = mid; else x0 = mid + 1;
-        }
-        fa = x0;
+    if (lane == 0) reinterpret_cast<float2 *>(sm + (size_t)f * a.region)[lp + c] = make_float2(mx, mn);
+  }
+  // ---- seed every frequency's threshold with the widest window of every start
+  auto window_power = [&](const float2 *P, int i, int e, float &pw) -> bool {
+    const float2 Pi = P[i], Pe = P[e];
+    const float s = Pe.x - Pi.x;
+    const float kk = Pe.y - Pi.y;
+    const float den = kk * ((Nf + Pi.y) - Pe.y);
+    if (!(kk > kkmi_f)) return false;
+    pw = __fdiv_rn(s * s, den);
+    return pw > 0.0f;
+  };
+  if (kma > kmi) {
+    for (int idx = tid; idx < (int)nfrem * nb; idx += kThreads) {
+      const int f = idx / nb, i = idx - f * nb;
+      const float2 *P = reinterpret_cast<const float2 *>(sm + (size_t)f * a.region);
+      float pw;
+      if (window_power(P, i, i + kma, pw)) {
+        atomicMax(best_thr + f, __float_as_uint(pw));
+        atomicMax(best_key + f, pack_key(pw, i, i + kma));
       }
-      // head and tail with full checks
-      auto checked = [&](int e_from, int e_to) {
-        for (int e = e_from; e <= e_to; ++e) {
-          const float2 Pe = P[padi<R>(e)];
-          const unsigned base = (unsigned)(e - i0 - kmi - 1);
+    }
+  }
+  __syncthreads();
+
+  // ---- candidate windows [i, e), k = e - i in (kmi, kma], kk > kkmi.  Work unit: a chunk of
+  // 32 consecutive end bins against kRS consecutive start bins.  The power of every window in
+  // the unit is bounded by
+  //   max(Pmax - ys_min, ys_max - Pmin)^2 / min(den(kk_lo), den(kk_hi))
+  // (den = kk (N - kk) is concave in kk), and units whose bound is below the frequency's shared
+  // running best (times the pre-test slack) cannot hold the maximum.  A warp takes four
+  // consecutive start groups; each lane bounds one (start group, chunk) unit, and the warp then
+  // evaluates the surviving units together, one end bin per lane.
+  const int ntask_f = (nb + kRS - 1) / kRS;          // start groups per frequency
+  const int ngrp_f = (ntask_f + 3) / 4;              // warp jobs per frequency
+  const int njob = (kma > kmi) ? (int)nfrem * ngrp_f : 0;
+  const int span_chunks = ((kRS - 1 + kma - kmi - 1) >> 5) + 2;   // chunks one start group touches
+  for (;;) {
+    int job = 0;
+    if (lane == 0) job = atomicAdd(&task_ctr, 1);
+    job = __shfl_sync(0xffffffffu, job, 0);
+    if (job >= njob) break;
+    const int f = job / ngrp_f;
+    const int t0 = (job - f * ngrp_f) * 4;
+    const float2 *P = reinterpret_cast<const float2 *>(sm + (size_t)f * a.region);
+    const float2 *CM = P + lp;
+    // this lane's start group for bounding
+    const int kb = lane >> 3, mb = lane & 7;
+    const int sb = (t0 + kb) * kRS;
+    const bool grp_ok = t0 + kb < ntask_f;
+    int b_elo = 0, b_ehi = -1;
+    float b_ysmin = 0.0f, b_ysmax = 0.0f, b_c0 = 0.0f, b_cl = 0.0f;
+    if (grp_ok) {
+      const int nrs_b = min(kRS, nb - sb);
+      b_elo = sb + kmi + 1;
+      b_ehi = min(sb + nrs_b - 1 + kma, elast);
+      b_ysmin = INFINITY;
+      b_ysmax = -INFINITY;
+      for (int r = 0; r < nrs_b; ++r) {
+        const float y = P[sb + r].x;
+        b_ysmin = fminf(b_ysmin, y);
+        b_ysmax = fmaxf(b_ysmax, y);
+      }
+      b_c0 = P[sb].y;
+      b_cl = P[sb + nrs_b - 1].y;
+    }
+    for (int cbase = 0; cbase < span_chunks; cbase += 8) {
+      // bound of unit (start group kb, chunk c) on this lane
+      const float thr = __uint_as_float(best_thr[f]) * kSlack;
+      const int c = (b_elo >> 5) + cbase + mb;
+      bool keep = false;
+      if (grp_ok && c <= (b_ehi >> 5)) {
+        const int ce_lo = max(32 * c, b_elo), ce_hi = min(32 * c + 31, b_ehi);
+        const float kk_hi = P[ce_hi].y - b_c0;
+        if (kk_hi > kkmi_f) {
+          const float kk_lo = fmaxf(P[ce_lo].y - b_cl, kkmi_f + 1.0f);
+          const float den_min = fminf(kk_lo * (Nf - kk_lo), kk_hi * (Nf - kk_hi));
+          const float2 cm = CM[c];
+          const float smax = fmaxf(cm.x - b_ysmin, b_ysmax - cm.y);
+          keep = !(den_min > 0.0f && smax * smax < thr * den_min);
+        }
+      }
+      unsigned live = __ballot_sync(0xffffffffu, keep);
+      int cur = -1;  // start group whose registers are loaded
+      float ys[kRS] = {}, beta[kRS] = {}, gamma[kRS] = {};
+      float blo = 0.0f, c0 = 0.0f, clast = 0.0f, bpow = 0.0f;
+      int bi = INT_MAX, be = INT_MAX, s0 = 0, nrs = 0, elo = 0, ehi = -1;
+      auto coeffs = [&]() {
 #pragma unroll
-          for (int r = 0; r < R; ++r)
-            if (base - (unsigned)r < (unsigned)(kma - kmi)) consider(r, Pe, e);
+        for (int r = 0; r < kRS; ++r) {
+          const float cr = P[s0 + r].y;
+          const float ar = cr - c0, br = (Nf + cr) - c0;
+          beta[r] = -blo * (ar + br);
+          gamma[r] = (blo * ar) * br;
         }
       };
-      if (fa > fb) {
-        checked(ebeg, eend);
-      } else {
-        checked(ebeg, fa - 1);
-        refresh();
-        // -blo*den = blo*u^2 + beta_r*u + gamma_r in counts u centred on the first start
-        const float c0 = P[padi<R>(i0)].y;
-        float beta[R], gamma[R];
-        auto coeffs = [&]() {
-#pragma unroll
-          for (int r = 0; r < R; ++r) {
-            const float cr = P[padi<R>(i0 + r)].y;
-            const float ar = cr - c0, br = (Nf + cr) - c0;
-            beta[r] = -blo * (ar + br);
-            gamma[r] = (blo * ar) * br;
+      // exact evaluation of (start s0 + r, end e): pre-test, then the rounded quotient
+      auto consider = [&](int r, float2 Pe, int e) {
+        const float cr = P[s0 + r].y;
+        const float s = Pe.x - ys[r];
+        const float kk = Pe.y - cr;
+        const float den = kk * ((Nf + cr) - Pe.y);
+        const float s2 = s * s;
+        if (r < nrs && kk > kkmi_f && fmaf(-blo, den, s2) >= 0.0f) {
+          const float pw = __fdiv_rn(s2, den);
+          if (pw > 0.0f && better(pw, s0 + r, e, bpow, bi, be)) {
+            bpow = pw;
+            bi = s0 + r;
+            be = e;
           }
-        };
-        coeffs();
-        for (int e = fa; e <= fb; ++e) {
-          const float2 Pe = P[padi<R>(e)];
+        }
+      };
+      auto flush = [&]() {  // warp best of the loaded start group into the frequency record
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const float op = __shfl_down_sync(0xffffffffu, bpow, o);
+          const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+          const int oe = __shfl_down_sync(0xffffffffu, be, o);
+          if (better(op, oi, oe, bpow, bi, be)) { bpow = op; bi = oi; be = oe; }
+        }
+        if (lane == 0 && bi != INT_MAX) atomicMax(best_key + f, pack_key(bpow, bi, be));
+        bpow = 0.0f;
+        bi = be = INT_MAX;
+      };
+      while (live) {
+        const int src = __ffs(live) - 1;
+        live &= live - 1;
+        const int k = src >> 3;
+        const int cc = (((t0 + k) * kRS + kmi + 1) >> 5) + cbase + (src & 7);
+        if (k != cur) {
+          if (cur >= 0) flush();
+          cur = k;
+          s0 = (t0 + k) * kRS;
+          nrs = min(kRS, nb - s0);
+          elo = s0 + kmi + 1;
+          ehi = min(s0 + nrs - 1 + kma, elast);
+#pragma unroll
+          for (int r = 0; r < kRS; ++r) ys[r] = P[s0 + r].x;  // entries up to nb + kRS - 1 exist
+          c0 = P[s0].y;
+          clast = P[s0 + nrs - 1].y;
+          blo = __uint_as_float(best_thr[f]) * kSlack;
+          coeffs();
+        } else {
+          const float gb = __uint_as_float(best_thr[f]) * kSlack;
+          if (gb > blo) { blo = gb; coeffs(); }
+        }
+        const int e = 32 * cc + lane;
+        const float before = bpow;
+        const bool interior = nrs == kRS && 32 * cc >= s0 + kRS + kmi && 32 * cc + 31 <= s0 + kma &&
+                              P[32 * cc].y - clast > kkmi_f;
+        if (interior) {
+          const float2 Pe = P[e];
           const float u = Pe.y - c0;
           const float G = (blo * u) * u;
           unsigned neg = 0xffffffffu;
 #pragma unroll
-          for (int r = 0; r < R; ++r) {
+          for (int r = 0; r < kRS; ++r) {
             const float s = Pe.x - ys[r];
-            const float t = fmaf(s, s, fmaf(u, beta[r], G + gamma[r]));
-            neg &= __float_as_uint(t);
+            neg &= __float_as_uint(fmaf(s, s, fmaf(u, beta[r], G + gamma[r])));
           }
-          if (!(neg >> 31)) {  // some candidate may reach the shared best
-            const float before = bpow;
+          if (!(neg >> 31)) {
 #pragma unroll
-            for (int r = 0; r < R; ++r) {
+            for (int r = 0; r < kRS; ++r) {
               const float s = Pe.x - ys[r];
               if (fmaf(s, s, fmaf(u, beta[r], G + gamma[r])) >= 0.0f) consider(r, Pe, e);
             }
-            if (bpow != before) publish();
-            refresh();
-            coeffs();
-          } else if (!((e - fa) & 15)) {
-            if (refresh()) coeffs();
           }
-        }
-        checked(fb + 1, eend);
-      }
-    }
-    // group reduction (max power, then lowest start, then lowest end)
+        } else if (e >= elo && e <= ehi) {
+          const float2 Pe = P[e];
+          const unsigned base = (unsigned)(e - s0 - kmi - 1);
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const float op = __shfl_down_sync(0xffffffffu, bpow, o);
-      const int oi = __shfl_down_sync(0xffffffffu, bi, o);
-      const int oe = __shfl_down_sync(0xffffffffu, be, o);
-      if (better(op, oi, oe, bpow, bi, be)) { bpow = op; bi = oi; be = oe; }
-    }
-    if (lane == 0) { red_p[warp] = bpow; red_i[warp] = bi; red_e[warp] = be; }
-    group_bar(1 + g, Tg);
-    if (gtid == 0) {
-      for (int w = 1; w < nwg; ++w) {
-        const float op = red_p[gw0 + w];
-        const int oi = red_i[gw0 + w], oe = red_e[gw0 + w];
-        if (better(op, oi, oe, bpow, bi, be)) { bpow = op; bi = oi; be = oe; }
+          for (int r = 0; r < kRS; ++r)
+            if (base - (unsigned)r < (unsigned)(kma - kmi)) consider(r, Pe, e);
+        }
+        if (bpow != before) atomicMax(best_thr + f, __float_as_uint(bpow));
       }
-      const size_t o = (size_t)q * a.nf + j0 + f;
-      const bool found = bi != INT_MAX;
-      a.blsp[o] = found ? ldexpf(sqrtf(bpow), -a.sx[q]) : 0.0f;
-      if (a.ph1) a.ph1[o] = found ? (uint32_t)bi : 0u;
-      if (a.ph2) a.ph2[o] = found ? (uint32_t)(be - 1) : 0u;
+      if (cur >= 0) flush();
     }
+  }
+  __syncthreads();
+  // ---- outputs
+  if (tid < (int)nfrem) {
+    const unsigned long long key = best_key[tid];
+    const size_t o = (size_t)q * a.nf + j0 + tid;
+    const bool found = key != 0ull;
+    const float pw = __uint_as_float((unsigned)(key >> 32));
+    const unsigned ie = 0xffffffffu - (unsigned)(key & 0xffffffffull);
+    a.blsp[o] = found ? ldexpf(sqrtf(pw), -a.sx[q]) : 0.0f;
+    if (a.ph1) a.ph1[o] = found ? (ie >> 15) : 0u;
+    if (a.ph2) a.ph2[o] = found ? (ie & 0x7fffu) - 1u : 0u;
   }
 }
 
@@ -577,27 +663,28 @@ __global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1) bls_fol
 // host side
 
 struct Plan {
-  uint32_t F, region, Tg, G, tiles;
+  uint32_t F, region, Tg, G, tiles, lp;
   int R;
   size_t smem;
 };
 
 int make_plan(uint32_t nb, uint32_t kma, uint32_t nf, Plan *p) {
   const int R = nb <= 4096 ? 8 : 16;
-  const int logR = R == 16 ? 4 : 3;
   uint32_t Tg = (nb + R - 1) / R;
   Tg = (Tg + 31) / 32 * 32;
   if (Tg < 64) Tg = 64;  // at most 8 groups: named barriers 1..8
-  // prefix entries 0 .. nb + kma are written; starts read entries up to nb + R - 2
-  const uint32_t last = nb + (kma > (uint32_t)R ? kma : (uint32_t)R);
-  uint32_t region = last + (last >> logR) + 1;
-  if (region < nb) region = nb;
+  // prefix entries 0 .. nb + kma are written and scan tasks read starts up to nb + kRS - 2;
+  // the prefix array is padded to whole 32-entry chunks, followed by one (max, min) pair
+  // per chunk
+  const uint32_t last = nb + (kma > (uint32_t)kRS ? kma : (uint32_t)kRS);
+  const uint32_t lp = (last + 1 + 31) / 32 * 32;
+  uint32_t region = lp + lp / 32;
   region = (region + 1) & ~1u;  // 16-byte multiple for the zero fill
   const uint32_t G = kThreads / Tg;
   const size_t per_f = (size_t)region * 8;
-  // Frequencies per block: fill about half an SM's shared memory so two blocks can
-  // overlap their fold and scan phases; at least one round of groups.
-  const size_t budget = 110 * 1024;
+  // Frequencies per block: fill half an SM's shared memory so two blocks can overlap their
+  // fold and scan phases; at least one round of groups.
+  const size_t budget = (size_t)gtrap::smem_per_sm() / 2 - 2048;
   uint32_t F = (uint32_t)(budget / per_f);
   if (F < G) F = G;
   if (F > 64) F = 64;
@@ -612,6 +699,7 @@ int make_plan(uint32_t nb, uint32_t kma, uint32_t nf, Plan *p) {
   }
   p->F = F;
   p->region = region;
+  p->lp = lp;
   p->Tg = Tg;
   p->G = G;
   p->R = R;
@@ -697,7 +785,7 @@ int run_bls(bool full, float *blsp, uint32_t *phase1, uint32_t *phase2, const fl
   ba.X = X; ba.AB = AB; ba.T = full ? T : tu; ba.sx = sx; ba.nv = nv; ba.ntrue = full ? ntrue : nullptr;
   ba.n = n; ba.n_den = n; ba.nq = nq; ba.nf = nf; ba.nb = nb; ba.kma = kma;
   ba.kmi = kmi_eff; ba.kkmi = kkmi_eff; ba.fmin = fmin; ba.df = df;
-  ba.F = p.F; ba.tiles = p.tiles; ba.region = p.region; ba.Tg = p.Tg; ba.G = p.G;
+  ba.F = p.F; ba.tiles = p.tiles; ba.region = p.region; ba.Tg = p.Tg; ba.G = p.G; ba.lp = p.lp;
   ba.lognb = gtrap::is_pow2(nb) ? gtrap::ilog2u(nb) : 0;
   ba.CB = CB;
   ba.ab_stride = full ? n : 0;

@@ -15,6 +15,7 @@ thread_local char g_last_error[512] = "no error";
 constexpr int kMaxDevices = 64;
 int g_sm_count[kMaxDevices];
 int g_smem_optin[kMaxDevices];
+int g_smem_sm[kMaxDevices];
 std::mutex g_attr_mutex;
 
 int current_device() {
@@ -56,6 +57,16 @@ int max_smem_optin() {
     g_smem_optin[dev] = v > 0 ? v : 48 * 1024;
   }
   return g_smem_optin[dev];
+}
+
+int smem_per_sm() {
+  int dev = current_device();
+  if (!g_smem_sm[dev]) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    g_smem_sm[dev] = v > 0 ? v : 100 * 1024;
+  }
+  return g_smem_sm[dev];
 }
 
 int ensure_smem(const void *func, size_t bytes, const char *what) {

@@ -22,6 +22,9 @@ int sm_count();
 // Maximum opt-in dynamic shared memory per block of the current device (cached).
 int max_smem_optin();
 
+// Shared memory per SM of the current device (cached).
+int smem_per_sm();
+
 // Raise the dynamic shared-memory limit of `func` to `bytes` once per device.
 int ensure_smem(const void *func, size_t bytes, const char *what);
 
