@@ -234,7 +234,6 @@ __global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1) bls_fol
   __shared__ int scan_c[kThreads / 32];
   __shared__ unsigned long long best_key[64];    // per frequency: best (power, -start, -end)
   __shared__ unsigned best_thr[64];              // per frequency: running best power (float bits)
-  __shared__ int task_ctr;                       // next scan task of this block
   __shared__ int scan_m[kThreads / 32];          // per-warp maximum bin count
   __shared__ unsigned drop_cnt[64];              // FP32-phase samples landing on bin nb
 
@@ -450,7 +449,6 @@ __global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1) bls_fol
     }
   }
   if (tid < 64) { best_key[tid] = 0ull; best_thr[tid] = 0u; }
-  if (tid == 0) task_ctr = 0;
   __syncthreads();
 
   // ---- per 32-entry chunk of end bins: maximum and minimum of the flux prefix
@@ -479,13 +477,21 @@ __global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1) bls_fol
     return pw > 0.0f;
   };
   if (kma > kmi) {
-    for (int idx = tid; idx < (int)nfrem * nb; idx += kThreads) {
-      const int f = idx / nb, i = idx - f * nb;
+    const int per_f = (nb + 31) & ~31;  // whole warps per frequency
+    for (int idx = tid; idx < (int)nfrem * per_f; idx += kThreads) {
+      const int f = idx / per_f, i = idx - f * per_f;
       const float2 *P = reinterpret_cast<const float2 *>(sm + (size_t)f * a.region);
-      float pw;
-      if (window_power(P, i, i + kma, pw)) {
-        atomicMax(best_thr + f, __float_as_uint(pw));
-        atomicMax(best_key + f, pack_key(pw, i, i + kma));
+      float pw = 0.0f;
+      if (i < nb && !window_power(P, i, i + kma, pw)) pw = 0.0f;
+      unsigned long long key = pw > 0.0f ? pack_key(pw, i, i + kma) : 0ull;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long ok = __shfl_xor_sync(0xffffffffu, key, o);
+        key = ok > key ? ok : key;
+      }
+      if (lane == 0 && key) {
+        atomicMax(best_thr + f, (unsigned)(key >> 32));
+        atomicMax(best_key + f, key);
       }
     }
   }
@@ -503,11 +509,7 @@ __global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1) bls_fol
   const int ngrp_f = (ntask_f + 3) / 4;              // warp jobs per frequency
   const int njob = (kma > kmi) ? (int)nfrem * ngrp_f : 0;
   const int span_chunks = ((kRS - 1 + kma - kmi - 1) >> 5) + 2;   // chunks one start group touches
-  for (;;) {
-    int job = 0;
-    if (lane == 0) job = atomicAdd(&task_ctr, 1);
-    job = __shfl_sync(0xffffffffu, job, 0);
-    if (job >= njob) break;
+  for (int job = warp; job < njob; job += kThreads / 32) {
     const int f = job / ngrp_f;
     const int t0 = (job - f * ngrp_f) * 4;
     const float2 *P = reinterpret_cast<const float2 *>(sm + (size_t)f * a.region);
@@ -569,7 +571,8 @@ __global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1) bls_fol
         const float kk = Pe.y - cr;
         const float den = kk * ((Nf + cr) - Pe.y);
         const float s2 = s * s;
-        if (r < nrs && kk > kkmi_f && fmaf(-blo, den, s2) >= 0.0f) {
+        // den <= 0 (a window holding every sample) gives an infinite or negative power
+        if (r < nrs && kk > kkmi_f && (den <= 0.0f || fmaf(-blo, den, s2) >= 0.0f)) {
           const float pw = __fdiv_rn(s2, den);
           if (pw > 0.0f && better(pw, s0 + r, e, bpow, bi, be)) {
             bpow = pw;
@@ -579,6 +582,7 @@ __global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1) bls_fol
         }
       };
       auto flush = [&]() {  // warp best of the loaded start group into the frequency record
+        if (!__any_sync(0xffffffffu, bi != INT_MAX)) return;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
           const float op = __shfl_down_sync(0xffffffffu, bpow, o);
@@ -614,31 +618,31 @@ __global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1) bls_fol
         }
         const int e = 32 * cc + lane;
         const float before = bpow;
-        const bool interior = nrs == kRS && 32 * cc >= s0 + kRS + kmi && 32 * cc + 31 <= s0 + kma &&
-                              P[32 * cc].y - clast > kkmi_f;
-        if (interior) {
+        // interior: every (lane, start) has k in range; otherwise windows outside
+        // (kmi, kma] or past the last end are masked before the fast test
+        const bool interior = nrs == kRS && 32 * cc >= s0 + kRS + kmi && 32 * cc + 31 <= s0 + kma;
+        if (interior || (e >= elo && e <= ehi)) {
           const float2 Pe = P[e];
           const float u = Pe.y - c0;
           const float G = (blo * u) * u;
+          const unsigned base = (unsigned)(e - s0 - kmi - 1);
           unsigned neg = 0xffffffffu;
 #pragma unroll
           for (int r = 0; r < kRS; ++r) {
             const float s = Pe.x - ys[r];
-            neg &= __float_as_uint(fmaf(s, s, fmaf(u, beta[r], G + gamma[r])));
+            const float t = fmaf(s, s, fmaf(u, beta[r], G + gamma[r]));
+            const bool in = interior || base - (unsigned)r < (unsigned)(kma - kmi);
+            neg &= in ? __float_as_uint(t) : 0x80000000u;
           }
-          if (!(neg >> 31)) {
+          if (!(neg >> 31)) {  // kk and the exact pre-test are checked in consider
 #pragma unroll
             for (int r = 0; r < kRS; ++r) {
               const float s = Pe.x - ys[r];
-              if (fmaf(s, s, fmaf(u, beta[r], G + gamma[r])) >= 0.0f) consider(r, Pe, e);
+              const float t = fmaf(s, s, fmaf(u, beta[r], G + gamma[r]));
+              const bool in = interior || base - (unsigned)r < (unsigned)(kma - kmi);
+              if (in && !(t < 0.0f)) consider(r, Pe, e);
             }
           }
-        } else if (e >= elo && e <= ehi) {
-          const float2 Pe = P[e];
-          const unsigned base = (unsigned)(e - s0 - kmi - 1);
-#pragma unroll
-          for (int r = 0; r < kRS; ++r)
-            if (base - (unsigned)r < (unsigned)(kma - kmi)) consider(r, Pe, e);
         }
         if (bpow != before) atomicMax(best_thr + f, __float_as_uint(bpow));
       }
