@@ -15,6 +15,7 @@ from . import _build
 c_float_p = C.POINTER(C.c_float)
 vp = C.c_void_p
 u32 = C.c_uint32
+u64 = C.c_uint64
 i32 = C.c_int32
 f32 = C.c_float
 f64 = C.c_double
@@ -44,6 +45,15 @@ _SIGNATURES = {
     "gtrap_geebls_simple_workspace_size": (sz, [u32, u32, u32]),
     "gtrap_geebls_simple": (C.c_int, [vp, vp, vp, vp, vp, u32, u32, u32, u32, u32, u32, u32,
                                       f32, f32, u32, u32, vp, sz, vp]),
+    "gtrap_gfilter_packed": (C.c_int, [vp, vp, vp, u32, u32, u32, vp]),
+    "gtrap_bls_offsets": (C.c_int, [vp, u32, vp, vp, vp]),
+    "gtrap_bls_tile_frequencies": (u32, [u32, u32]),
+    "gtrap_bls_pool_bytes": (sz, [u64, u32]),
+    "gtrap_bls_prepare": (C.c_int, [vp, u32, u32, vp, vp, u64, vp, sz, u32, vp]),
+    "gtrap_bls_run": (C.c_int, [vp, vp, vp, u32, vp, vp, sz, u64, u32, u32, u32, u32, u32, u32,
+                                vp, vp, vp, vp, vp]),
+    "gtrap_gtls_run": (C.c_int, [vp, vp, vp, u32, vp, vp, i32, i32, i32, i32, u32, u32, vp, vp, vp,
+                                 vp, vp, vp, vp]),
     "gtrap_blsstat": (C.c_int, [vp, vp, vp, u32, u32, f64, f64, u32, vp, vp, vp, vp, vp]),
     "gtrap_getmax": (C.c_int, [vp, vp, vp, u32, u32, u32, vp, vp, vp, vp, vp, vp, vp]),
     "gtrap_gtls": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, i32, i32, i32, i32, i32, f32, f32, f32,

@@ -1,0 +1,475 @@
+"""Packed (ragged) batches: many light curves of different lengths and grids, one device pool.
+
+Curves of different lengths, cadences and frequency grids are concatenated into flat
+float32 time and flux arrays (curve q = samples ``[off[q], off[q] + n[q])``).  One call of
+:meth:`RaggedBatch.launch` issues, on one stream and without host synchronisation,
+
+1. the running-median detrend of every curve (``gtrap_gfilter_packed``),
+2. the per-curve offset of the BLS curves (``gtrap_bls_offsets``; get_offset,
+   gtrap/gfilter.py:94-101),
+3. quantisation and exact phase encoding of the BLS samples (``gtrap_bls_prepare``),
+4. one persistent BLS launch that pops (curve, frequency tile) items from a device work
+   queue (``gtrap_bls_run``; the geebls statistic, include/geebls.h:35-165), and
+5. one persistent GTLS launch over (curve, 32-epoch tile) items (``gtrap_gtls_run``; the
+   gtls statistic, include/gtls_simple.h:51-404),
+
+so the whole sequence can be captured in a CUDA graph (:meth:`RaggedBatch.capture`) and
+replayed.  The reference has no packed path: it launches one kernel per ``[n, nq]`` image
+(gtrap/geebls.py:10-22, gtrap/gtls.py:11-27), so a set of curves with different lengths or
+grids costs one launch sequence per curve (:func:`run_plain`).  Every curve's result here is
+bit-identical to the plain entry points run on that curve alone: the kernels are the same and
+every sum has a fixed order.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _native as N
+from . import api
+from ._dev import as_ptr, require_cuda, stream_handle
+
+# Layouts of the C structs (include/gtrap_gb300.h).
+BLS_CURVE = np.dtype([("off", "<u8"), ("out", "<u8"), ("n", "<u4"), ("nf", "<u4"),
+                      ("fmin", "<f4"), ("df", "<f4"), ("offset", "<f4"), ("ntrue", "<u4"),
+                      ("sx", "<i4"), ("nv", "<u4"), ("cb", "<i4"), ("kkmi", "<u4")])
+TLS_CURVE = np.dtype([("off", "<u8"), ("out", "<u8"), ("nt", "<i4"), ("nsc", "<i4"),
+                      ("wmax", "<f4"), ("dw", "<f4"), ("deltat", "<f4"), ("reserved", "<u4")])
+SEGMENT = np.dtype([("curve", "<u4"), ("tile0", "<u4")])
+assert BLS_CURVE.itemsize == 56 and TLS_CURVE.itemsize == 40 and SEGMENT.itemsize == 8
+
+TLS_TILE = 32  # epochs per GTLS work item
+
+
+@dataclass(frozen=True)
+class BlsSpec:
+    """Launch-wide BLS bin grid (shared-memory layout of the persistent kernel)."""
+    nb: int = 2048
+    kma: int = 205
+    kmi: int = 10
+    phase: str = "exact"
+
+    @property
+    def flags(self) -> int:
+        return api._phase_flags(self.phase)
+
+
+@dataclass(frozen=True)
+class TlsSpec:
+    """Launch-wide GTLS template grid: nw widths, nl ingress widths, mode 0 simple / 1 absolute."""
+    nw: int = 8
+    nl: int = 16
+    mode: int = 0
+    fix_a: bool = False
+
+    @property
+    def flags(self) -> int:
+        return N.TLS_FIX_A if self.fix_a else 0
+
+
+@dataclass
+class _Bls:
+    t: np.ndarray
+    x: np.ndarray
+    nf: int
+    fmin: float
+    df: float
+    kkmi: int
+    ntrue: int
+    offset: float
+
+
+@dataclass
+class _Tls:
+    t: np.ndarray
+    x: np.ndarray
+    nt: int
+    nsc: int
+    wmax: float
+    dw: float
+    deltat: float
+
+
+def _tiles(count: int, per: int) -> int:
+    return (count + per - 1) // per
+
+
+class RaggedBatch:
+    """A device-resident packed batch of BLS and GTLS requests.
+
+    Add curves with :meth:`add_bls` / :meth:`add_tls`, then :meth:`build` uploads them.
+    ``detrend_r`` (window 2r+1) detrends every curve before its search; with
+    ``auto_offset`` (default: when detrending) the BLS offsets are computed on the device
+    from the detrended flux, otherwise the per-curve offsets given to :meth:`add_bls` are
+    used."""
+
+    def __init__(self, bls: BlsSpec = BlsSpec(), tls: TlsSpec = TlsSpec(), detrend_r=None,
+                 auto_offset=None, device=None):
+        self.bls_spec = bls
+        self.tls_spec = tls
+        self.detrend_r = None if detrend_r is None else int(detrend_r)
+        self.auto_offset = (self.detrend_r is not None) if auto_offset is None else bool(auto_offset)
+        self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device) \
+            if torch.cuda.is_available() else None
+        self._bls: list[_Bls] = []
+        self._tls: list[_Tls] = []
+        self.built = False
+        self.F = None
+        self.bls_blocks = 0
+        self.tls_blocks = 0
+
+    # -- assembling ---------------------------------------------------------------------
+    def add_bls(self, t, x, nf, fmin, df, kkmi=None, qmi=0.005, ntrue=None, offset=0.0) -> int:
+        """Queue a masked-BLS request (geebls semantics: samples with t < 0 are not folded,
+        the power's denominator count is ``ntrue`` -- by default the valid samples --, and
+        windows must hold more than ``kkmi`` samples, by default ``int(n*qmi)``)."""
+        t = np.ascontiguousarray(t, np.float32).reshape(-1)
+        x = np.ascontiguousarray(x, np.float32).reshape(-1)
+        n = t.size
+        if n == 0 or x.size != n:
+            raise ValueError("a BLS curve needs n >= 1 samples of time and flux")
+        if n >= 1 << 23:
+            raise ValueError("n=%d must be below 2^23" % n)
+        if nf < 1:
+            raise ValueError("nf must be positive")
+        self._bls.append(_Bls(t, x, int(nf), float(fmin), float(df),
+                              int(n * qmi) if kkmi is None else int(kkmi),
+                              int(np.count_nonzero(t >= 0)) if ntrue is None else int(ntrue),
+                              float(offset)))
+        self.built = False
+        return len(self._bls) - 1
+
+    def add_tls(self, t, x, nsc, wmax, dw, deltat, nt=None) -> int:
+        """Queue a GTLS request over the first ``nt`` (default: all) samples."""
+        t = np.ascontiguousarray(t, np.float32).reshape(-1)
+        x = np.ascontiguousarray(x, np.float32).reshape(-1)
+        n = t.size
+        nt = n if nt is None else int(nt)
+        if n == 0 or x.size != n or not 1 <= nt <= n:
+            raise ValueError("a GTLS curve needs 1 <= nt <= n samples of time and flux")
+        if not 1 <= int(nsc) <= 65536:
+            raise ValueError("nsc must be in [1, 65536]")
+        self._tls.append(_Tls(t, x, nt, int(nsc), float(wmax), float(dw), float(deltat)))
+        self.built = False
+        return len(self._tls) - 1
+
+    @property
+    def n_bls(self) -> int:
+        return len(self._bls)
+
+    @property
+    def n_tls(self) -> int:
+        return len(self._tls)
+
+    @property
+    def bls_evals(self) -> int:
+        """(curve, trial frequency) pairs of the BLS requests."""
+        return sum(c.nf for c in self._bls)
+
+    @property
+    def tls_evals(self) -> int:
+        """(curve, epoch) pairs of the GTLS requests."""
+        return sum(c.nt for c in self._tls)
+
+    # -- upload ---------------------------------------------------------------------------
+    def build(self) -> "RaggedBatch":
+        """Pack the curves (BLS first, then GTLS) and upload them with their tables."""
+        require_cuda()
+        dev = self.device
+        items = list(self._bls) + list(self._tls)
+        if not items:
+            raise ValueError("empty batch")
+        lens = np.array([c.t.size for c in items], np.uint64)
+        offs = np.zeros(len(items) + 1, np.uint64)
+        np.cumsum(lens, out=offs[1:])
+        self.total = int(offs[-1])
+        self.bls_total = int(offs[len(self._bls)])
+        self.max_n = int(lens.max())
+        self.max_n_bls = int(lens[:len(self._bls)].max()) if self._bls else 0
+        t_h = torch.empty(self.total, dtype=torch.float32, pin_memory=True)
+        x_h = torch.empty(self.total, dtype=torch.float32, pin_memory=True)
+        tn, xn = t_h.numpy(), x_h.numpy()
+        for k, c in enumerate(items):
+            a, b = int(offs[k]), int(offs[k + 1])
+            tn[a:b] = c.t
+            xn[a:b] = c.x
+        self.offs_host = offs
+        self.t = t_h.to(dev, non_blocking=True)
+        self.x = x_h.to(dev, non_blocking=True)
+        self.offs = torch.from_numpy(offs.view(np.int64)).to(dev)
+        self.resid = torch.empty_like(self.x) if self.detrend_r is not None else self.x
+
+        nbls = len(self._bls)
+        bt = np.zeros(nbls, BLS_CURVE)
+        out = 0
+        for k, c in enumerate(self._bls):
+            bt[k]["off"] = offs[k]
+            bt[k]["out"] = out
+            bt[k]["n"] = c.t.size
+            bt[k]["nf"] = c.nf
+            bt[k]["fmin"] = c.fmin
+            bt[k]["df"] = c.df
+            bt[k]["offset"] = c.offset
+            bt[k]["ntrue"] = c.ntrue
+            bt[k]["kkmi"] = c.kkmi
+            out += c.nf
+        self.bls_table = bt
+        self.bls_out = out
+        tt = np.zeros(len(self._tls), TLS_CURVE)
+        out = 0
+        for k, c in enumerate(self._tls):
+            tt[k]["off"] = offs[nbls + k]
+            tt[k]["out"] = out
+            tt[k]["nt"] = c.nt
+            tt[k]["nsc"] = c.nsc
+            tt[k]["wmax"] = c.wmax
+            tt[k]["dw"] = c.dw
+            tt[k]["deltat"] = c.deltat
+            out += c.nt
+        self.tls_table = tt
+        self.tls_out = out
+        self.max_nsc = int(tt["nsc"].max()) if len(tt) else 1
+
+        def up(arr):
+            return torch.from_numpy(np.frombuffer(arr.tobytes(), np.uint8).copy()).to(dev)
+
+        self.bls_curves = up(bt) if nbls else None
+        self.tls_curves = up(tt) if len(tt) else None
+        flags = self.bls_spec.flags
+        self.pool_bytes = int(N.fn("gtrap_bls_pool_bytes")(max(self.bls_total, 1), flags))
+        self.pool = torch.empty(self.pool_bytes, dtype=torch.uint8, device=dev) if nbls else None
+        self.blsp = torch.empty(max(self.bls_out, 1), dtype=torch.float32, device=dev)
+        self.ph1 = torch.empty(max(self.bls_out, 1), dtype=torch.int32, device=dev)
+        self.ph2 = torch.empty(max(self.bls_out, 1), dtype=torch.int32, device=dev)
+        self.tls_outs = tuple(torch.empty(max(self.tls_out, 1), dtype=torch.float32, device=dev)
+                              for _ in range(5))
+        self.counters = torch.zeros(2, dtype=torch.int32, device=dev)
+        self.built = True
+        if self.F is None:
+            self.set_config(default_F(self.bls_spec), 0, 0)
+        else:
+            self.set_config(self.F, self.bls_blocks, self.tls_blocks)
+        return self
+
+    def _bls_segments(self, F, curves=None):
+        """One segment per curve, largest fold (n) first so the longest items start early."""
+        idx = np.arange(self.n_bls) if curves is None else np.asarray(curves)
+        order = idx[np.argsort(-self.bls_table["n"][idx].astype(np.int64), kind="stable")]
+        segs = np.zeros(order.size, SEGMENT)
+        segs["curve"] = order
+        counts = (self.bls_table["nf"][order].astype(np.int64) + F - 1) // F
+        cum = np.zeros(order.size + 1, np.uint32)
+        np.cumsum(counts, out=cum[1:])
+        return segs, cum
+
+    def _tls_segments(self, curves=None):
+        idx = np.arange(self.n_tls) if curves is None else np.asarray(curves)
+        order = idx[np.argsort(-self.tls_table["nsc"][idx].astype(np.int64), kind="stable")]
+        segs = np.zeros(order.size, SEGMENT)
+        segs["curve"] = order
+        counts = (self.tls_table["nt"][order].astype(np.int64) + TLS_TILE - 1) // TLS_TILE
+        cum = np.zeros(order.size + 1, np.uint32)
+        np.cumsum(counts, out=cum[1:])
+        return segs, cum
+
+    def _upload_segments(self, segs, cum):
+        dev = self.device
+        return (torch.from_numpy(np.frombuffer(segs.tobytes(), np.uint8).copy()).to(dev),
+                torch.from_numpy(cum.view(np.int32).copy()).to(dev), int(segs.size))
+
+    def set_config(self, F: int, bls_blocks: int = 0, tls_blocks: int = 0):
+        """Frequencies per BLS tile and persistent block counts (0: one or two per SM for
+        BLS, the occupancy limit for GTLS)."""
+        if not self.built:
+            raise RuntimeError("build() the batch first")
+        self.F = int(F)
+        self.bls_blocks = int(bls_blocks)
+        self.tls_blocks = int(tls_blocks)
+        self.bls_q = self._upload_segments(*self._bls_segments(self.F)) if self.n_bls else None
+        self.tls_q = self._upload_segments(*self._tls_segments()) if self.n_tls else None
+
+    # -- launches -----------------------------------------------------------------------
+    def launch_prep(self, stream=None):
+        """Detrend, offsets and BLS sample encoding."""
+        st = stream_handle(stream)
+        if self.detrend_r is not None:
+            N.call("gtrap_gfilter_packed", as_ptr(self.x), as_ptr(self.resid), as_ptr(self.offs),
+                   self.n_bls + self.n_tls, self.max_n, self.detrend_r, st)
+        if self.n_bls:
+            if self.auto_offset:
+                N.call("gtrap_bls_offsets", as_ptr(self.bls_curves), self.n_bls, as_ptr(self.t),
+                       as_ptr(self.resid), st)
+            N.call("gtrap_bls_prepare", as_ptr(self.bls_curves), self.n_bls, self.max_n_bls,
+                   as_ptr(self.t), as_ptr(self.resid), self.bls_total, as_ptr(self.pool),
+                   self.pool_bytes, self.bls_spec.flags, st)
+
+    def launch_bls(self, stream=None, queue=None, blocks=None, F=None):
+        if not self.n_bls:
+            return
+        segs, cum, nseg = self.bls_q if queue is None else queue
+        s = self.bls_spec
+        N.call("gtrap_bls_run", as_ptr(self.bls_curves), as_ptr(segs), as_ptr(cum), nseg,
+               as_ptr(self.t), as_ptr(self.pool), self.pool_bytes, self.bls_total, s.nb, s.kma,
+               s.kmi, self.F if F is None else int(F), s.flags,
+               self.bls_blocks if blocks is None else int(blocks), as_ptr(self.counters[0:1]),
+               as_ptr(self.blsp), as_ptr(self.ph1), as_ptr(self.ph2), stream_handle(stream))
+
+    def launch_tls(self, stream=None, queue=None, blocks=None):
+        if not self.n_tls:
+            return
+        segs, cum, nseg = self.tls_q if queue is None else queue
+        s = self.tls_spec
+        o = self.tls_outs
+        N.call("gtrap_gtls_run", as_ptr(self.tls_curves), as_ptr(segs), as_ptr(cum), nseg,
+               as_ptr(self.t), as_ptr(self.resid), s.nw, s.nl, self.max_nsc, s.mode, s.flags,
+               self.tls_blocks if blocks is None else int(blocks), as_ptr(self.counters[1:2]),
+               *[as_ptr(a) for a in o], stream_handle(stream))
+
+    def launch(self, stream=None):
+        """The whole pipeline on one stream: prep, then the BLS and GTLS persistent launches."""
+        if not self.built:
+            raise RuntimeError("build() the batch first")
+        self.launch_prep(stream)
+        self.launch_bls(stream)
+        self.launch_tls(stream)
+
+    def capture(self) -> torch.cuda.CUDAGraph:
+        """Capture :meth:`launch` in a CUDA graph (after one eager run that also sets the
+        kernels' shared-memory limits).  Replays read the current contents of the batch's
+        device arrays, so new data of the same layout can be written in place."""
+        side = torch.cuda.Stream(self.device)
+        side.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(side):
+            self.launch()
+        torch.cuda.current_stream(self.device).wait_stream(side)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, capture_error_mode="thread_local"):
+            self.launch()
+        self.graph = g
+        return g
+
+    # -- results ------------------------------------------------------------------------
+    def bls_result(self, k: int):
+        """(blsp, phase1, phase2) of BLS request k as numpy arrays (synchronises)."""
+        o, nf = int(self.bls_table[k]["out"]), int(self.bls_table[k]["nf"])
+        return (self.blsp[o:o + nf].cpu().numpy(), self.ph1[o:o + nf].cpu().numpy(),
+                self.ph2[o:o + nf].cpu().numpy())
+
+    def tls_result(self, k: int):
+        """(sn, w, t0, l, hmax) of GTLS request k as numpy arrays (synchronises)."""
+        o, nt = int(self.tls_table[k]["out"]), int(self.tls_table[k]["nt"])
+        return tuple(a[o:o + nt].cpu().numpy() for a in self.tls_outs)
+
+
+def default_F(spec: BlsSpec) -> int:
+    """Frequencies per tile when not tuned: the choice of the plain entry point."""
+    F = int(N.fn("gtrap_bls_tile_frequencies")(spec.nb, spec.kma))
+    if F == 0:
+        raise ValueError("BLS bin grid nb=%d, kma=%d is out of range" % (spec.nb, spec.kma))
+    return F
+
+
+# -- autotuner ------------------------------------------------------------------------------
+_TUNED: dict = {}
+
+
+def _time_ms(fn, reps=1):
+    fn()
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(True), torch.cuda.Event(True)
+    s.record()
+    for _ in range(reps):
+        fn()
+    e.record()
+    torch.cuda.synchronize()
+    return s.elapsed_time(e) / reps
+
+
+def autotune(batch: RaggedBatch, F_candidates=(2, 3, 4, 5, 6, 8, 12), bps_candidates=(1, 2, 3, 4),
+             sample=256, seed=0, reps=1, verbose=False):
+    """Pick the BLS tile size F and the persistent block counts by timing each candidate on a
+    sample of the batch's curves (the per-curve results do not depend on the choice).
+    Results are cached per (bin grid, phase mode, device) and applied to ``batch``."""
+    if not batch.built:
+        batch.build()
+    dev = batch.device
+    key = (batch.bls_spec, batch.tls_spec, torch.cuda.get_device_name(dev))
+    if key in _TUNED:
+        F, bb, tb = _TUNED[key]
+        batch.set_config(F, bb, tb)
+        return _TUNED[key]
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    rng = np.random.default_rng(seed)
+    batch.launch_prep()
+    best_bls = (None, math.inf)
+    table = []
+    if batch.n_bls:
+        pick = rng.choice(batch.n_bls, size=min(sample, batch.n_bls), replace=False)
+        for F in F_candidates:
+            q = batch._upload_segments(*batch._bls_segments(F, pick))
+            for bps in bps_candidates:
+                try:
+                    ms = _time_ms(lambda: batch.launch_bls(queue=q, blocks=bps * sms, F=F), reps)
+                except N.GtrapError:
+                    continue  # F does not fit in shared memory
+                table.append(("bls", F, bps, ms))
+                if ms < best_bls[1]:
+                    best_bls = ((F, bps * sms), ms)
+    best_tls = (0, math.inf)
+    if batch.n_tls:
+        pick = rng.choice(batch.n_tls, size=min(sample, batch.n_tls), replace=False)
+        q = batch._upload_segments(*batch._tls_segments(pick))
+        for blocks in [0] + [b * sms for b in bps_candidates]:
+            ms = _time_ms(lambda: batch.launch_tls(queue=q, blocks=blocks), reps)
+            table.append(("tls", None, blocks, ms))
+            if ms < best_tls[1]:
+                best_tls = (blocks, ms)
+    F, bb = best_bls[0] if best_bls[0] is not None else (default_F(batch.bls_spec), 0)
+    res = (F, bb, best_tls[0])
+    _TUNED[key] = res
+    batch.set_config(*res)
+    if verbose:
+        for row in table:
+            print("autotune", *row)
+    return res
+
+
+# -- plain baseline ---------------------------------------------------------------------------
+def run_plain(batch: RaggedBatch, stream=None):
+    """The same requests through the plain per-curve entry points (one gfilter, offset and
+    geebls or gtls launch sequence per curve, as a caller of the reference does for curves
+    with different lengths or grids), writing into the batch's output arrays."""
+    if not batch.built:
+        batch.build()
+    dev = batch.device
+    offs = batch.offs_host
+    s = batch.bls_spec
+    ntrue = torch.from_numpy(batch.bls_table["ntrue"].astype(np.int32)).to(dev) if batch.n_bls else None
+    given = torch.from_numpy(batch.bls_table["offset"].astype(np.float32)).to(dev) if batch.n_bls else None
+    for k in range(batch.n_bls):
+        a, n = int(offs[k]), int(offs[k + 1] - offs[k])
+        x = batch.x[a:a + n].view(n, 1)
+        t = batch.t[a:a + n].view(n, 1)
+        r = api.gfilter(x, batch.detrend_r, stream=stream) if batch.detrend_r is not None else x
+        off = api.offset(r, t, stream=stream) if batch.auto_offset else given[k:k + 1]
+        row = batch.bls_table[k]
+        o, nf = int(row["out"]), int(row["nf"])
+        api.geebls(r, t, off, ntrue[k:k + 1], nf, s.nb, s.kma, s.kmi, int(row["kkmi"]),
+                   float(row["fmin"]), float(row["df"]), phase=s.phase,
+                   out=(batch.blsp[o:o + nf].view(1, nf), batch.ph1[o:o + nf].view(1, nf),
+                        batch.ph2[o:o + nf].view(1, nf)), stream=stream)
+    ts = batch.tls_spec
+    for k in range(batch.n_tls):
+        j = batch.n_bls + k
+        a, n = int(offs[j]), int(offs[j + 1] - offs[j])
+        x = batch.x[a:a + n].view(n, 1)
+        t = batch.t[a:a + n].view(n, 1)
+        r = api.gfilter(x, batch.detrend_r, stream=stream) if batch.detrend_r is not None else x
+        row = batch.tls_table[k]
+        o, nt = int(row["out"]), int(row["nt"])
+        api.gtls(r, t, nt, ts.nw, ts.nl, int(row["nsc"]), float(row["wmax"]), float(row["dw"]),
+                 float(row["deltat"]), mode=ts.mode, fix_a=ts.fix_a,
+                 out=tuple(v[o:o + nt].view(nt, 1) for v in batch.tls_outs), stream=stream)

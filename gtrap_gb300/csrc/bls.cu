@@ -189,8 +189,110 @@ __global__ void bls_common_phase_kernel(const float *__restrict__ tu, ulonglong2
 }
 
 // ---------------------------------------------------------------------------
+// prep of packed (ragged) batches: curve q owns samples [off, off + n) of the packed arrays
+
+// Per curve: count bits of the 64-bit fold format, power-of-two flux scale, valid samples.
+__global__ void __launch_bounds__(256) bls_ragged_scale_kernel(gtrap_bls_curve *curves,
+                                                               const float *__restrict__ t,
+                                                               const float *__restrict__ x) {
+  __shared__ double pm[8];
+  __shared__ uint32_t pc[8];
+  const gtrap_bls_curve c = curves[blockIdx.x];
+  const double off = (double)c.offset;
+  double amax = 0.0;
+  uint32_t cnt = 0;
+  for (uint32_t i = threadIdx.x; i < c.n; i += 256) {
+    const float tt = __ldg(t + c.off + i), xx = __ldg(x + c.off + i);
+    if (tt >= 0.0f && isfinite(tt) && isfinite(xx) && isfinite((double)xx - off)) {
+      amax = fmax(amax, fabs((double)xx - off));
+      ++cnt;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+    cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+  }
+  if ((threadIdx.x & 31) == 0) { pm[threadIdx.x >> 5] = amax; pc[threadIdx.x >> 5] = cnt; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < 8; ++w) { amax = fmax(amax, pm[w]); cnt += pc[w]; }
+    const int CB = c.n ? 32 - __clz((int)c.n) : 1;  // counts <= n < 2^CB
+    double xq_max = c.n ? ldexp(1.0, 62 - CB) / (double)c.n : 1.0;
+    if (xq_max > 1073741823.0) xq_max = 1073741823.0;
+    curves[blockIdx.x].sx = amax > 0.0 ? ilogb(xq_max) - ilogb(amax) - 1 : 0;
+    curves[blockIdx.x].nv = cnt;
+    curves[blockIdx.x].cb = CB;
+  }
+}
+
+// curves[q].offset = sum of resid over samples with t >= 0, divided by n (get_offset).  The
+// summation order is the one of gtrap_offset (lane k sums the samples i = k mod 32 in order
+// with Neumaier compensation; the 32 partials are added in lane order in double), so a packed
+// curve gets the same offset, to the bit, as the same curve in an [n, nq] image.
+__global__ void __launch_bounds__(32) bls_ragged_offset_kernel(gtrap_bls_curve *curves,
+                                                               const float *__restrict__ t,
+                                                               const float *__restrict__ resid) {
+  const gtrap_bls_curve c = curves[blockIdx.x];
+  float sum = 0.0f, comp = 0.0f;
+  for (uint32_t i = threadIdx.x; i < c.n; i += 32) {
+    if (!(__ldg(t + c.off + i) < 0.0f)) {
+      const float v = __ldg(resid + c.off + i);
+      const float s = sum + v;
+      comp += (fabsf(sum) >= fabsf(v)) ? ((sum - s) + v) : ((v - s) + sum);
+      sum = s;
+    }
+  }
+  const double part = (double)sum + (double)comp;
+  double acc = 0.0;
+  for (int k = 0; k < 32; ++k) acc += __shfl_sync(0xffffffffu, part, k);
+  if (threadIdx.x == 0) curves[blockIdx.x].offset = c.n ? (float)(acc / (double)c.n) : 0.0f;
+}
+
+__global__ void __launch_bounds__(256) bls_ragged_pack_kernel(const gtrap_bls_curve *curves,
+                                                              uint32_t ncurves,
+                                                              const float *__restrict__ t,
+                                                              const float *__restrict__ x,
+                                                              int32_t *X, ulonglong2 *AB) {
+  for (uint32_t q = blockIdx.y; q < ncurves; q += gridDim.y) {
+    const gtrap_bls_curve c = curves[q];
+    const double off = (double)c.offset, scale = ldexp(1.0, c.sx);
+    for (uint32_t i = blockIdx.x * 256 + threadIdx.x; i < c.n; i += gridDim.x * 256) {
+      const float tt = __ldg(t + c.off + i), xx = __ldg(x + c.off + i);
+      const bool ok = tt >= 0.0f && isfinite(tt) && isfinite(xx) && isfinite((double)xx - off);
+      X[c.off + i] = ok ? (int32_t)__double2ll_rn(((double)xx - off) * scale) : kMasked;
+      if (AB) AB[c.off + i] = make_ulonglong2(frac64(tt, c.fmin), frac64(tt, c.df));
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // fold + scan
 
+// Launch-wide shape of the fold + scan.
+struct BlsShape {
+  uint32_t nb, kma, kmi, kkmi;
+  uint32_t F, region, Tg, G, lp;  // frequencies per block, shared-memory layout, scan groups
+  int lognb;
+  uint32_t flags;
+};
+
+// One block's work: F consecutive trial frequencies of one curve.
+struct BlsTile {
+  const int32_t *X;        // quantised flux of the curve's samples (kMasked = not folded)
+  const ulonglong2 *AB;    // exact phase pairs (frac(t*fmin), frac(t*df)) as 64-bit fractions
+  const float *T;          // raw times (FP32-reference phase)
+  uint32_t n, nv;          // samples, valid samples (the fold's total count)
+  float N;                 // denominator count of the power
+  float kkmi;              // windows must hold more than kkmi samples
+  int sx, CB;              // flux scale exponent, count bits of the 64-bit format
+  uint32_t j0, nfrem;      // first frequency index, frequencies in this tile
+  float fmin, df;          // frequency grid (FP32-reference phase)
+  float *blsp;             // outputs of frequency j0 (nfrem consecutive elements)
+  uint32_t *ph1, *ph2;
+};
+
+// Curves in the reference's [n, nq] image layout, one launch per call.
 struct BlsArgs {
   float *blsp;
   uint32_t *ph1, *ph2;
@@ -198,14 +300,12 @@ struct BlsArgs {
   const ulonglong2 *AB;    // exact phase pairs
   const float *T;          // FP32-reference times
   const int32_t *sx;       // [nq]
-  const uint32_t *nv;      // [nq] valid samples (the fold's total count)
+  const uint32_t *nv;      // [nq] valid samples
   const uint32_t *ntrue;   // [nq] or null (use n_den)
-  uint32_t n, n_den, nq, nf, nb, kma, kmi, kkmi;
-  float fmin, df;
-  uint32_t F, tiles, region, Tg, G, lp;
-  int lognb, CB;
+  uint32_t n, n_den, nq, nf, tiles;
   uint32_t ab_stride, t_stride;  // elements per curve (0: shared by all curves)
-  uint32_t flags;
+  int CB;
+  float fmin, df;
 };
 
 // Start bins per scan task (one warp; its lanes take 32 end bins at a time).
@@ -226,9 +326,10 @@ __device__ __forceinline__ bool better(float p, int i, int e, float bp, int bi, 
   return p > bp || (p == bp && (i < bi || (i == bi && e < be)));
 }
 
+// Fold + scan of one tile by the whole block (blockDim.x == kThreads).
 // MODE 0: exact phase, nb power of two; 1: exact phase, any nb; 2: FP32 reference phase.
 template <int R, int MODE>
-__global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1) bls_fold_scan_kernel(const BlsArgs a) {
+__device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
   extern __shared__ __align__(16) unsigned long long sm[];
   __shared__ long long scan_x[kThreads / 32];
   __shared__ int scan_c[kThreads / 32];
@@ -237,12 +338,8 @@ __global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1) bls_fol
   __shared__ int scan_m[kThreads / 32];          // per-warp maximum bin count
   __shared__ unsigned drop_cnt[64];              // FP32-phase samples landing on bin nb
 
-  const uint32_t item = blockIdx.x;
-  const uint32_t q = item / a.tiles;
-  const uint32_t tile = item - q * a.tiles;
-  if (q >= a.nq) return;
-  const uint32_t j0 = tile * a.F;
-  const uint32_t nfrem = min(a.F, a.nf - j0);
+  const uint32_t j0 = tj.j0;
+  const uint32_t nfrem = tj.nfrem;
   const int tid = threadIdx.x;
   const int nb = (int)a.nb;
 
@@ -259,12 +356,12 @@ __global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1) bls_fol
   // C += ((xq & 1023) << 12) | 1, exact while every bin holds at most kFastMaxCount
   // samples (|xq| < 2^30).  The scan verifies that and re-folds a frequency in the 64-bit
   // format ((xq << CB) | 1, one 64-bit atomic) when it does not hold.
-  const int32_t *Xq = a.X + (size_t)q * a.n;
-  const int CB = a.CB;
+  const int32_t *Xq = tj.X;
+  const int CB = tj.CB;
   unsigned *h32 = reinterpret_cast<unsigned *>(sm);
   const int shift = 64 - a.lognb;
-  const ulonglong2 *ABq = a.AB + (size_t)q * a.ab_stride;
-  const float *Tq = a.T + (size_t)q * a.t_stride;
+  const ulonglong2 *ABq = tj.AB;
+  const float *Tq = tj.T;
   const float nbf = (float)nb;
   const bool f0_nofma = a.flags & GTRAP_BLS_REF_F0_NOFMA;
   const bool ph_fma = a.flags & GTRAP_BLS_REF_PH_FMA;
@@ -272,7 +369,7 @@ __global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1) bls_fol
   // dropped (the reference's wrap overwrites that slot)
   auto ref_bin = [&](float t, uint32_t f) -> uint32_t {
     const float jf = (float)(j0 + f);
-    const float f0 = f0_nofma ? __fadd_rn(a.fmin, __fmul_rn(a.df, jf)) : __fmaf_rn(a.df, jf, a.fmin);
+    const float f0 = f0_nofma ? __fadd_rn(tj.fmin, __fmul_rn(tj.df, jf)) : __fmaf_rn(tj.df, jf, tj.fmin);
     const float p = __fmul_rn(t, f0);
     const float ip = __int2float_rn(__float2int_rz(p));
     const float ph = ph_fma ? __fmaf_rn(t, f0, -ip) : __fsub_rn(p, ip);
@@ -281,14 +378,14 @@ __global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1) bls_fol
   if (MODE != 2) {
     // kU samples per thread per step, all loads issued before any is used
     constexpr int kU = 4;
-    for (uint32_t k0 = tid; k0 < a.n; k0 += kU * kThreads) {
+    for (uint32_t k0 = tid; k0 < tj.n; k0 += kU * kThreads) {
       int32_t xq[kU];
       ulonglong2 ab[kU];
 #pragma unroll
       for (int u = 0; u < kU; ++u) {
         const uint32_t k = k0 + u * kThreads;
-        xq[u] = k < a.n ? __ldg(Xq + k) : kMasked;
-        ab[u] = k < a.n ? __ldg(ABq + k) : make_ulonglong2(0ull, 0ull);
+        xq[u] = k < tj.n ? __ldg(Xq + k) : kMasked;
+        ab[u] = k < tj.n ? __ldg(ABq + k) : make_ulonglong2(0ull, 0ull);
       }
 #pragma unroll
       for (int u = 0; u < kU; ++u) {
@@ -307,7 +404,7 @@ __global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1) bls_fol
       }
     }
   } else {
-    for (uint32_t k = tid; k < a.n; k += kThreads) {
+    for (uint32_t k = tid; k < tj.n; k += kThreads) {
       const int32_t xq = __ldg(Xq + k);
       if (xq == kMasked) continue;
       const float t = __ldg(Tq + k);
@@ -329,7 +426,7 @@ __global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1) bls_fol
   // 64-bit re-fold of frequency j0 + f by the Tg_ threads of one group
   auto refold64 = [&](uint32_t f, int gtid_, int Tg_) {
     unsigned long long *Hf = sm + (size_t)f * a.region;
-    for (uint32_t k = gtid_; k < a.n; k += Tg_) {
+    for (uint32_t k = gtid_; k < tj.n; k += Tg_) {
       const int32_t xq = __ldg(Xq + k);
       if (xq == kMasked) continue;
       const unsigned long long inc = ((unsigned long long)(long long)xq << CB) | 1ull;
@@ -355,8 +452,8 @@ __global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1) bls_fol
   const int gw0 = (g * Tg) >> 5;           // first warp of this group
   const int nwg = Tg >> 5;                 // warps in the group
   const int kma = (int)a.kma, kmi = (int)a.kmi;
-  const float kkmi_f = (float)a.kkmi;
-  const float Nf = a.ntrue ? (float)a.ntrue[q] : (float)a.n_den;
+  const float kkmi_f = tj.kkmi;
+  const float Nf = tj.N;
   const unsigned long long cmask = (1ull << CB) - 1ull;
   const int i0 = gtid * R;
   const int rounds = (int)((nfrem + a.G - 1) / a.G);
@@ -425,7 +522,7 @@ __global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1) bls_fol
         gmax = max(gmax, scan_m[gw0 + w]);
       }
       if (!fast) break;
-      const int expect = (int)a.nv[q] - (MODE == 2 ? (int)drop_cnt[f] : 0);
+      const int expect = (int)tj.nv - (MODE == 2 ? (int)drop_cnt[f] : 0);
       if (tc == expect && gmax <= kFastMaxCount) break;
       // some bin may have overflowed the 32-bit format: fold this frequency again in 64 bits
       group_bar(1 + g, Tg);  // every thread has read scan_* and H before they are rewritten
@@ -653,13 +750,102 @@ __global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1) bls_fol
   // ---- outputs
   if (tid < (int)nfrem) {
     const unsigned long long key = best_key[tid];
-    const size_t o = (size_t)q * a.nf + j0 + tid;
     const bool found = key != 0ull;
     const float pw = __uint_as_float((unsigned)(key >> 32));
     const unsigned ie = 0xffffffffu - (unsigned)(key & 0xffffffffull);
-    a.blsp[o] = found ? ldexpf(sqrtf(pw), -a.sx[q]) : 0.0f;
-    if (a.ph1) a.ph1[o] = found ? (ie >> 15) : 0u;
-    if (a.ph2) a.ph2[o] = found ? (ie & 0x7fffu) - 1u : 0u;
+    tj.blsp[tid] = found ? ldexpf(sqrtf(pw), -tj.sx) : 0.0f;
+    if (tj.ph1) tj.ph1[tid] = found ? (ie >> 15) : 0u;
+    if (tj.ph2) tj.ph2[tid] = found ? (ie & 0x7fffu) - 1u : 0u;
+  }
+}
+
+// Plain launch: one block per (curve, tile) of an [n, nq] image batch.
+template <int R, int MODE>
+__global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1)
+bls_fold_scan_kernel(const BlsShape sh, const BlsArgs a) {
+  // the tile descriptor lives in shared memory: read where used, not held in registers
+  __shared__ BlsTile t;
+  const uint32_t q = blockIdx.x / a.tiles;
+  const uint32_t tile = blockIdx.x - q * a.tiles;
+  if (q >= a.nq) return;
+  if (threadIdx.x == 0) {
+  t.X = a.X + (size_t)q * a.n;
+  t.AB = a.AB + (size_t)q * a.ab_stride;
+  t.T = a.T + (size_t)q * a.t_stride;
+  t.n = a.n;
+  t.nv = a.nv[q];
+  t.N = a.ntrue ? (float)a.ntrue[q] : (float)a.n_den;
+  t.kkmi = (float)sh.kkmi;
+  t.sx = a.sx[q];
+  t.CB = a.CB;
+  t.j0 = tile * sh.F;
+  t.nfrem = min(sh.F, a.nf - t.j0);
+  t.fmin = a.fmin;
+  t.df = a.df;
+  const size_t o = (size_t)q * a.nf + t.j0;
+  t.blsp = a.blsp + o;
+  t.ph1 = a.ph1 ? a.ph1 + o : nullptr;
+  t.ph2 = a.ph2 ? a.ph2 + o : nullptr;
+  }
+  __syncthreads();
+  bls_tile<R, MODE>(sh, t);
+}
+
+// Persistent launch over a device work queue of (curve, tile) items of a packed batch.
+struct BlsQueue {
+  const gtrap_bls_curve *curves;
+  const gtrap_bls_segment *segs;
+  const uint32_t *cum;     // [nseg + 1] tile prefix over the segments
+  uint32_t nseg;
+  const int32_t *X;        // packed quantised flux
+  const ulonglong2 *AB;    // packed phase pairs
+  const float *T;          // packed times
+  float *blsp;
+  uint32_t *ph1, *ph2;
+  uint32_t *counter;       // next item (zeroed before the launch)
+};
+
+template <int R, int MODE>
+__global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1)
+bls_queue_kernel(const BlsShape sh, const BlsQueue qa) {
+  __shared__ uint32_t item_s;
+  __shared__ BlsTile t;  // descriptor of the current tile (see bls_fold_scan_kernel)
+  const uint32_t total = qa.cum[qa.nseg];
+  for (;;) {
+    if (threadIdx.x == 0) item_s = atomicAdd(qa.counter, 1u);
+    __syncthreads();
+    const uint32_t it = item_s;
+    __syncthreads();
+    if (it >= total) break;
+    uint32_t lo = 0, hi = qa.nseg;  // segment k with cum[k] <= it < cum[k + 1]
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (qa.cum[mid] <= it) lo = mid; else hi = mid;
+    }
+    const gtrap_bls_segment sg = qa.segs[lo];
+    const gtrap_bls_curve c = qa.curves[sg.curve];
+    const uint32_t j0 = (sg.tile0 + (it - qa.cum[lo])) * sh.F;
+    if (j0 >= c.nf) continue;  // uniform across the block
+    if (threadIdx.x == 0) {
+    t.X = qa.X + c.off;
+    t.AB = qa.AB ? qa.AB + c.off : nullptr;
+    t.T = qa.T + c.off;
+    t.n = c.n;
+    t.nv = c.nv;
+    t.N = (float)c.ntrue;
+    t.kkmi = (float)(c.kkmi < 5u ? 5u : c.kkmi);  // MINBIN, include/geebls.h:31-33
+    t.sx = c.sx;
+    t.CB = c.cb;
+    t.j0 = j0;
+    t.nfrem = min(sh.F, c.nf - j0);
+    t.fmin = c.fmin;
+    t.df = c.df;
+    t.blsp = qa.blsp + c.out + j0;
+    t.ph1 = qa.ph1 ? qa.ph1 + c.out + j0 : nullptr;
+    t.ph2 = qa.ph2 ? qa.ph2 + c.out + j0 : nullptr;
+    }
+    __syncthreads();
+    bls_tile<R, MODE>(sh, t);
   }
 }
 
@@ -672,7 +858,8 @@ struct Plan {
   size_t smem;
 };
 
-int make_plan(uint32_t nb, uint32_t kma, uint32_t nf, Plan *p) {
+// F_req > 0 forces the number of frequencies per block (batched runs fix it per batch).
+int make_plan(uint32_t nb, uint32_t kma, uint32_t nf, uint32_t F_req, Plan *p) {
   const int R = nb <= 4096 ? 8 : 16;
   uint32_t Tg = (nb + R - 1) / R;
   Tg = (Tg + 31) / 32 * 32;
@@ -696,7 +883,9 @@ int make_plan(uint32_t nb, uint32_t kma, uint32_t nf, Plan *p) {
   if (F == 0) F = G;
   const char *env = getenv("GTRAP_BLS_F");
   if (env && atoi(env) > 0) F = (uint32_t)atoi(env);
-  if (F > nf) F = nf;
+  if (F_req) F = F_req;
+  if (F > 64) return fail(GTRAP_ERR_INVALID_ARG, "geebls: at most 64 frequencies per block (F=%u)", F);
+  if (nf && F > nf) F = nf;
   if ((size_t)F * per_f > (size_t)gtrap::max_smem_optin()) {
     F = (uint32_t)((size_t)gtrap::max_smem_optin() / per_f);
     if (F == 0) return fail(GTRAP_ERR_INVALID_ARG, "geebls: nb=%u, kma=%u do not fit in shared memory", nb, kma);
@@ -707,9 +896,19 @@ int make_plan(uint32_t nb, uint32_t kma, uint32_t nf, Plan *p) {
   p->Tg = Tg;
   p->G = G;
   p->R = R;
-  p->tiles = (nf + F - 1) / F;
+  p->tiles = nf ? (nf + F - 1) / F : 0;
   p->smem = (size_t)F * per_f;
   return GTRAP_OK;
+}
+
+BlsShape shape_of(const Plan &p, uint32_t nb, uint32_t kma, uint32_t kmi_eff, uint32_t kkmi_eff,
+                  uint32_t flags) {
+  BlsShape sh;
+  sh.nb = nb; sh.kma = kma; sh.kmi = kmi_eff; sh.kkmi = kkmi_eff;
+  sh.F = p.F; sh.region = p.region; sh.Tg = p.Tg; sh.G = p.G; sh.lp = p.lp;
+  sh.lognb = gtrap::is_pow2(nb) ? gtrap::ilog2u(nb) : 0;
+  sh.flags = flags;
+  return sh;
 }
 
 size_t ws_size(uint32_t n, uint32_t nq, uint32_t flags, bool full) {
@@ -783,21 +982,16 @@ int run_bls(bool full, float *blsp, uint32_t *phase1, uint32_t *phase2, const fl
   }
 
   Plan p;
-  GTRAP_TRY(make_plan(nb, kma, nf, &p));
+  GTRAP_TRY(make_plan(nb, kma, nf, 0, &p));
+  const BlsShape sh = shape_of(p, nb, kma, kmi_eff, kkmi_eff, flags);
   BlsArgs ba;
   ba.blsp = blsp; ba.ph1 = phase1; ba.ph2 = phase2;
   ba.X = X; ba.AB = AB; ba.T = full ? T : tu; ba.sx = sx; ba.nv = nv; ba.ntrue = full ? ntrue : nullptr;
-  ba.n = n; ba.n_den = n; ba.nq = nq; ba.nf = nf; ba.nb = nb; ba.kma = kma;
-  ba.kmi = kmi_eff; ba.kkmi = kkmi_eff; ba.fmin = fmin; ba.df = df;
-  ba.F = p.F; ba.tiles = p.tiles; ba.region = p.region; ba.Tg = p.Tg; ba.G = p.G; ba.lp = p.lp;
-  ba.lognb = gtrap::is_pow2(nb) ? gtrap::ilog2u(nb) : 0;
+  ba.n = n; ba.n_den = n; ba.nq = nq; ba.nf = nf; ba.tiles = p.tiles;
+  ba.fmin = fmin; ba.df = df;
   ba.CB = CB;
   ba.ab_stride = full ? n : 0;
   ba.t_stride = full ? n : 0;
-  ba.flags = flags;
-  if (kmi_eff >= kma) {
-    // no admissible width: every SR is zero (reference: power stays 0)
-  }
   const uint64_t blocks = (uint64_t)p.tiles * nq;
   if (blocks >= (1ull << 31)) return fail(GTRAP_ERR_INVALID_ARG, "%s: grid too large", name);
   const void *fn;
@@ -805,7 +999,7 @@ int run_bls(bool full, float *blsp, uint32_t *phase1, uint32_t *phase2, const fl
 #define GTRAP_BLS_LAUNCH(RR, MM)                                                          \
   fn = (const void *)bls_fold_scan_kernel<RR, MM>;                                         \
   GTRAP_TRY(gtrap::ensure_smem(fn, p.smem, name));                                         \
-  bls_fold_scan_kernel<RR, MM><<<(unsigned)blocks, kThreads, p.smem, stream>>>(ba);
+  bls_fold_scan_kernel<RR, MM><<<(unsigned)blocks, kThreads, p.smem, stream>>>(sh, ba);
   if (p.R == 8) {
     if (mode == 0) { GTRAP_BLS_LAUNCH(8, 0) } else if (mode == 1) { GTRAP_BLS_LAUNCH(8, 1) } else { GTRAP_BLS_LAUNCH(8, 2) }
   } else {
@@ -838,9 +1032,101 @@ int noalloc_scratch(void **out) {
   return GTRAP_OK;
 }
 
+int pool_carve(void *pool, size_t pool_bytes, uint64_t total, uint32_t flags, int32_t **X,
+               ulonglong2 **AB) {
+  const bool exact = !(flags & GTRAP_BLS_PHASE_FP32_REF);
+  if (!pool || ((uintptr_t)pool & 255)) return fail(GTRAP_ERR_WORKSPACE, "bls batch: pool must be 256-byte aligned");
+  gtrap::Carver cv{(char *)pool, pool_bytes, 0};
+  *X = cv.take<int32_t>(total);
+  *AB = exact ? cv.take<ulonglong2>(total) : nullptr;
+  if (!*X || (exact && !*AB)) return fail(GTRAP_ERR_WORKSPACE, "bls batch: pool of %zu bytes is too small", pool_bytes);
+  return GTRAP_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+uint32_t gtrap_bls_tile_frequencies(uint32_t nb, uint32_t kma) {
+  if (nb == 0 || nb > (uint32_t)kMaxNb || kma == 0 || kma > nb) return 0;
+  Plan p;
+  if (make_plan(nb, kma, 0, 0, &p) != GTRAP_OK) return 0;
+  return p.F;
+}
+
+size_t gtrap_bls_pool_bytes(uint64_t total_samples, uint32_t flags) {
+  const bool exact = !(flags & GTRAP_BLS_PHASE_FP32_REF);
+  return gtrap::align256(total_samples * 4) + (exact ? gtrap::align256(total_samples * 16) : 0) + 256;
+}
+
+int gtrap_bls_prepare(gtrap_bls_curve *curves, uint32_t ncurves, uint32_t max_n, const float *t,
+                      const float *x, uint64_t total_samples, void *pool, size_t pool_bytes,
+                      uint32_t flags, gtrap_stream_t stream) {
+  if (ncurves == 0) return GTRAP_OK;
+  if (!curves || !t || !x) return fail(GTRAP_ERR_INVALID_ARG, "bls_prepare: null pointer");
+  if (max_n >= (1u << 23)) return fail(GTRAP_ERR_INVALID_ARG, "bls_prepare: max_n=%u must be below 2^23", max_n);
+  int32_t *X;
+  ulonglong2 *AB;
+  GTRAP_TRY(pool_carve(pool, pool_bytes, total_samples, flags, &X, &AB));
+  bls_ragged_scale_kernel<<<ncurves, 256, 0, stream>>>(curves, t, x);
+  GTRAP_TRY(gtrap::check_launch("bls_ragged_scale_kernel"));
+  const unsigned gx = (unsigned)((max_n + 1023) / 1024 > 0 ? (max_n + 1023) / 1024 : 1);
+  const unsigned gy = ncurves < 65535 ? ncurves : 65535;
+  bls_ragged_pack_kernel<<<dim3(gx, gy), 256, 0, stream>>>(curves, ncurves, t, x, X, AB);
+  return gtrap::check_launch("bls_ragged_pack_kernel");
+}
+
+int gtrap_bls_offsets(gtrap_bls_curve *curves, uint32_t ncurves, const float *t, const float *resid,
+                      gtrap_stream_t stream) {
+  if (ncurves == 0) return GTRAP_OK;
+  if (!curves || !t || !resid) return fail(GTRAP_ERR_INVALID_ARG, "bls_offsets: null pointer");
+  bls_ragged_offset_kernel<<<ncurves, 32, 0, stream>>>(curves, t, resid);
+  return gtrap::check_launch("bls_ragged_offset_kernel");
+}
+
+int gtrap_bls_run(const gtrap_bls_curve *curves, const gtrap_bls_segment *segs, const uint32_t *cum,
+                  uint32_t nseg, const float *t, const void *pool, size_t pool_bytes,
+                  uint64_t total_samples, uint32_t nb, uint32_t kma, uint32_t kmi, uint32_t F,
+                  uint32_t flags, uint32_t blocks, uint32_t *counter, float *blsp,
+                  uint32_t *phase1, uint32_t *phase2, gtrap_stream_t stream) {
+  if (nseg == 0) return GTRAP_OK;
+  if (!curves || !segs || !cum || !counter || !blsp) return fail(GTRAP_ERR_INVALID_ARG, "bls_run: null pointer");
+  if (nb == 0 || nb > (uint32_t)kMaxNb) return fail(GTRAP_ERR_INVALID_ARG, "bls_run: nb=%u must be in [1, %d]", nb, kMaxNb);
+  if (kma == 0 || kma > nb) return fail(GTRAP_ERR_INVALID_ARG, "bls_run: kma=%u must be in [1, nb]", kma);
+  if (F == 0) return fail(GTRAP_ERR_INVALID_ARG, "bls_run: F (frequencies per tile) must be positive");
+  const bool exact = !(flags & GTRAP_BLS_PHASE_FP32_REF);
+  if (!exact && !t) return fail(GTRAP_ERR_INVALID_ARG, "bls_run: the FP32-reference phase needs the times");
+  int32_t *X;
+  ulonglong2 *AB;
+  GTRAP_TRY(pool_carve(const_cast<void *>(pool), pool_bytes, total_samples, flags, &X, &AB));
+  Plan p;
+  GTRAP_TRY(make_plan(nb, kma, 0, F, &p));
+  const uint32_t kmi_eff = kmi < 1 ? 1 : kmi;
+  const BlsShape sh = shape_of(p, nb, kma, kmi_eff, 5, flags);
+  BlsQueue qa;
+  qa.curves = curves; qa.segs = segs; qa.cum = cum; qa.nseg = nseg;
+  qa.X = X; qa.AB = AB; qa.T = t; qa.blsp = blsp; qa.ph1 = phase1; qa.ph2 = phase2;
+  qa.counter = counter;
+  cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), stream);
+  if (e != cudaSuccess) return fail(GTRAP_ERR_CUDA, "bls_run: cudaMemsetAsync: %s", cudaGetErrorString(e));
+  if (blocks == 0) {
+    const int per_sm = (size_t)gtrap::smem_per_sm() >= 2 * (p.smem + 4096) ? 2 : 1;
+    blocks = (uint32_t)(gtrap::sm_count() * per_sm);
+  }
+  const int mode = !exact ? 2 : (gtrap::is_pow2(nb) ? 0 : 1);
+  const void *fn;
+#define GTRAP_BLS_QLAUNCH(RR, MM)                                                          \
+  fn = (const void *)bls_queue_kernel<RR, MM>;                                              \
+  GTRAP_TRY(gtrap::ensure_smem(fn, p.smem, "bls_run"));                                     \
+  bls_queue_kernel<RR, MM><<<blocks, kThreads, p.smem, stream>>>(sh, qa);
+  if (p.R == 8) {
+    if (mode == 0) { GTRAP_BLS_QLAUNCH(8, 0) } else if (mode == 1) { GTRAP_BLS_QLAUNCH(8, 1) } else { GTRAP_BLS_QLAUNCH(8, 2) }
+  } else {
+    if (mode == 0) { GTRAP_BLS_QLAUNCH(16, 0) } else if (mode == 1) { GTRAP_BLS_QLAUNCH(16, 1) } else { GTRAP_BLS_QLAUNCH(16, 2) }
+  }
+#undef GTRAP_BLS_QLAUNCH
+  return gtrap::check_launch("bls_queue_kernel");
+}
 
 size_t gtrap_geebls_noalloc_max_scratch(void) { return kNoallocScratchBytes; }
 

@@ -81,6 +81,68 @@ __global__ void __launch_bounds__(256) gfilter_kernel(const float *__restrict__ 
   }
 }
 
+// Packed curves (curve q = samples [offs[q], offs[q+1]) of a flat array): each lane filters
+// a run of `run` consecutive rows of one curve with its own sorted window, as above.
+__global__ void __launch_bounds__(256) gfilter_packed_kernel(const float *__restrict__ in,
+                                                             float *__restrict__ out,
+                                                             const unsigned long long *__restrict__ offs,
+                                                             unsigned ncurves, int r, int run) {
+  extern __shared__ float sorted_windows[];
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int w = 2 * r + 1;
+  float *S = sorted_windows + (size_t)warp * w * 32 + lane;
+  for (unsigned q = blockIdx.y; q < ncurves; q += gridDim.y) {
+    const unsigned long long off = offs[q];
+    const long long n = (long long)(offs[q + 1] - off);
+    const float *x = in + off;
+    float *y = out + off;
+    const long long row0 = ((long long)(blockIdx.x * (blockDim.x >> 5) + warp) * 32 + lane) * run;
+    if (row0 >= n) continue;
+    const long long row1 = min(n, row0 + run);
+    auto ld = [&](long long i) -> float { return (i >= 0 && i < n) ? __ldg(x + i) : 0.0f; };
+    for (int k = 0; k < w; ++k) {
+      const float v = ld(row0 - r + k);
+      int j = k;
+      while (j > 0) {
+        const float u = S[32 * (j - 1)];
+        if (u <= v) break;
+        S[32 * j] = u;
+        --j;
+      }
+      S[32 * j] = v;
+    }
+    for (long long i = row0; i < row1; ++i) {
+      y[i] = __fsub_rn(__ldg(x + i), S[32 * r]);
+      if (i + 1 >= row1) break;
+      const float vold = ld(i - r), vnew = ld(i + r + 1);
+      if (vnew == vold) continue;
+      int lo = 0, hi = w - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (S[32 * mid] < vold) lo = mid + 1; else hi = mid;
+      }
+      int j = lo;
+      if (vnew > vold) {
+        while (j + 1 < w) {
+          const float u = S[32 * (j + 1)];
+          if (!(u < vnew)) break;
+          S[32 * j] = u;
+          ++j;
+        }
+      } else {
+        while (j > 0) {
+          const float u = S[32 * (j - 1)];
+          if (!(u > vnew)) break;
+          S[32 * j] = u;
+          --j;
+        }
+      }
+      S[32 * j] = vnew;
+    }
+  }
+}
+
 // offset[q] = sum of resid over samples whose time is not negative, divided by n.
 // One block per 32 curves; each of the 32 warps sums every 32nd row with Neumaier
 // compensation; the 32 partials are combined in a fixed order (deterministic).
@@ -152,6 +214,33 @@ int gtrap_gfilter(const float *in, float *out, uint32_t n, uint32_t nq, uint32_t
   gfilter_kernel<<<grid, 32 * warps, smem, stream>>>(in, out, (int)n, (int)nq, (int)r,
                                                      (int)rows_per_warp);
   return check_launch("gfilter_kernel");
+}
+
+int gtrap_gfilter_packed(const float *in, float *out, const uint64_t *offs, uint32_t ncurves,
+                         uint32_t max_n, uint32_t r, gtrap_stream_t stream) {
+  using namespace gtrap;
+  if (ncurves == 0 || max_n == 0) return GTRAP_OK;
+  if (!in || !out || !offs) return fail(GTRAP_ERR_INVALID_ARG, "gfilter_packed: null pointer");
+  if (in == out) return fail(GTRAP_ERR_INVALID_ARG, "gfilter_packed: in and out must not alias");
+  const size_t w = 2 * (size_t)r + 1;
+  const size_t per_warp = w * 32 * sizeof(float);
+  const size_t budget = (size_t)max_smem_optin();
+  if (per_warp > budget)
+    return fail(GTRAP_ERR_INVALID_ARG, "gfilter_packed: r=%u needs %zu bytes of shared memory per warp", r, per_warp);
+  int warps = (int)(budget / per_warp);
+  if (warps > 8) warps = 8;
+  while (warps > 1 && per_warp * warps > 56 * 1024) --warps;
+  int run = (int)(8 * w);
+  if (run < 64) run = 64;
+  if (run > 1024) run = 1024;
+  const size_t rows_per_block = (size_t)run * 32 * warps;
+  const unsigned gx = (unsigned)((max_n + rows_per_block - 1) / rows_per_block);
+  const unsigned gy = ncurves < 65535 ? ncurves : 65535;
+  const size_t smem = per_warp * warps;
+  GTRAP_TRY(ensure_smem((const void *)gfilter_packed_kernel, smem, "gfilter_packed"));
+  gfilter_packed_kernel<<<dim3(gx, gy), 32 * warps, smem, stream>>>(
+      in, out, (const unsigned long long *)offs, ncurves, (int)r, run);
+  return check_launch("gfilter_packed_kernel");
 }
 
 int gtrap_offset(const float *resid, const float *tu, float *offset, uint32_t n, uint32_t nq,

@@ -40,15 +40,16 @@ constexpr int kWarps = 8;
 constexpr int kTlsThreads = kWarps * 32;
 constexpr int kMaxStage = 7000;  // staged samples: nsc + 31
 
+// One curve as a tile sees it: sample s at lc[s*stride], epoch e's outputs at [e*ostride].
 struct TlsArgs {
   float *sn, *w, *t0, *l, *h;
   const float *lc, *tu;
-  int nt, nq, nw, nl, nsc;
+  int stride, ostride;
+  int nt, nw, nl, nsc;
   float wmax, dw, deltat;
   int mode;          // 0: simple, 1: absolute
   int w_fma, t_fma;  // float32 contraction choices (see GTRAP_TLS_*_NOFMA)
   int fix_a;         // 1: region A's own flux in H (GTRAP_TLS_FIX_A)
-  int tiles;         // epoch tiles per curve
 };
 
 struct DF {  // double-float value hi + lo
@@ -78,16 +79,13 @@ __device__ __forceinline__ double df_diff_d(float bh, float bl, float ah, float 
   return ((double)bh - (double)ah) + ((double)bl - (double)al);
 }
 
-__global__ void __launch_bounds__(kTlsThreads) gtls_kernel(const TlsArgs a) {
+// 32 consecutive epochs [e0, e0 + 32) of one curve, by the whole block.
+__device__ __forceinline__ void gtls_tile(const TlsArgs &a, const int e0) {
   extern __shared__ __align__(16) float st[];
   __shared__ float red_sn[kWarps][32], red_l[kWarps][32], red_h[kWarps][32];
   __shared__ int red_w[kWarps][32];
   __shared__ float xref;
 
-  const int item = blockIdx.x;
-  const int tile = item / a.nq;
-  const int q = item - tile * a.nq;
-  const int e0 = tile * 32;
   const int nsch = a.nsc / 2;
   // staged sample range [base, base + S) in sample indices, clipped to [0, nt)
   const int first = e0 - nsch;
@@ -107,7 +105,7 @@ __global__ void __launch_bounds__(kTlsThreads) gtls_kernel(const TlsArgs a) {
 
   // ---- stage the scoop union: (t + 1000) - 1000 rounding (include/gtls_simple.h:54-65)
   for (int s = tid; s < S; s += kTlsThreads) {
-    const size_t idx = (size_t)(base + s) * a.nq + q;
+    const size_t idx = (size_t)(base + s) * a.stride;
     const float tr = __ldg(a.tu + idx);
     const float tqv = __fadd_rn(-1000.0f, __double2float_rn((double)tr + 1000.0));
     const float x = __ldg(a.lc + idx);
@@ -353,13 +351,76 @@ __global__ void __launch_bounds__(kTlsThreads) gtls_kernel(const TlsArgs a) {
     if (best_w == INT_MAX || !(best_sn > 0.0f)) { best_sn = 0.0f; best_w = 0; best_l = 0.0f; best_h = 0.0f; }
     const float wf = (float)best_w;
     const float W = a.w_fma ? __fmaf_rn(-a.dw, wf, a.wmax) : __fsub_rn(a.wmax, __fmul_rn(a.dw, wf));
-    const size_t k = (size_t)e * a.nq + q;
+    const size_t k = (size_t)e * a.ostride;
     a.sn[k] = best_sn;
     a.t0[k] = dte;
     a.w[k] = W;
     a.l[k] = best_l;
     a.h[k] = best_h;
   }
+}
+
+// Plain launch over an [n, nq] image: block = (epoch tile, curve), curves fastest.
+__global__ void __launch_bounds__(kTlsThreads) gtls_kernel(const TlsArgs img, const int nq) {
+  __shared__ TlsArgs v;
+  const int tile = blockIdx.x / nq;
+  const int q = blockIdx.x - tile * nq;
+  if (threadIdx.x == 0) {
+    v = img;
+    v.lc += q; v.tu += q;
+    v.sn += q; v.w += q; v.t0 += q; v.l += q; v.h += q;
+  }
+  __syncthreads();
+  gtls_tile(v, tile * 32);
+}
+
+// Persistent launch over a device work queue of (curve, epoch tile) items of a packed batch.
+struct TlsQueue {
+  const gtrap_tls_curve *curves;
+  const gtrap_tls_segment *segs;
+  const uint32_t *cum;
+  uint32_t nseg;
+  const float *t, *x;
+  float *sn, *w, *t0, *l, *h;
+  int nw, nl, mode, w_fma, t_fma, fix_a;
+  uint32_t *counter;
+};
+
+__global__ void __launch_bounds__(kTlsThreads) gtls_queue_kernel(const TlsQueue qa) {
+  __shared__ uint32_t item_s;
+  __shared__ TlsArgs v;
+  const uint32_t total = qa.cum[qa.nseg];
+  for (;;) {
+    if (threadIdx.x == 0) item_s = atomicAdd(qa.counter, 1u);
+    __syncthreads();
+    const uint32_t it = item_s;
+    __syncthreads();
+    if (it >= total) break;
+    uint32_t lo = 0, hi = qa.nseg;  // segment k with cum[k] <= it < cum[k + 1]
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (qa.cum[mid] <= it) lo = mid; else hi = mid;
+    }
+    const gtrap_tls_segment sg = qa.segs[lo];
+    const gtrap_tls_curve c = qa.curves[sg.curve];
+    const int e0 = (int)(sg.tile0 + (it - qa.cum[lo])) * 32;
+    if (e0 >= c.nt) continue;  // uniform across the block
+    if (threadIdx.x == 0) {
+      v.lc = qa.x + c.off; v.tu = qa.t + c.off;
+      v.sn = qa.sn + c.out; v.w = qa.w + c.out; v.t0 = qa.t0 + c.out; v.l = qa.l + c.out; v.h = qa.h + c.out;
+      v.stride = 1; v.ostride = 1;
+      v.nt = c.nt; v.nw = qa.nw; v.nl = qa.nl; v.nsc = c.nsc;
+      v.wmax = c.wmax; v.dw = c.dw; v.deltat = c.deltat;
+      v.mode = qa.mode; v.w_fma = qa.w_fma; v.t_fma = qa.t_fma; v.fix_a = qa.fix_a;
+    }
+    __syncthreads();
+    gtls_tile(v, e0);
+  }
+}
+
+size_t tls_smem(int nsc) {
+  const int S = nsc + 31;
+  return (size_t)S * 8 + (size_t)(S + 1) * 20 + 64;
 }
 
 }  // namespace
@@ -383,20 +444,53 @@ int gtrap_gtls(float *tlssn, float *tlsw, float *tlst0, float *tlsl, float *tlsh
   if (!(deltat > 0.0f)) return fail(GTRAP_ERR_INVALID_ARG, "gtls: deltat must be positive");
   const long long tiles = ((long long)nt + 31) / 32;
   if (tiles * nq >= (1LL << 31)) return fail(GTRAP_ERR_INVALID_ARG, "gtls: grid too large");
-  const int S = nsc + 31;
-  const size_t smem = (size_t)S * 8 + (size_t)(S + 1) * 20 + 64;
+  const size_t smem = tls_smem(nsc);
   GTRAP_TRY(gtrap::ensure_smem((const void *)gtls_kernel, smem, "gtls"));
   TlsArgs ta;
   ta.sn = tlssn; ta.w = tlsw; ta.t0 = tlst0; ta.l = tlsl; ta.h = tlshmax;
   ta.lc = lc; ta.tu = tu;
-  ta.nt = nt; ta.nq = nq; ta.nw = nw; ta.nl = nl; ta.nsc = nsc;
+  ta.stride = nq; ta.ostride = nq;
+  ta.nt = nt; ta.nw = nw; ta.nl = nl; ta.nsc = nsc;
   ta.wmax = wmax; ta.dw = dw; ta.deltat = deltat; ta.mode = mode;
   ta.w_fma = (flags & GTRAP_TLS_W_NOFMA) ? 0 : 1;
   ta.t_fma = (flags & GTRAP_TLS_T_NOFMA) ? 0 : 1;
   ta.fix_a = (flags & GTRAP_TLS_FIX_A) ? 1 : 0;
-  ta.tiles = (int)tiles;
-  gtls_kernel<<<(unsigned)(tiles * nq), kTlsThreads, smem, stream>>>(ta);
+  gtls_kernel<<<(unsigned)(tiles * nq), kTlsThreads, smem, stream>>>(ta, nq);
   return gtrap::check_launch("gtls_kernel");
+}
+
+int gtrap_gtls_run(const gtrap_tls_curve *curves, const gtrap_tls_segment *segs,
+                   const uint32_t *cum, uint32_t nseg, const float *t, const float *x, int32_t nw,
+                   int32_t nl, int32_t max_nsc, int32_t mode, uint32_t flags, uint32_t blocks,
+                   uint32_t *counter, float *tlssn, float *tlsw, float *tlst0, float *tlsl,
+                   float *tlshmax, gtrap_stream_t stream) {
+  if (nseg == 0) return GTRAP_OK;
+  if (!curves || !segs || !cum || !t || !x || !counter || !tlssn || !tlsw || !tlst0 || !tlsl || !tlshmax)
+    return fail(GTRAP_ERR_INVALID_ARG, "gtls_run: null pointer");
+  if (nw < 1 || nw > 1024) return fail(GTRAP_ERR_INVALID_ARG, "gtls_run: nw=%d must be in [1, 1024]", nw);
+  if (nl < 1 || nl > 4096) return fail(GTRAP_ERR_INVALID_ARG, "gtls_run: nl=%d must be in [1, 4096]", nl);
+  if (max_nsc < 1 || max_nsc + 31 > kMaxStage)
+    return fail(GTRAP_ERR_INVALID_ARG, "gtls_run: max_nsc=%d must be in [1, %d]", max_nsc, kMaxStage - 31);
+  if (mode != 0 && mode != 1) return fail(GTRAP_ERR_INVALID_ARG, "gtls_run: mode must be 0 or 1");
+  const size_t smem = tls_smem(max_nsc);
+  GTRAP_TRY(gtrap::ensure_smem((const void *)gtls_queue_kernel, smem, "gtls_run"));
+  TlsQueue qa;
+  qa.curves = curves; qa.segs = segs; qa.cum = cum; qa.nseg = nseg; qa.t = t; qa.x = x;
+  qa.sn = tlssn; qa.w = tlsw; qa.t0 = tlst0; qa.l = tlsl; qa.h = tlshmax;
+  qa.nw = nw; qa.nl = nl; qa.mode = mode;
+  qa.w_fma = (flags & GTRAP_TLS_W_NOFMA) ? 0 : 1;
+  qa.t_fma = (flags & GTRAP_TLS_T_NOFMA) ? 0 : 1;
+  qa.fix_a = (flags & GTRAP_TLS_FIX_A) ? 1 : 0;
+  qa.counter = counter;
+  cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), stream);
+  if (e != cudaSuccess) return fail(GTRAP_ERR_CUDA, "gtls_run: cudaMemsetAsync: %s", cudaGetErrorString(e));
+  if (blocks == 0) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gtls_queue_kernel, kTlsThreads, smem);
+    blocks = (uint32_t)(gtrap::sm_count() * (per_sm > 0 ? per_sm : 1));
+  }
+  gtls_queue_kernel<<<blocks, kTlsThreads, smem, stream>>>(qa);
+  return gtrap::check_launch("gtls_queue_kernel");
 }
 
 }  // extern "C"

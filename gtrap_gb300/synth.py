@@ -8,6 +8,7 @@ running median ignores them (``gtrap/read_keplerlc.py:41-46``).
 """
 from __future__ import annotations
 
+import math
 from dataclasses import dataclass
 
 import numpy as np
@@ -173,3 +174,66 @@ def tls_grid(wmin_h=0.5, wmax_h=8.0, nw=8, nl=16, deltat=TESS_CADENCE):
     nsc = int(wmax / deltat + 3.0)   # kepler/gtls_mockkepler.py:256
     return dict(nw=nw, nl=nl, wmax=float(np.float32(wmax)), dw=float(np.float32(dw)),
                 deltat=float(np.float32(deltat)), nsc=nsc)
+
+
+def next_pow2(v: float) -> int:
+    return 1 << max(0, int(math.ceil(math.log2(max(v, 1.0)))))
+
+
+def ragged_curve(k, seed=4000, n_range=(2000, 70000), mask_frac=0.10, tls_frac=0.5,
+                 signal_frac=0.25, qmi=0.005):
+    """Curve k of the uneven mixed batch: n log-uniform on ``n_range``, cadence 2 min or
+    29.4 min (coin), contiguous gaps (t = -1000, zig-zag filled flux) covering
+    ``mask_frac``, three sinusoids plus a quadratic trend, and a box (BLS requests) or
+    flipped trapezoid (GTLS requests) in ``signal_frac`` of the curves.  BLS grids:
+    nf = clip(next_pow2(8 * baseline_days), 2048, 32768), fmin = 2/baseline, fmax = 2 per day.
+    Returns a dict with kind ("bls" or "tls"), t, x and the request's grid."""
+    rng = np.random.default_rng(seed + k)
+    lo, hi = n_range
+    n = int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
+    cad = TESS_CADENCE if rng.uniform() < 0.5 else KEPLER_CADENCE
+    kind = "tls" if rng.uniform() < tls_frac else "bls"
+    t = (np.arange(n) + 0.5) * cad + rng.uniform(-1.0, 1.0, n) / 86400.0
+    T = t[-1]
+    mask = np.zeros(n, bool)
+    target = int(mask_frac * n)
+    cap = max(1, n // 10)
+    while mask.sum() < target:
+        glen = min(cap, max(1, int(rng.uniform(0.5, 3.0) / cad)))
+        g0 = int(rng.integers(0, n))
+        mask[g0:g0 + glen] = True
+    f = np.ones(n)
+    for _ in range(3):
+        f += rng.uniform(2e-4, 2e-3) * np.sin(2 * np.pi * t / rng.uniform(5.0, 50.0) +
+                                            rng.uniform(0, 2 * np.pi))
+    xx = t / T
+    f += rng.uniform(-1e-3, 1e-3) * xx * xx + rng.uniform(-1e-3, 1e-3) * xx
+    out = dict(kind=kind, n=n, cadence=cad)
+    if kind == "bls":
+        if rng.uniform() < signal_frac:
+            per = rng.uniform(1.0, max(1.5, min(200.0, T / 2)))
+            f -= rng.uniform(3e-4, 3e-3) * box_profile(t, per, rng.uniform(0.0, per),
+                                                       rng.uniform(1.0, 6.0) / 24.0)
+        f += rng.normal(0.0, 5e-4, n)
+        nf = int(min(32768, max(2048, next_pow2(8.0 * T))))
+        fmin = 2.0 / T
+        out.update(nf=nf, fmin=float(np.float32(fmin)),
+                   df=float(np.float32((2.0 - fmin) / (nf - 1))), kkmi=int(n * qmi))
+    else:
+        if rng.uniform() < signal_frac:
+            width = rng.uniform(0.5, 8.0) / 24.0
+            per = rng.uniform(0.5, 12.0)
+            f -= rng.uniform(2e-4, 5e-3) * trapezoid_profile(t, per, rng.uniform(0.0, per), width,
+                                                             rng.uniform(0.05, 0.5) * width)
+        f += rng.normal(0.0, 1e-3, n)
+        f = 2.0 - f
+        out.update(tls_grid(deltat=cad))
+    f = zigzag_fill(f, mask)
+    out["t"] = np.where(mask, INVALID_T, t).astype(np.float32)
+    out["x"] = f.astype(np.float32)
+    return out
+
+
+def ragged_mix(ncurves, seed=4000, **kw):
+    """Curves 0 .. ncurves-1 of :func:`ragged_curve`."""
+    return [ragged_curve(k, seed=seed, **kw) for k in range(ncurves)]

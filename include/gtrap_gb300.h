@@ -121,6 +121,65 @@ int gtrap_geebls_simple(float *blsp, uint32_t *phase1, uint32_t *phase2, const f
                         size_t workspace_bytes, gtrap_stream_t stream);
 
 /* ---------------------------------------------------------------------------
+ * Packed (ragged) BLS batches: curves of different lengths and frequency grids, kept
+ * device-resident and processed by one persistent launch over a device work queue.  No
+ * counterpart in the reference (which takes one [n, nq] image per call); the statistic is
+ * the one of gtrap_geebls (mask t < 0, flux - offset, N = ntrue).
+ *
+ * Curve q owns samples [off, off + n) of the packed time/flux arrays and output elements
+ * [out, out + nf) of the packed spectra.  A segment asks for tiles [tile0, tile0 + count) of
+ * one curve, tile t covering frequencies [t*F, min((t+1)*F, nf)); cum[k] is the number of
+ * tiles of segments 0..k-1 (cum[nseg] = total).  All arrays are device memory, so a batch
+ * can be captured in a CUDA graph and replayed.
+ * ------------------------------------------------------------------------- */
+typedef struct {
+  uint64_t off;     /* first sample in the packed time and flux arrays */
+  uint64_t out;     /* first element of this curve's spectrum in the packed outputs */
+  uint32_t n;       /* samples */
+  uint32_t nf;      /* trial frequencies f_j = fmin + j*df, j < nf */
+  float fmin, df;
+  float offset;     /* subtracted from the flux before folding */
+  uint32_t ntrue;   /* denominator count N of the power */
+  int32_t sx;       /* set by gtrap_bls_prepare: flux scale exponent */
+  uint32_t nv;      /* set by gtrap_bls_prepare: valid samples */
+  int32_t cb;       /* set by gtrap_bls_prepare: count bits of the 64-bit fold format */
+  uint32_t kkmi;    /* windows must hold more than max(kkmi, 5) samples */
+} gtrap_bls_curve; /* 56 bytes */
+
+typedef struct {
+  uint32_t curve;   /* index into the curve array */
+  uint32_t tile0;   /* first tile of this segment */
+} gtrap_bls_segment;
+
+/* Detrend of packed curves: curve q is in[offs[q] .. offs[q+1]) (offs on the device, ncurves+1
+ * entries); out = in - zero-padded running median of window 2r+1 within each curve
+ * (gtrap_gfilter per curve).  max_n: longest curve. */
+int gtrap_gfilter_packed(const float *in, float *out, const uint64_t *offs, uint32_t ncurves,
+                         uint32_t max_n, uint32_t r, gtrap_stream_t stream);
+/* curves[q].offset = sum of resid over samples with t >= 0, divided by n (get_offset,
+ * gtrap/gfilter.py:94-101), for packed curves. */
+int gtrap_bls_offsets(gtrap_bls_curve *curves, uint32_t ncurves, const float *t, const float *resid,
+                      gtrap_stream_t stream);
+/* Frequencies per tile that gtrap_geebls picks for this bin grid on the current device
+ * (0 when nb or kma is out of range). */
+uint32_t gtrap_bls_tile_frequencies(uint32_t nb, uint32_t kma);
+/* Bytes of the per-sample pool (quantised flux and exact phase pairs). */
+size_t gtrap_bls_pool_bytes(uint64_t total_samples, uint32_t flags);
+/* Quantise and phase-encode every curve's samples into the pool; fills sx, nv and cb of the
+ * (device) curve array.  max_n: largest n of the batch (< 2^23). */
+int gtrap_bls_prepare(gtrap_bls_curve *curves, uint32_t ncurves, uint32_t max_n, const float *t,
+                      const float *x, uint64_t total_samples, void *pool, size_t pool_bytes,
+                      uint32_t flags, gtrap_stream_t stream);
+/* Run the listed tiles: persistent blocks pop items from a device counter (zeroed by the
+ * call).  blocks = 0 picks one or two blocks per SM.  t is needed only with
+ * GTRAP_BLS_PHASE_FP32_REF.  phase pointers may be NULL. */
+int gtrap_bls_run(const gtrap_bls_curve *curves, const gtrap_bls_segment *segs, const uint32_t *cum,
+                  uint32_t nseg, const float *t, const void *pool, size_t pool_bytes,
+                  uint64_t total_samples, uint32_t nb, uint32_t kma, uint32_t kmi, uint32_t F,
+                  uint32_t flags, uint32_t blocks, uint32_t *counter, float *blsp,
+                  uint32_t *phase1, uint32_t *phase2, gtrap_stream_t stream);
+
+/* ---------------------------------------------------------------------------
  * BLS peak statistics.  Replaces getmax + combine_stat (gtrap/getstat.py:14-57,
  * 100-123) as called by get_blsstat (gtrap/getstat.py:64-67).  Over the first
  * floor(nf/patch)*patch frequencies of each curve (all nf when patch == 0):
@@ -157,6 +216,31 @@ int gtrap_gtls(float *tlssn, float *tlsw, float *tlst0, float *tlsl, float *tlsh
                const float *lc, const float *tu, int32_t nt, int32_t nq, int32_t nw,
                int32_t nl, int32_t nsc, float t0min, float dt, float wmax, float dw,
                float deltat, int32_t mode, uint32_t flags, gtrap_stream_t stream);
+
+/* Packed (ragged) GTLS batches, persistent launch over a device work queue of (curve,
+ * 32-epoch tile) items.  No counterpart in the reference; the statistic is the one of
+ * gtrap_gtls.  Curve q's sample s is t[off + s], x[off + s]; epoch e's outputs are at
+ * [out + e].  Segments and cum as for the BLS batches (tile t = epochs [32t, 32t + 32)).
+ * max_nsc: largest nsc of the batch (sizes the shared memory). */
+typedef struct {
+  uint64_t off;     /* first sample in the packed time and flux arrays */
+  uint64_t out;     /* first element of this curve's outputs */
+  int32_t nt;       /* epochs (the first nt samples are used) */
+  int32_t nsc;      /* scoop length */
+  float wmax, dw, deltat;
+  uint32_t reserved;
+} gtrap_tls_curve; /* 40 bytes */
+
+typedef struct {
+  uint32_t curve;
+  uint32_t tile0;
+} gtrap_tls_segment;
+
+int gtrap_gtls_run(const gtrap_tls_curve *curves, const gtrap_tls_segment *segs,
+                   const uint32_t *cum, uint32_t nseg, const float *t, const float *x, int32_t nw,
+                   int32_t nl, int32_t max_nsc, int32_t mode, uint32_t flags, uint32_t blocks,
+                   uint32_t *counter, float *tlssn, float *tlsw, float *tlst0, float *tlsl,
+                   float *tlshmax, gtrap_stream_t stream);
 
 /* ---------------------------------------------------------------------------
  * Measurement helpers (used by the benchmark to report roofline fractions).

@@ -1,0 +1,167 @@
+"""Packed (ragged) batches: one persistent BLS launch and one GTLS launch over device work
+queues, against the plain per-curve entry points (bit-identical) and the FP64 oracle.
+
+Tolerances as for the plain kernels: SR relative error <= 1e-4 and best bins identical up to
+FP64 near-ties (1e-5 of the maximum power); GTLS S/N within 1e-4 (relative, absolute below 1).
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from gtrap_gb300 import batch as B, synth
+
+pytestmark = pytest.mark.gpu
+
+R = 8  # detrend window 17
+BLS = B.BlsSpec(nb=256, kma=27, kmi=1)
+TLS = B.TlsSpec(nw=4, nl=8)
+
+
+def _mix(count=10, seed=4100):
+    mix = synth.ragged_mix(count, seed=seed, n_range=(400, 4000))
+    bat = B.RaggedBatch(BLS, TLS, detrend_r=R)
+    for k, c in enumerate(mix):
+        if c["kind"] == "bls":
+            nf = min(c["nf"], 120 + 37 * k)  # uneven grids, small enough for the oracle
+            bat.add_bls(c["t"], c["x"], nf, c["fmin"], c["df"], kkmi=c["kkmi"])
+        else:
+            bat.add_tls(c["t"], c["x"], c["nsc"], c["wmax"], c["dw"], c["deltat"])
+    return mix, bat
+
+
+def _results(bat):
+    bls = [bat.bls_result(k) for k in range(bat.n_bls)]
+    tls = [bat.tls_result(k) for k in range(bat.n_tls)]
+    return bls, tls
+
+
+def _same(a, b):
+    for x, y in zip(a[0], b[0]):
+        for u, v in zip(x, y):
+            np.testing.assert_array_equal(u, v)
+    for x, y in zip(a[1], b[1]):
+        for u, v in zip(x, y):
+            np.testing.assert_array_equal(u, v)
+
+
+@pytest.fixture(scope="module")
+def ragged(cuda):
+    mix, bat = _mix()
+    assert bat.n_bls >= 2 and bat.n_tls >= 2
+    bat.build()
+    bat.launch()
+    torch.cuda.synchronize()
+    return mix, bat, _results(bat)
+
+
+def test_ragged_equals_plain_per_curve(ragged):
+    mix, bat, got = ragged
+    B.run_plain(bat)
+    torch.cuda.synchronize()
+    _same(got, _results(bat))
+
+
+def test_ragged_bls_against_oracle(ragged):
+    mix, bat, got = ragged
+    dev_table = np.frombuffer(bat.bls_curves.cpu().numpy().tobytes(), B.BLS_CURVE)
+    k = 0
+    for c in mix:
+        if c["kind"] != "bls":
+            continue
+        row = bat.bls_table[k]
+        x, t = c["x"].astype(np.float32), c["t"].astype(np.float32)
+        resid = oracle.medfilt_residual(x[:, None], R)
+        np.testing.assert_array_equal(bat.resid[int(row["off"]):int(row["off"]) + x.size].cpu().numpy(),
+                                      resid[:, 0])
+        off64 = oracle.offset(resid, t[:, None])
+        off = np.array([dev_table[k]["offset"]], np.float32)  # get_offset on the device
+        assert abs(off[0] - off64[0]) <= 1e-6 * max(1e-3, abs(off64[0])), (off[0], off64[0])
+        assert dev_table[k]["nv"] == row["ntrue"]
+        nf = int(row["nf"])
+        osr, op1, op2, opmax = oracle.bls(resid, t[:, None], nf, BLS.nb, BLS.kma, BLS.kmi,
+                                          int(row["kkmi"]), float(row["fmin"]), float(row["df"]),
+                                          offset=off, ntrue=np.array([row["ntrue"]], np.uint32))
+        sr, p1, p2 = got[0][k]
+        fin = np.isfinite(osr[0])
+        rel = np.abs(sr[fin] - osr[0][fin]) / np.maximum(osr[0][fin], 1e-30)
+        assert rel.max() <= 1e-4, (k, rel.max())
+        for j in np.flatnonzero(((p1 != op1[0]) | (p2 != op2[0])) & fin):
+            pw = oracle.bls_window_power(resid, t[:, None], 0, j, int(p1[j]), int(p2[j]), BLS.nb,
+                                         float(row["fmin"]), float(row["df"]), offset=off,
+                                         ntrue=np.array([row["ntrue"]], np.uint32))
+            assert abs(pw - opmax[0, j]) <= 1e-5 * opmax[0, j], (k, j)
+        k += 1
+
+
+def test_ragged_tls_against_oracle(ragged):
+    mix, bat, got = ragged
+    k = 0
+    for c in mix:
+        if c["kind"] != "tls":
+            continue
+        x, t = c["x"].astype(np.float32), c["t"].astype(np.float32)
+        resid = oracle.medfilt_residual(x[:, None], R)
+        n = x.size
+        ref = oracle.gtls(resid, t[:, None], n, TLS.nw, TLS.nl, c["nsc"], c["wmax"], c["dw"], c["deltat"])
+        sn = got[1][k][0]
+        osn = ref[0][:, 0]
+        err = np.abs(sn - osn) / np.maximum(np.abs(osn), 1.0)
+        assert err.max() <= 1e-4, (k, err.max())
+        np.testing.assert_array_equal(got[1][k][2], ref[2][:, 0])
+        k += 1
+
+
+def test_graph_replay_and_in_place_update(ragged, cuda):
+    mix, bat, got = ragged
+    g = bat.capture()
+    g.replay()
+    torch.cuda.synchronize()
+    _same(got, _results(bat))
+    # new flux of the same layout: the replay must follow the arrays' contents
+    x0 = bat.x.clone()
+    bat.x.mul_(1.25).add_(0.001)
+    g.replay()
+    torch.cuda.synchronize()
+    replayed = _results(bat)
+    bat.launch()
+    torch.cuda.synchronize()
+    _same(replayed, _results(bat))
+    assert not np.array_equal(replayed[0][0][0], got[0][0][0])
+    bat.x.copy_(x0)
+    g.replay()
+    torch.cuda.synchronize()
+    _same(got, _results(bat))
+
+
+def test_autotune_and_partial_segments_keep_results(ragged):
+    mix, bat, got = ragged
+    F, bb, tb = B.autotune(bat, F_candidates=(2, 5), bps_candidates=(1, 2), sample=3)
+    assert F in (2, 5)
+    bat.launch()
+    torch.cuda.synchronize()
+    _same(got, _results(bat))
+    # a segment may start at any tile: only frequencies [F*tile0, F*(tile0+count)) are written
+    bat.blsp.fill_(-1.0)
+    segs = np.zeros(1, B.SEGMENT)
+    segs["curve"], segs["tile0"] = 1, 1
+    cum = np.array([0, 2], np.uint32)
+    bat.launch_bls(queue=bat._upload_segments(segs, cum))
+    sr = bat.bls_result(1)[0]
+    nf = sr.size
+    lo, hi = min(F, nf), min(3 * F, nf)
+    np.testing.assert_array_equal(sr[lo:hi], got[0][1][0][lo:hi])
+    assert (sr[:lo] == -1.0).all() and (sr[hi:] == -1.0).all()
+    bat.launch()
+
+
+def test_fp32_reference_phase_batch(cuda):
+    mix, bat = _mix(count=6, seed=4200)
+    bat.bls_spec = B.BlsSpec(nb=256, kma=27, kmi=1, phase="fp32")
+    bat.build()
+    bat.launch()
+    torch.cuda.synchronize()
+    got = _results(bat)
+    B.run_plain(bat)
+    torch.cuda.synchronize()
+    _same(got, _results(bat))

@@ -63,3 +63,33 @@ def test_missing_workspace_is_an_error(lib):
     st = lib.gtrap_geebls_simple(C.c_void_p(256), None, None, C.c_void_p(256), C.c_void_p(256), 100, 2,
                                  10, 64, 10, 1, 5, 0.1, 0.01, 0, 0, None, 0, None)
     assert st == _native.ERR_WORKSPACE
+
+
+def test_packed_struct_layouts_match_the_header(tmp_path):
+    """The numpy record layouts used by gtrap_gb300.batch equal the C structs' offsets."""
+    import shutil
+    import subprocess
+    from gtrap_gb300 import batch
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    fields = {"gtrap_bls_curve": batch.BLS_CURVE, "gtrap_tls_curve": batch.TLS_CURVE,
+              "gtrap_bls_segment": batch.SEGMENT}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "gtrap_gb300.h"', "int main(void) {"]
+    for st, dt in fields.items():
+        lines.append('printf("%s size %%zu\\n", sizeof(%s));' % (st, st))
+        for f in dt.names:
+            lines.append('printf("%s %s %%zu\\n", offsetof(%s, %s));' % (st, f, st, f))
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines():
+        st, f, v = line.split()
+        got[(st, f)] = int(v)
+    for st, dt in fields.items():
+        assert got[(st, "size")] == dt.itemsize, st
+        for f in dt.names:
+            assert got[(st, f)] == dt.fields[f][1], (st, f)
