@@ -45,7 +45,7 @@ _SIGNATURES = {
     "gtrap_geebls_simple_workspace_size": (sz, [u32, u32, u32]),
     "gtrap_geebls_simple": (C.c_int, [vp, vp, vp, vp, vp, u32, u32, u32, u32, u32, u32, u32,
                                       f32, f32, u32, u32, vp, sz, vp]),
-    "gtrap_gfilter_packed": (C.c_int, [vp, vp, vp, u32, u32, u32, vp]),
+    "gtrap_gfilter_packed": (C.c_int, [vp, vp, vp, vp, u32, u32, u32, vp]),
     "gtrap_bls_offsets": (C.c_int, [vp, u32, vp, vp, vp]),
     "gtrap_bls_tile_frequencies": (u32, [u32, u32]),
     "gtrap_bls_pool_bytes": (sz, [u64, u32]),

@@ -199,7 +199,8 @@ class RaggedBatch:
         self.offs_host = offs
         self.t = t_h.to(dev, non_blocking=True)
         self.x = x_h.to(dev, non_blocking=True)
-        self.offs = torch.from_numpy(offs.view(np.int64)).to(dev)
+        self.offs = torch.from_numpy(offs[:-1].view(np.int64).copy()).to(dev)
+        self.lens = torch.from_numpy(lens.astype(np.int32)).to(dev)
         self.resid = torch.empty_like(self.x) if self.detrend_r is not None else self.x
 
         nbls = len(self._bls)
@@ -297,7 +298,7 @@ class RaggedBatch:
         st = stream_handle(stream)
         if self.detrend_r is not None:
             N.call("gtrap_gfilter_packed", as_ptr(self.x), as_ptr(self.resid), as_ptr(self.offs),
-                   self.n_bls + self.n_tls, self.max_n, self.detrend_r, st)
+                   as_ptr(self.lens), self.n_bls + self.n_tls, self.max_n, self.detrend_r, st)
         if self.n_bls:
             if self.auto_offset:
                 N.call("gtrap_bls_offsets", as_ptr(self.bls_curves), self.n_bls, as_ptr(self.t),

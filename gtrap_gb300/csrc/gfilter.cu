@@ -81,11 +81,12 @@ __global__ void __launch_bounds__(256) gfilter_kernel(const float *__restrict__ 
   }
 }
 
-// Packed curves (curve q = samples [offs[q], offs[q+1]) of a flat array): each lane filters
-// a run of `run` consecutive rows of one curve with its own sorted window, as above.
+// Packed curves (curve q = samples [off[q], off[q] + len[q]) of a flat array): each lane
+// filters a run of `run` consecutive rows of one curve with its own sorted window, as above.
 __global__ void __launch_bounds__(256) gfilter_packed_kernel(const float *__restrict__ in,
                                                              float *__restrict__ out,
                                                              const unsigned long long *__restrict__ offs,
+                                                             const uint32_t *__restrict__ lens,
                                                              unsigned ncurves, int r, int run) {
   extern __shared__ float sorted_windows[];
   const int lane = threadIdx.x & 31;
@@ -94,7 +95,7 @@ __global__ void __launch_bounds__(256) gfilter_packed_kernel(const float *__rest
   float *S = sorted_windows + (size_t)warp * w * 32 + lane;
   for (unsigned q = blockIdx.y; q < ncurves; q += gridDim.y) {
     const unsigned long long off = offs[q];
-    const long long n = (long long)(offs[q + 1] - off);
+    const long long n = (long long)lens[q];
     const float *x = in + off;
     float *y = out + off;
     const long long row0 = ((long long)(blockIdx.x * (blockDim.x >> 5) + warp) * 32 + lane) * run;
@@ -216,11 +217,11 @@ int gtrap_gfilter(const float *in, float *out, uint32_t n, uint32_t nq, uint32_t
   return check_launch("gfilter_kernel");
 }
 
-int gtrap_gfilter_packed(const float *in, float *out, const uint64_t *offs, uint32_t ncurves,
-                         uint32_t max_n, uint32_t r, gtrap_stream_t stream) {
+int gtrap_gfilter_packed(const float *in, float *out, const uint64_t *off, const uint32_t *n,
+                         uint32_t ncurves, uint32_t max_n, uint32_t r, gtrap_stream_t stream) {
   using namespace gtrap;
   if (ncurves == 0 || max_n == 0) return GTRAP_OK;
-  if (!in || !out || !offs) return fail(GTRAP_ERR_INVALID_ARG, "gfilter_packed: null pointer");
+  if (!in || !out || !off || !n) return fail(GTRAP_ERR_INVALID_ARG, "gfilter_packed: null pointer");
   if (in == out) return fail(GTRAP_ERR_INVALID_ARG, "gfilter_packed: in and out must not alias");
   const size_t w = 2 * (size_t)r + 1;
   const size_t per_warp = w * 32 * sizeof(float);
@@ -239,7 +240,7 @@ int gtrap_gfilter_packed(const float *in, float *out, const uint64_t *offs, uint
   const size_t smem = per_warp * warps;
   GTRAP_TRY(ensure_smem((const void *)gfilter_packed_kernel, smem, "gfilter_packed"));
   gfilter_packed_kernel<<<dim3(gx, gy), 32 * warps, smem, stream>>>(
-      in, out, (const unsigned long long *)offs, ncurves, (int)r, run);
+      in, out, (const unsigned long long *)off, n, ncurves, (int)r, run);
   return check_launch("gfilter_packed_kernel");
 }
 

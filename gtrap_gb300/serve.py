@@ -1,0 +1,590 @@
+"""Continuous-batching transit search on one GPU.
+
+Requests (one light curve each, with a BLS frequency grid or a GTLS template grid) arrive at
+any time.  The server keeps every admitted request's samples, encoded BLS samples and outputs
+in device-resident arenas sized by an HBM budget, and runs in steps.  A step
+
+1. admits waiting requests in arrival order while their samples and outputs fit in the free
+   space of the arenas (admission by HBM budget; a request waits until earlier ones free
+   memory) and copies their samples to the device on a copy stream,
+2. detrends the newly admitted curves (``gtrap_gfilter_packed``), computes their BLS offsets
+   and encodes their BLS samples (``gtrap_bls_offsets``, ``gtrap_bls_prepare``),
+3. runs a bounded slice of work: up to ``bls_tiles`` (curve, frequency tile) items and
+   ``tls_tiles`` (curve, 32-epoch tile) items taken from the oldest in-flight requests, in one
+   persistent BLS launch and one persistent GTLS launch (``gtrap_bls_run``,
+   ``gtrap_gtls_run``), so tiles of many requests run side by side and a long request spans
+   several steps while newer requests join, and
+4. when a request's last tile has run, copies its outputs to the host on a second copy stream
+   and frees its memory.
+
+The host prepares step k+1 while step k runs (at most ``depth`` steps in flight).  Each
+request's result is bit-identical to a solo run: the kernels treat every curve and tile
+independently and every sum has a fixed order.  The reference has no serving loop; its
+drivers launch one kernel per image (gtrap/geebls.py:10-22, gtrap/gtls.py:11-27), which
+:class:`PlainServer` reproduces per request as the baseline.
+"""
+from __future__ import annotations
+
+import collections
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _native as N
+from . import api
+from .batch import BLS_CURVE, SEGMENT, TLS_CURVE, TLS_TILE, BlsSpec, TlsSpec, default_F
+from ._dev import as_ptr, require_cuda
+
+SAMPLE_BYTES = 32   # t, x, detrended x (4 B each) + quantised flux (4 B) + phase pair (16 B)
+OUTPUT_BYTES = 20   # five float32/int32 output arrays per output element
+ALIGN = 32          # arena granularity (elements)
+
+
+@dataclass
+class Request:
+    """One light curve and its search grid.  ``kind`` is "bls" (nf, fmin, df, kkmi, ntrue)
+    or "tls" (nsc, wmax, dw, deltat; epochs = samples)."""
+    kind: str
+    t: np.ndarray
+    x: np.ndarray
+    nf: int = 0
+    fmin: float = 0.0
+    df: float = 0.0
+    kkmi: int | None = None
+    ntrue: int | None = None
+    nsc: int = 0
+    wmax: float = 0.0
+    dw: float = 0.0
+    deltat: float = 0.0
+
+    @property
+    def n(self) -> int:
+        return int(np.asarray(self.t).size)
+
+    @property
+    def outputs(self) -> int:
+        return int(self.nf) if self.kind == "bls" else self.n
+
+    @staticmethod
+    def from_curve(c: dict) -> "Request":
+        """From a :func:`gtrap_gb300.synth.ragged_curve` dict."""
+        if c["kind"] == "bls":
+            return Request("bls", c["t"], c["x"], nf=c["nf"], fmin=c["fmin"], df=c["df"], kkmi=c["kkmi"])
+        return Request("tls", c["t"], c["x"], nsc=c["nsc"], wmax=c["wmax"], dw=c["dw"], deltat=c["deltat"])
+
+
+@dataclass
+class Result:
+    rid: int
+    kind: str
+    arrival: float
+    admitted: float
+    done: float
+    outputs: tuple   # bls: (blsp, phase1, phase2); tls: (sn, w, t0, l, hmax)
+    evals: int
+
+    @property
+    def latency(self) -> float:
+        return self.done - self.arrival
+
+
+class Arena:
+    """First-fit allocator of contiguous ranges of [0, cap) in units of ``align`` elements."""
+
+    def __init__(self, cap: int, align: int = ALIGN):
+        self.align = align
+        self.cap = cap // align * align
+        self.free_list = [(0, self.cap)] if self.cap else []   # sorted, coalesced (start, end)
+        self.used = 0
+        self.high_water = 0
+
+    def _round(self, size):
+        return max(self.align, (size + self.align - 1) // self.align * self.align)
+
+    def alloc(self, size: int):
+        need = self._round(size)
+        for k, (a, b) in enumerate(self.free_list):
+            if b - a >= need:
+                if b - a == need:
+                    del self.free_list[k]
+                else:
+                    self.free_list[k] = (a + need, b)
+                self.used += need
+                self.high_water = max(self.high_water, self.used)
+                return a
+        return None
+
+    def free(self, start: int, size: int):
+        need = self._round(size)
+        a, b = start, start + need
+        fl = self.free_list
+        lo, hi = 0, len(fl)
+        while lo < hi:
+            mid = (lo + hi) // 2
+            if fl[mid][0] < a:
+                lo = mid + 1
+            else:
+                hi = mid
+        if lo > 0 and fl[lo - 1][1] > a or lo < len(fl) and fl[lo][0] < b:
+            raise ValueError("double free of [%d, %d)" % (a, b))
+        if lo > 0 and fl[lo - 1][1] == a:
+            a = fl[lo - 1][0]
+            lo -= 1
+            del fl[lo]
+        if lo < len(fl) and fl[lo][0] == b:
+            b = fl[lo][1]
+            del fl[lo]
+        fl.insert(lo, (a, b))
+        self.used -= need
+
+
+@dataclass
+class _Live:
+    rid: int
+    req: Request
+    arrival: float
+    admitted: float = 0.0
+    soff: int = 0          # sample slot
+    ooff: int = 0          # output slot
+    desc: int = 0          # descriptor slot
+    tiles: int = 0
+    next_tile: int = 0
+    last_step: int = -1
+    result: tuple = ()
+    d2h_event: object = None
+
+
+@dataclass
+class _Step:
+    index: int
+    event: object
+    finishing: list = field(default_factory=list)
+
+
+class TransitServer:
+    """Continuous-batching BLS/GTLS server (see the module docstring).
+
+    ``hbm_budget`` bytes are split between the sample arena (``SAMPLE_BYTES`` per sample)
+    and the output arena (``OUTPUT_BYTES`` per output element) in the ratio
+    ``sample_share``; a request whose samples or outputs alone exceed an arena is rejected
+    by :meth:`submit`."""
+
+    def __init__(self, bls: BlsSpec = BlsSpec(), tls: TlsSpec = TlsSpec(), detrend_r: int = 24,
+                 hbm_budget: float = 100e9, sample_share: float = 0.8, bls_tiles: int | None = None,
+                 tls_tiles: int | None = None, F: int | None = None, max_requests: int = 1 << 16,
+                 depth: int = 2, device=None):
+        require_cuda()
+        self.dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
+        self.bls_spec, self.tls_spec = bls, tls
+        self.r = int(detrend_r)
+        self.F = int(F) if F else default_F(bls)
+        sms = torch.cuda.get_device_properties(self.dev).multi_processor_count
+        self.bls_tiles = int(bls_tiles) if bls_tiles else sms * 2 * 8
+        self.tls_tiles = int(tls_tiles) if tls_tiles else sms * 64
+        self.depth = max(1, int(depth))
+        budget = int(hbm_budget)
+        self.sample_cap = int(budget * sample_share) // SAMPLE_BYTES // ALIGN * ALIGN
+        self.out_cap = int(budget * (1.0 - sample_share)) // OUTPUT_BYTES // ALIGN * ALIGN
+        if self.sample_cap < ALIGN or self.out_cap < ALIGN:
+            raise ValueError("hbm_budget too small")
+        self.samples = Arena(self.sample_cap)
+        self.outs = Arena(self.out_cap)
+        self.bls_desc = Arena(max_requests, align=1)
+        self.tls_desc = Arena(max_requests, align=1)
+        d = self.dev
+        self.t = torch.zeros(self.sample_cap, dtype=torch.float32, device=d)
+        self.x = torch.zeros(self.sample_cap, dtype=torch.float32, device=d)
+        self.resid = torch.zeros(self.sample_cap, dtype=torch.float32, device=d)
+        self.pool_bytes = int(N.fn("gtrap_bls_pool_bytes")(self.sample_cap, bls.flags))
+        self.pool = torch.empty(self.pool_bytes, dtype=torch.uint8, device=d)
+        self.o = [torch.zeros(self.out_cap, dtype=torch.float32, device=d) for _ in range(5)]
+        self.bls_table = torch.zeros(max_requests * BLS_CURVE.itemsize, dtype=torch.uint8, device=d)
+        self.tls_table = torch.zeros(max_requests * TLS_CURVE.itemsize, dtype=torch.uint8, device=d)
+        self.counters = torch.zeros(2, dtype=torch.int32, device=d)
+        self.hbm_bytes = (self.sample_cap * SAMPLE_BYTES + self.out_cap * OUTPUT_BYTES +
+                          2 * max_requests * 64)
+        self.stream = torch.cuda.Stream(d)
+        self.h2d = torch.cuda.Stream(d)
+        self.d2h = torch.cuda.Stream(d)
+        self.waiting: collections.deque = collections.deque()
+        self.live_bls: list = []
+        self.live_tls: list = []
+        self.steps: collections.deque = collections.deque()
+        self.draining: list = []
+        self.results: list = []
+        self.step_count = 0
+        self.next_rid = 0
+        self.max_tls_nsc = 1
+
+    # -- requests -----------------------------------------------------------------------
+    def submit(self, req: Request, arrival: float | None = None) -> int:
+        n = req.n
+        if req.kind not in ("bls", "tls"):
+            raise ValueError("kind must be 'bls' or 'tls'")
+        if n == 0 or np.asarray(req.x).size != n:
+            raise ValueError("a request needs n >= 1 samples of time and flux")
+        if n > self.samples.cap or req.outputs > self.outs.cap:
+            raise ValueError("request of %d samples / %d outputs exceeds the HBM budget" % (n, req.outputs))
+        if req.kind == "bls" and (req.nf < 1 or n >= 1 << 23):
+            raise ValueError("BLS requests need nf >= 1 and n < 2^23")
+        if req.kind == "tls" and not 1 <= req.nsc <= 65536 - 31:
+            raise ValueError("GTLS requests need nsc in [1, 65505]")
+        rid = self.next_rid
+        self.next_rid += 1
+        self.waiting.append(_Live(rid, req, time.perf_counter() if arrival is None else arrival))
+        return rid
+
+    @property
+    def idle(self) -> bool:
+        return not (self.waiting or self.live_bls or self.live_tls or self.steps or self.draining)
+
+    # -- one step -------------------------------------------------------------------------
+    def _admit(self, now):
+        new = []
+        while self.waiting:
+            lv = self.waiting[0]
+            req = lv.req
+            desc_arena = self.bls_desc if req.kind == "bls" else self.tls_desc
+            s = self.samples.alloc(req.n)
+            if s is None:
+                break
+            o = self.outs.alloc(req.outputs)
+            if o is None:
+                self.samples.free(s, req.n)
+                break
+            dsl = desc_arena.alloc(1)
+            if dsl is None:
+                self.samples.free(s, req.n)
+                self.outs.free(o, req.outputs)
+                break
+            self.waiting.popleft()
+            lv.soff, lv.ooff, lv.desc, lv.admitted = s, o, dsl, now
+            if req.kind == "bls":
+                lv.tiles = (req.nf + self.F - 1) // self.F
+            else:
+                lv.tiles = (req.n + TLS_TILE - 1) // TLS_TILE
+            new.append(lv)
+        return new
+
+    def _upload_samples(self, new):
+        """Copy the new curves' samples (pinned staging, copy stream); returns the event the
+        compute stream waits for."""
+        total = sum(lv.req.n for lv in new)
+        th = torch.empty(total, dtype=torch.float32, pin_memory=True)
+        xh = torch.empty(total, dtype=torch.float32, pin_memory=True)
+        tn, xn = th.numpy(), xh.numpy()
+        p = 0
+        spans = []
+        for lv in new:
+            n = lv.req.n
+            tn[p:p + n] = lv.req.t
+            xn[p:p + n] = lv.req.x
+            spans.append((p, lv.soff, n))
+            p += n
+        # Slots are freed only after the last step reading them has finished, so the copy
+        # need not wait for the compute stream and overlaps the steps in flight.
+        with torch.cuda.stream(self.h2d):
+            for a, s, n in spans:
+                self.t[s:s + n].copy_(th[a:a + n], non_blocking=True)
+                self.x[s:s + n].copy_(xh[a:a + n], non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record(self.h2d)
+        return ev
+
+    def _meta(self, new, bls_segs, tls_segs):
+        """One pinned buffer with the step's descriptor rows, detrend list and work queues."""
+        nb = [lv for lv in new if lv.req.kind == "bls"]
+        nt = [lv for lv in new if lv.req.kind == "tls"]
+        parts = []
+        g_off = np.array([lv.soff for lv in new], np.uint64)
+        g_n = np.array([lv.req.n for lv in new], np.uint32)
+        bt = np.zeros(len(nb), BLS_CURVE)
+        for k, lv in enumerate(nb):
+            r = lv.req
+            bt[k] = (lv.soff, lv.ooff, r.n, r.nf, r.fmin, r.df, 0.0,
+                     r.ntrue if r.ntrue is not None else int(np.count_nonzero(np.asarray(r.t) >= 0)),
+                     0, 0, 0, r.kkmi if r.kkmi is not None else int(r.n * 0.005))
+        tt = np.zeros(len(nt), TLS_CURVE)
+        for k, lv in enumerate(nt):
+            r = lv.req
+            tt[k] = (lv.soff, lv.ooff, r.n, r.nsc, r.wmax, r.dw, r.deltat, 0)
+        bsg, bcum = bls_segs
+        tsg, tcum = tls_segs
+        for arr in (g_off, g_n, bsg, bcum, tsg, tcum):
+            parts.append(np.frombuffer(arr.tobytes(), np.uint8))
+        offs, p = [], 0
+        for a in parts:
+            offs.append(p)
+            p += (a.size + 255) // 256 * 256
+        host = torch.empty(max(p, 256), dtype=torch.uint8, pin_memory=True)
+        hn = host.numpy()
+        for a, o in zip(parts, offs):
+            hn[o:o + a.size] = a
+        devbuf = host.to(self.dev, non_blocking=True)   # on self.stream (current)
+        base = devbuf.data_ptr()
+        # descriptor rows go straight to their slots (new requests get consecutive slots
+        # when the descriptor arena is not fragmented; otherwise one copy per row)
+        for rows, table, live, dt in ((bt, self.bls_table, nb, BLS_CURVE), (tt, self.tls_table, nt, TLS_CURVE)):
+            if not len(rows):
+                continue
+            hb = torch.from_numpy(np.frombuffer(rows.tobytes(), np.uint8).copy()).pin_memory()
+            sz = dt.itemsize
+            slots = [lv.desc for lv in live]
+            if slots == list(range(slots[0], slots[0] + len(slots))):
+                table[slots[0] * sz:(slots[0] + len(slots)) * sz].copy_(hb, non_blocking=True)
+            else:
+                for k, sl in enumerate(slots):
+                    table[sl * sz:(sl + 1) * sz].copy_(hb[k * sz:(k + 1) * sz], non_blocking=True)
+        return devbuf, [base + o for o in offs], nb, nt
+
+    def _take(self, live, budget):
+        segs, counts = [], []
+        for lv in live:
+            if budget <= 0:
+                break
+            left = lv.tiles - lv.next_tile
+            if left <= 0:
+                continue
+            c = min(left, budget)
+            segs.append((lv.desc, lv.next_tile))
+            counts.append(c)
+            lv.next_tile += c
+            budget -= c
+        sg = np.array(segs, SEGMENT) if segs else np.zeros(0, SEGMENT)
+        cum = np.zeros(len(counts) + 1, np.uint32)
+        if counts:
+            np.cumsum(counts, out=cum[1:])
+        return sg, cum
+
+    def step(self, now: float | None = None) -> list:
+        """Admit, launch one step if there is work and fewer than ``depth`` steps in flight,
+        and collect finished requests.  Returns the results completed by this call."""
+        now = time.perf_counter() if now is None else now
+        done = self.poll()
+        if len(self.steps) >= self.depth:
+            return done
+        new = self._admit(now)
+        self.live_bls += [lv for lv in new if lv.req.kind == "bls"]
+        self.live_tls += [lv for lv in new if lv.req.kind == "tls"]
+        bls_segs = self._take(self.live_bls, self.bls_tiles)
+        tls_segs = self._take(self.live_tls, self.tls_tiles)
+        if not new and not len(bls_segs[0]) and not len(tls_segs[0]):
+            return done
+        si = self.step_count
+        self.step_count += 1
+        st = self.stream
+        with torch.cuda.stream(st):
+            if new:
+                ev = self._upload_samples(new)
+                st.wait_event(ev)
+            devbuf, (p_goff, p_gn, p_bsg, p_bcum, p_tsg, p_tcum), nb, nt = self._meta(new, bls_segs, tls_segs)
+            h = st.cuda_stream
+            if new:
+                N.call("gtrap_gfilter_packed", as_ptr(self.x), as_ptr(self.resid), p_goff, p_gn,
+                       len(new), max(lv.req.n for lv in new), self.r, h)
+            bsz = BLS_CURVE.itemsize
+            for lo, hi in _runs([lv.desc for lv in nb]):
+                nbr = hi - lo
+                tbl = as_ptr(self.bls_table) + lo * bsz
+                mx = max(lv.req.n for lv in nb if lo <= lv.desc < hi)
+                N.call("gtrap_bls_offsets", tbl, nbr, as_ptr(self.t), as_ptr(self.resid), h)
+                N.call("gtrap_bls_prepare", tbl, nbr, mx, as_ptr(self.t), as_ptr(self.resid),
+                       self.sample_cap, as_ptr(self.pool), self.pool_bytes, self.bls_spec.flags, h)
+            for lv in nt:
+                self.max_tls_nsc = max(self.max_tls_nsc, lv.req.nsc)
+            s = self.bls_spec
+            if len(bls_segs[0]):
+                N.call("gtrap_bls_run", as_ptr(self.bls_table), p_bsg, p_bcum, len(bls_segs[0]),
+                       as_ptr(self.t), as_ptr(self.pool), self.pool_bytes, self.sample_cap, s.nb,
+                       s.kma, s.kmi, self.F, s.flags, 0, as_ptr(self.counters[0:1]),
+                       as_ptr(self.o[0]), as_ptr(self.o[1]), as_ptr(self.o[2]), h)
+            ts = self.tls_spec
+            if len(tls_segs[0]):
+                N.call("gtrap_gtls_run", as_ptr(self.tls_table), p_tsg, p_tcum, len(tls_segs[0]),
+                       as_ptr(self.t), as_ptr(self.resid), ts.nw, ts.nl, self.max_tls_nsc, ts.mode,
+                       ts.flags, 0, as_ptr(self.counters[1:2]), *[as_ptr(a) for a in self.o], h)
+            ev = torch.cuda.Event()
+            ev.record(st)
+        step = _Step(si, ev)
+        step._keep = devbuf  # staging stays alive until the step has run
+        for live in (self.live_bls, self.live_tls):
+            for lv in live:
+                if lv.next_tile >= lv.tiles and lv.last_step < 0:
+                    lv.last_step = si
+                    step.finishing.append(lv)
+        self.live_bls = [lv for lv in self.live_bls if lv.last_step < 0]
+        self.live_tls = [lv for lv in self.live_tls if lv.last_step < 0]
+        self.steps.append(step)
+        return done
+
+    def poll(self) -> list:
+        """Start output copies of requests whose last step finished; return completed results."""
+        while self.steps and self.steps[0].event.query():
+            step = self.steps.popleft()
+            self.d2h.wait_event(step.event)
+            with torch.cuda.stream(self.d2h):
+                for lv in step.finishing:
+                    m, o = lv.req.outputs, lv.ooff
+                    k = 3 if lv.req.kind == "bls" else 5
+                    outs = []
+                    for j in range(k):
+                        h = torch.empty(m, dtype=torch.float32, pin_memory=True)
+                        h.copy_(self.o[j][o:o + m], non_blocking=True)
+                        outs.append(h)
+                    lv.result = tuple(outs)
+                    ev = torch.cuda.Event()
+                    ev.record(self.d2h)
+                    lv.d2h_event = ev
+            self.draining.extend(step.finishing)
+        out = []
+        keep = []
+        for lv in self.draining:
+            if lv.d2h_event.query():
+                now = time.perf_counter()
+                res = lv.result
+                if lv.req.kind == "bls":
+                    res = (res[0].numpy(), res[1].numpy().view(np.int32), res[2].numpy().view(np.int32))
+                else:
+                    res = tuple(a.numpy() for a in res)
+                self.samples.free(lv.soff, lv.req.n)
+                self.outs.free(lv.ooff, lv.req.outputs)
+                (self.bls_desc if lv.req.kind == "bls" else self.tls_desc).free(lv.desc, 1)
+                r = Result(lv.rid, lv.req.kind, lv.arrival, lv.admitted, now, res, lv.req.outputs)
+                self.results.append(r)
+                out.append(r)
+            else:
+                keep.append(lv)
+        self.draining = keep
+        return out
+
+    def wait(self, until: float | None = None):
+        """Block until something can change: the oldest step finishes when the pipeline is
+        full, else a short sleep (bounded by ``until``, a perf_counter time)."""
+        if len(self.steps) >= self.depth:
+            self.steps[0].event.synchronize()
+            return
+        dt = 0.0002
+        if until is not None:
+            dt = max(0.0, min(dt, until - time.perf_counter()))
+        if self.draining and not self.steps and until is None:
+            self.draining[0].d2h_event.synchronize()
+        elif dt > 0:
+            time.sleep(dt)
+
+    def run_until_idle(self) -> list:
+        """Drive steps until every submitted request has completed."""
+        out = []
+        while not self.idle:
+            n0 = self.step_count
+            got = self.step()
+            out += got
+            if self.step_count == n0 and not got:
+                self.wait()
+        return out
+
+    def hbm_high_water(self) -> int:
+        """Bytes of arena space held by admitted requests at the busiest moment."""
+        return self.samples.high_water * SAMPLE_BYTES + self.outs.high_water * OUTPUT_BYTES
+
+
+def _runs(slots):
+    """Maximal runs [lo, hi) of consecutive descriptor slots (slots sorted on return)."""
+    s = sorted(slots)
+    out = []
+    i = 0
+    while i < len(s):
+        j = i
+        while j + 1 < len(s) and s[j + 1] == s[j] + 1:
+            j += 1
+        out.append((s[i], s[j] + 1))
+        i = j + 1
+    return out
+
+
+class PlainServer:
+    """Baseline: each request is processed alone, in arrival order, by the plain entry points
+    (copy in, gfilter, get_offset, geebls or gtls, copy out), as a caller of the reference's
+    per-image kernels does."""
+
+    def __init__(self, bls: BlsSpec = BlsSpec(), tls: TlsSpec = TlsSpec(), detrend_r: int = 24,
+                 device=None):
+        require_cuda()
+        self.dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
+        self.bls_spec, self.tls_spec, self.r = bls, tls, int(detrend_r)
+        self.results: list = []
+        self.next_rid = 0
+
+    def process(self, req: Request, arrival: float | None = None) -> Result:
+        arrival = time.perf_counter() if arrival is None else arrival
+        start = time.perf_counter()
+        n = req.n
+        t = torch.from_numpy(np.ascontiguousarray(req.t, np.float32)).pin_memory().to(self.dev, non_blocking=True).view(n, 1)
+        x = torch.from_numpy(np.ascontiguousarray(req.x, np.float32)).pin_memory().to(self.dev, non_blocking=True).view(n, 1)
+        r = api.gfilter(x, self.r)
+        if req.kind == "bls":
+            s = self.bls_spec
+            off = api.offset(r, t)
+            ntrue = req.ntrue if req.ntrue is not None else int(np.count_nonzero(np.asarray(req.t) >= 0))
+            nt = torch.tensor([ntrue], dtype=torch.int32).pin_memory().to(self.dev, non_blocking=True)
+            kkmi = req.kkmi if req.kkmi is not None else int(n * 0.005)
+            outs = api.geebls(r, t, off, nt, req.nf, s.nb, s.kma, s.kmi, kkmi, req.fmin, req.df,
+                              phase=s.phase)
+            res = tuple(o.reshape(-1).cpu().numpy() for o in outs)
+            ev = req.nf
+        else:
+            ts = self.tls_spec
+            outs = api.gtls(r, t, n, ts.nw, ts.nl, req.nsc, req.wmax, req.dw, req.deltat,
+                            mode=ts.mode, fix_a=ts.fix_a)
+            res = tuple(o.reshape(-1).cpu().numpy() for o in outs)
+            ev = n
+        rid = self.next_rid
+        self.next_rid += 1
+        out = Result(rid, req.kind, arrival, start, time.perf_counter(), res, ev)
+        self.results.append(out)
+        return out
+
+
+# -- load generation and measurement ------------------------------------------------------------
+def poisson_trace(n_requests: int, rate: float, seed: int = 0) -> np.ndarray:
+    """Arrival offsets (seconds) of a Poisson process of ``rate`` requests per second."""
+    rng = np.random.default_rng(seed)
+    return np.cumsum(rng.exponential(1.0 / rate, n_requests))
+
+
+def serve_trace(server, requests, offsets) -> list:
+    """Offer ``requests[k]`` at ``offsets[k]`` seconds after the start (real time) and run the
+    server until all have completed.  Works with :class:`TransitServer` and
+    :class:`PlainServer`; returns the results in completion order."""
+    t0 = time.perf_counter()
+    k = 0
+    out = []
+    if isinstance(server, PlainServer):
+        for k, req in enumerate(requests):
+            arr = t0 + offsets[k]
+            while time.perf_counter() < arr:
+                pass
+            out.append(server.process(req, arr))
+        return out
+    n = len(requests)
+    while k < n or not server.idle:
+        now = time.perf_counter()
+        while k < n and t0 + offsets[k] <= now:
+            server.submit(requests[k], t0 + offsets[k])
+            k += 1
+        n0 = server.step_count
+        got = server.step(now)
+        out += got
+        if server.step_count == n0 and not got:
+            server.wait(t0 + offsets[k] if k < n else None)
+    return out
+
+
+def latency_summary(results, wall: float | None = None) -> dict:
+    lat = np.array([r.latency for r in results]) * 1e3
+    span = wall if wall is not None else (max(r.done for r in results) - min(r.arrival for r in results))
+    ev = sum(r.evals for r in results)
+    return dict(requests=len(results), p50_ms=float(np.percentile(lat, 50)),
+                p99_ms=float(np.percentile(lat, 99)), mean_ms=float(lat.mean()),
+                req_per_s=len(results) / span, evals_per_s=ev / span)

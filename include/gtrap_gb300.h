@@ -151,11 +151,11 @@ typedef struct {
   uint32_t tile0;   /* first tile of this segment */
 } gtrap_bls_segment;
 
-/* Detrend of packed curves: curve q is in[offs[q] .. offs[q+1]) (offs on the device, ncurves+1
- * entries); out = in - zero-padded running median of window 2r+1 within each curve
- * (gtrap_gfilter per curve).  max_n: longest curve. */
-int gtrap_gfilter_packed(const float *in, float *out, const uint64_t *offs, uint32_t ncurves,
-                         uint32_t max_n, uint32_t r, gtrap_stream_t stream);
+/* Detrend of packed curves: curve q is in[off[q] .. off[q] + n[q]) (off and n on the device);
+ * out = in - zero-padded running median of window 2r+1 within each curve (gtrap_gfilter per
+ * curve).  max_n: longest curve of the call. */
+int gtrap_gfilter_packed(const float *in, float *out, const uint64_t *off, const uint32_t *n,
+                         uint32_t ncurves, uint32_t max_n, uint32_t r, gtrap_stream_t stream);
 /* curves[q].offset = sum of resid over samples with t >= 0, divided by n (get_offset,
  * gtrap/gfilter.py:94-101), for packed curves. */
 int gtrap_bls_offsets(gtrap_bls_curve *curves, uint32_t ncurves, const float *t, const float *resid,

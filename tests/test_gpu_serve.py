@@ -1,0 +1,92 @@
+"""Continuous-batching server: every result equals its solo run (bit for bit) when mixed with
+other requests that arrive while it is on the GPU, admission holds to the HBM budget, and the
+plain per-request path gives the same spectra."""
+import numpy as np
+import pytest
+import torch
+
+from gtrap_gb300 import batch as B, serve as S, synth
+
+pytestmark = pytest.mark.gpu
+
+BLS = B.BlsSpec(nb=256, kma=27, kmi=1)
+TLS = B.TlsSpec(nw=4, nl=8)
+R = 8
+
+
+def _requests(count=10, seed=5000):
+    return [S.Request.from_curve(c) for c in synth.ragged_mix(count, seed=seed, n_range=(500, 5000))]
+
+
+def _server(**kw):
+    kw.setdefault("hbm_budget", 64e6)
+    kw.setdefault("bls_tiles", 60)   # small steps: requests span several steps
+    kw.setdefault("tls_tiles", 30)
+    return S.TransitServer(BLS, TLS, detrend_r=R, **kw)
+
+
+def _eq(a, b):
+    assert len(a) == len(b)
+    for u, v in zip(a, b):
+        np.testing.assert_array_equal(u, v)
+
+
+@pytest.fixture(scope="module")
+def solo(cuda):
+    reqs = _requests()
+    assert {r.kind for r in reqs} == {"bls", "tls"}
+    srv = _server()
+    out = []
+    for r in reqs:
+        srv.submit(r)
+        res = srv.run_until_idle()
+        assert len(res) == 1
+        out.append(res[0].outputs)
+    return reqs, out
+
+
+def test_mixed_equals_solo(solo):
+    reqs, ref = solo
+    srv = _server()
+    rids = [srv.submit(r) for r in reqs[:4]]
+    for _ in range(3):
+        srv.step()
+    rids += [srv.submit(r) for r in reqs[4:]]   # arrive while the first ones run
+    res = {r.rid: r for r in srv.run_until_idle()}
+    assert srv.step_count > 3 and len(res) == len(reqs)
+    for k, rid in enumerate(rids):
+        _eq(res[rid].outputs, ref[k])
+
+
+def test_admission_by_hbm_budget(solo):
+    reqs, ref = solo
+    n_max = max(r.n for r in reqs)
+    o_max = max(r.outputs for r in reqs)
+    # room for about two requests at a time
+    budget = int(2.2 * max(n_max * S.SAMPLE_BYTES / 0.8, o_max * S.OUTPUT_BYTES / 0.2))
+    srv = _server(hbm_budget=budget)
+    rids = [srv.submit(r) for r in reqs]
+    res = {r.rid: r for r in srv.run_until_idle()}
+    assert srv.samples.high_water <= srv.samples.cap and srv.outs.high_water <= srv.outs.cap
+    assert srv.hbm_high_water() <= budget
+    assert max(r.admitted for r in res.values()) > min(r.done for r in res.values())  # some waited
+    for k, rid in enumerate(rids):
+        _eq(res[rid].outputs, ref[k])
+    big = S.Request("bls", np.zeros(srv.samples.cap + 1, np.float32), np.zeros(srv.samples.cap + 1, np.float32), nf=10)
+    with pytest.raises(ValueError):
+        srv.submit(big)
+
+
+def test_plain_server_and_trace(solo):
+    reqs, ref = solo
+    plain = S.PlainServer(BLS, TLS, detrend_r=R)
+    for k, r in enumerate(reqs[:4]):
+        _eq(plain.process(r).outputs, ref[k])
+    srv = _server()
+    offsets = S.poisson_trace(len(reqs), rate=400.0, seed=3)
+    res = S.serve_trace(srv, reqs, offsets)
+    assert sorted(r.rid for r in res) == list(range(len(reqs)))
+    for r in res:
+        _eq(r.outputs, ref[r.rid])
+    summ = S.latency_summary(res)
+    assert summ["p99_ms"] >= summ["p50_ms"] > 0

@@ -1,0 +1,59 @@
+"""Host-side logic of the serving loop (no GPU): the HBM arena allocator, the descriptor-run
+splitter and the Poisson arrival trace."""
+import numpy as np
+import pytest
+
+from gtrap_gb300.serve import Arena, _runs, poisson_trace
+
+
+def test_arena_random_alloc_free_never_overlaps():
+    rng = np.random.default_rng(7)
+    a = Arena(100_000, align=32)
+    live = {}
+    occ = np.zeros(a.cap, bool)
+    for it in range(3000):
+        if live and rng.uniform() < 0.45:
+            s = list(live)[int(rng.integers(len(live)))]
+            n = live.pop(s)
+            a.free(s, n)
+            occ[s:s + a._round(n)] = False
+        else:
+            n = int(rng.integers(1, 5000))
+            s = a.alloc(n)
+            if s is None:
+                # first fit fails only when no free run is long enough
+                assert a._round(n) > max([0] + [y - x for x, y in a.free_list])
+                continue
+            assert s % 32 == 0
+            assert not occ[s:s + a._round(n)].any()
+            occ[s:s + a._round(n)] = True
+            live[s] = n
+        assert a.used == int(occ.sum())
+        # free list is sorted, coalesced and disjoint from the occupied ranges
+        fl = a.free_list
+        for (x0, x1), (y0, y1) in zip(fl, fl[1:]):
+            assert x1 < y0
+        for x0, x1 in fl:
+            assert not occ[x0:x1].any()
+    for s, n in list(live.items()):
+        a.free(s, n)
+    assert a.free_list == [(0, a.cap)] and a.used == 0
+    assert a.high_water <= a.cap
+
+
+def test_arena_double_free_and_exhaustion():
+    a = Arena(1024, align=32)
+    s = a.alloc(100)
+    assert a.alloc(2000) is None
+    a.free(s, 100)
+    with pytest.raises(ValueError):
+        a.free(s, 100)
+    assert a.alloc(1024) == 0 and a.alloc(1) is None
+
+
+def test_runs_and_trace():
+    assert _runs([]) == []
+    assert _runs([4, 2, 3, 7]) == [(2, 5), (7, 8)]
+    tr = poisson_trace(20000, rate=500.0, seed=1)
+    assert np.all(np.diff(tr) > 0)
+    assert abs(tr[-1] / 20000 - 1 / 500.0) < 0.05 / 500.0 * 10
