@@ -1,23 +1,31 @@
-"""Benchmark: detrend + masked BLS on Kepler-like light curves (one GB300).
+"""Benchmark of the batched transit search on one GB300 (one process per GPU).
 
-Workload (per GPU): 1024 curves x 65,536 samples at 29.4-min cadence with per-curve
-jittered times, 5% masked in contiguous gaps, sinusoid + quadratic trends, noise 5e-4 and
-box transits in a quarter of the curves; median detrend with a 49-sample window, offsets,
-then BLS over 16,384 frequencies (1/200 .. 2 per day) with nb = 2048 bins, qmi = 0.005,
-qma = 0.1 (kma = 205, kmi = 10, kkmi = 327), then per-curve peak statistics.
+Default workload (``--workload ragged``): the uneven mixed batch.  10,000 curves per GPU
+whose lengths are log-uniform on [2,000, 70,000] samples, each at 2-min or 29.4-min cadence,
+10% masked in contiguous gaps (t = -1000, zig-zag filled flux), three sinusoids plus a
+quadratic trend, box (BLS) or trapezoid (GTLS) signals in a quarter of the curves; half the
+curves are BLS requests (nb = 2048, qmi = 0.005, qma = 0.1 -> kma = 205, kmi = 10,
+kkmi = int(n*qmi); nf = clip(next_pow2(8 * baseline_days), 2048, 32768), fmin = 2/baseline,
+fmax = 2 per day) and half GTLS requests (8 widths from 8 h to 0.5 h, 16 ingress widths,
+nsc = wmax/cadence + 3, every sample an epoch).  Every curve is detrended with a 49-sample
+running median first.  A step is the whole batch: packed detrend -> offsets -> encoding ->
+one persistent BLS launch -> one persistent GTLS launch, replayed from CUDA graphs with the
+inputs resident in HBM (5-7 GB, far above L2).  ``value`` is evaluations per second:
+(curve, trial frequency) pairs of the BLS requests plus (curve, epoch) pairs of the GTLS
+requests.  ``plain`` is the same requests through the plain per-curve entry points (one
+launch sequence per curve); ``e2e`` repeats the step with the light curves copied from
+pinned host memory and every spectrum copied back inside the timed region.
 
-A step is that whole pipeline over the batch: gfilter -> offset -> geebls -> blsstat.
-``value`` is (curve x trial-frequency) evaluations per second with the inputs resident
-in HBM (inputs are 512 MiB, larger than L2).  ``e2e`` repeats the step through the
-tensor API with host buffers: pinned host -> device copies of the light curves and a
-device -> host read of the spectrum and peak statistics inside the timed region.
+``--workload masked``: 1024 Kepler-like curves x 65,536 samples, detrend + masked BLS over
+16,384 frequencies (the plain image entry points).  ``--workload served``: the
+continuous-batching server under Poisson arrivals (p50/p99 latency per offered load).
 
 ``--impl reference`` times the reference's algorithm on the host CPU (the FP64 C
-restatement of geebls with scipy's median filter, all host threads) on a bounded
+restatement of geebls and gtls with scipy's median filter, all host threads) on a bounded
 sample of the same workload and prints the same metric.
 
-Multi-GPU: one process per GPU (torchrun); every rank processes its own batch of
-curves (weak scaling, no data-path collective); the time is the max over ranks.
+Multi-GPU: one process per GPU (torchrun); every rank processes its own batch of curves
+(weak scaling, no data-path collective); times are the max over ranks.
 """
 from __future__ import annotations
 
@@ -38,8 +46,13 @@ sys.path.insert(0, ROOT)
 METRIC = "BLS/TLS (curve x freq) evals/sec vs plain; served p50/p99 at SR rel err<=1e-4"
 UNIT = "evals/s"
 
+# masked workload
 NQ, N, NF, NB, R_MEDIAN = 1024, 65536, 16384, 2048, 24
 QMI, QMA = 0.005, 0.1
+# ragged workload
+NCURVES = 10000
+KMA, KMI = int(QMA * NB) + 1, int(QMI * NB)
+NW, NL = 8, 16
 
 
 def parse():
@@ -48,25 +61,65 @@ def parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--nq", type=int, default=NQ, help="curves per GPU (default: the workload's 1024)")
+    p.add_argument("--workload", default="ragged", choices=["ragged", "masked", "served"])
+    p.add_argument("--nq", type=int, default=None,
+                   help="curves per GPU (default: 10,000 ragged, 1024 masked)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-plain", action="store_true")
     return p.parse_args()
 
 
-def workload_config(nq):
+def masked_config(nq):
     return {"workload": "detrend+masked BLS, Kepler-like: %d curves x %d samples, 29.4-min cadence, "
                         "5%% masked gaps, median window 49, nf=%d (1/200..2 /d), nb=%d, qmi=%g, qma=%g"
                         % (nq, N, NF, NB, QMI, QMA),
-            "curves_per_gpu": nq, "samples": N, "nf": NF, "nb": NB, "kma": int(QMA * NB) + 1,
-            "kmi": int(QMI * NB), "kkmi": int(N * QMI), "median_window": 2 * R_MEDIAN + 1,
+            "curves_per_gpu": nq, "samples": N, "nf": NF, "nb": NB, "kma": KMA,
+            "kmi": KMI, "kkmi": int(N * QMI), "median_window": 2 * R_MEDIAN + 1,
             "phase": "exact 64-bit fixed point", "l2": "inputs 512 MiB per GPU exceed L2 (no flush needed)"}
 
 
-def make_data(nq, seed):
-    from gtrap_gb300 import synth
-    lc, tu, ntrue, grid, inj = synth.kepler_like(nq=nq, n=N, nf=NF, nb=NB, qmi=QMI, qma=QMA, seed=seed)
-    return lc, tu, ntrue, grid
+def ragged_config(nc, bat=None):
+    cfg = {"workload": "uneven mixed BLS/GTLS batch: %d curves, n log-uniform [2000, 70000], cadence 2 or "
+                       "29.4 min, 10%% masked, median window 49; BLS nb=%d kma=%d kmi=%d kkmi=n*%g, "
+                       "nf=clip(next_pow2(8*baseline_d), 2048, 32768) from 2/baseline to 2 /d; GTLS "
+                       "nw=%d nl=%d (W 8 h..0.5 h), every sample an epoch; one persistent launch per "
+                       "search kind, CUDA graphs, autotuned tiles" % (nc, NB, KMA, KMI, QMI, NW, NL),
+           "curves_per_gpu": nc, "nb": NB, "kma": KMA, "kmi": KMI, "nw": NW, "nl": NL,
+           "median_window": 2 * R_MEDIAN + 1, "phase": "exact 64-bit fixed point",
+           "l2": "inputs of several GB per GPU exceed L2 (no flush needed)"}
+    if bat is not None:
+        cfg.update({"bls_curves": bat.n_bls, "tls_curves": bat.n_tls, "bls_evals": bat.bls_evals,
+                    "tls_evals": bat.tls_evals, "samples_total": bat.total,
+                    "tile_frequencies": bat.F, "bls_blocks": bat.bls_blocks, "tls_blocks": bat.tls_blocks})
+    return cfg
+
+
+def _profile(name):
+    path = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(path):
+        return None
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except Exception:
+        return None
+
+
+def fp32_peak_tflops(dev):
+    """FP32 FMA issue peak of this GPU, measured live (MEASURED_PEAKS.json has no FP32 figure)."""
+    import torch
+    from gtrap_gb300 import api
+    stream = torch.cuda.current_stream(dev)
+    _, flops = api.fp32_peak_probe(iters=4096)
+    torch.cuda.synchronize(dev)
+    ps, pe = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ps.record(stream)
+    for _ in range(3):
+        api.fp32_peak_probe(iters=4096)
+    pe.record(stream)
+    torch.cuda.synchronize(dev)
+    return flops * 3 / (ps.elapsed_time(pe) / 1e3) / 1e12
 
 
 # ----------------------------------------------------------------------------- clocks
@@ -117,7 +170,13 @@ class ClockSampler:
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
 
 
-# ----------------------------------------------------------------------------- CPU legs
+# ----------------------------------------------------------------------------- masked workload
+
+def make_data(nq, seed):
+    from gtrap_gb300 import synth
+    lc, tu, ntrue, grid, inj = synth.kepler_like(nq=nq, n=N, nf=NF, nb=NB, qmi=QMI, qma=QMA, seed=seed)
+    return lc, tu, ntrue, grid
+
 
 def cpu_pipeline_sample(lc, tu, ntrue, grid, n_curves, n_freqs, threads):
     """Reference algorithm on the host: scipy medfilt residual, masked mean offset and
@@ -134,7 +193,7 @@ def cpu_pipeline_sample(lc, tu, ntrue, grid, n_curves, n_freqs, threads):
     return n_curves * n_freqs / dt, dt
 
 
-def cpu_baseline(lc, tu, ntrue, grid):
+def masked_cpu_baseline(lc, tu, ntrue, grid):
     threads = os.cpu_count() or 1
     n_curves, n_freqs = 2, 256 * threads
     value, dt = cpu_pipeline_sample(lc, tu, ntrue, grid, n_curves, n_freqs, threads)
@@ -143,7 +202,7 @@ def cpu_baseline(lc, tu, ntrue, grid):
                       % (n_curves, n_freqs, dt)}
 
 
-def run_reference(args, rank, world):
+def run_masked_reference(args, rank, world):
     if rank != 0:
         return
     lc, tu, ntrue, grid = make_data(4, 2000)
@@ -160,7 +219,7 @@ def run_reference(args, rank, world):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": workload_config(NQ),
+            "data": "synthetic", "config": masked_config(NQ),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": "per step %d curve x %d frequencies (medfilt + offset + FP64 BLS)"
                                        % (n_curves, n_freqs)},
@@ -168,9 +227,7 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-# ----------------------------------------------------------------------------- GPU legs
-
-def run_ours(args, rank, world, local_rank):
+def run_masked(args, rank, world, local_rank):
     import torch
     import torch.distributed as dist
     from gtrap_gb300 import _build, api
@@ -178,7 +235,7 @@ def run_ours(args, rank, world, local_rank):
     _build.build()
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
-    nq = args.nq
+    nq = args.nq or NQ
     lc, tu, ntrue, grid = make_data(nq, 2000 + 100000 * rank)
     d_lc = torch.from_numpy(lc).to(dev)
     d_tu = torch.from_numpy(tu).to(dev)
@@ -265,30 +322,18 @@ def run_ours(args, rank, world, local_rank):
     if rank != 0:
         return
     # roofline of the dominant kernel (the BLS call: prep + fold/scan), FP32-pipe bound
-    sink, flops = api.fp32_peak_probe(iters=4096)
-    torch.cuda.synchronize(dev)
-    ps, pe = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ps.record(stream)
-    for _ in range(3):
-        api.fp32_peak_probe(iters=4096)
-    pe.record(stream)
-    torch.cuda.synchronize(dev)
-    peak = flops * 3 / (ps.elapsed_time(pe) / 1e3) / 1e12
+    peak = fp32_peak_tflops(dev)
     cand = NB * (kma - max(kmi, 1))            # accepted windows per evaluation
     flop_per_eval = 7.0 * cand                  # s, kk, N-kk, den, s^2 and an FMA compare
     achieved = flop_per_eval * nq * NF / (bls_ms / 1e3) / 1e12
     traffic = None
-    prof = os.path.join(ROOT, "profiles", "bls_fold_scan_traffic.json")
-    if os.path.exists(prof):
-        try:
-            with open(prof) as f:
-                traffic = json.load(f).get("dram_bytes_per_launch_full_workload")
-        except Exception:
-            traffic = None
+    prof = _profile("bls_fold_scan_traffic.json")
+    if prof:
+        traffic = prof.get("dram_bytes_per_launch_full_workload")
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+i64", "data": "synthetic",
-            "config": workload_config(nq) | {"parallelism": "replicas x%d (curves sharded)" % world},
+            "config": masked_config(nq) | {"parallelism": "replicas x%d (curves sharded)" % world},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "kernel": "geebls (prep + bls_fold_scan_kernel)", "kernel_ms": bls_ms,
@@ -299,7 +344,323 @@ def run_ours(args, rank, world, local_rank):
     if e2e:
         line["e2e"] = e2e
     if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(lc, tu, ntrue, grid)
+        line["cpu_baseline"] = masked_cpu_baseline(lc, tu, ntrue, grid)
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------- ragged workload
+
+def make_mix(nc, seed):
+    from gtrap_gb300 import synth
+    return synth.ragged_mix(nc, seed=seed)
+
+
+def build_batch(mix, dev_index):
+    from gtrap_gb300 import batch as B
+    bat = B.RaggedBatch(B.BlsSpec(nb=NB, kma=KMA, kmi=KMI), B.TlsSpec(nw=NW, nl=NL),
+                        detrend_r=R_MEDIAN, device=dev_index)
+    for c in mix:
+        if c["kind"] == "bls":
+            bat.add_bls(c["t"], c["x"], c["nf"], c["fmin"], c["df"], kkmi=c["kkmi"])
+        else:
+            bat.add_tls(c["t"], c["x"], c["nsc"], c["wmax"], c["dw"], c["deltat"])
+    return bat.build()
+
+
+def cpu_mix_rates(mix, threads, seconds):
+    """The reference's algorithm on the host for a bounded sample of the mix: scipy's median
+    filter, get_offset and the FP64 restatements of geebls and gtls, each kind run over
+    curves until ``seconds`` have passed.  Returns per-kind rates and a description."""
+    import oracle
+    bls = [c for c in mix if c["kind"] == "bls"]
+    tls = [c for c in mix if c["kind"] == "tls"]
+    t_med = n_med = 0.0
+    t_b = e_b = 0.0
+    t_t = e_t = 0.0
+    nb_c = nt_c = 0
+    for c in bls:
+        t0 = time.perf_counter()
+        resid = oracle.medfilt_residual(c["x"][:, None], R_MEDIAN)
+        t1 = time.perf_counter()
+        off = oracle.offset(resid, c["t"][:, None]).astype(np.float32)
+        ntrue = np.array([np.count_nonzero(c["t"] >= 0)], np.uint32)
+        nf = min(c["nf"], 64 * threads)
+        oracle.bls(resid, c["t"][:, None], nf, NB, KMA, KMI, c["kkmi"], c["fmin"], c["df"],
+                   offset=off, ntrue=ntrue, nthreads=threads)
+        t2 = time.perf_counter()
+        t_med += t1 - t0
+        n_med += c["x"].size
+        t_b += t2 - t1
+        e_b += nf
+        nb_c += 1
+        if t_b >= seconds:
+            break
+    for c in tls:
+        t0 = time.perf_counter()
+        resid = oracle.medfilt_residual(c["x"][:, None], R_MEDIAN)
+        t1 = time.perf_counter()
+        nt = min(c["x"].size, 512 * threads)
+        oracle.gtls(resid, c["t"][:, None], nt, NW, NL, c["nsc"], c["wmax"], c["dw"], c["deltat"],
+                    nthreads=threads)
+        t2 = time.perf_counter()
+        t_med += t1 - t0
+        n_med += c["x"].size
+        t_t += t2 - t1
+        e_t += nt
+        nt_c += 1
+        if t_t >= seconds:
+            break
+    rates = {"bls": e_b / t_b, "tls": e_t / t_t, "medfilt_samples": n_med / t_med}
+    desc = ("%d BLS curves x <=%d frequencies and %d GTLS curves x <=%d epochs of the mix "
+            "(scipy medfilt + get_offset + FP64 geebls/gtls restatements), %.1f s"
+            % (nb_c, 64 * threads, nt_c, 512 * threads, t_med + t_b + t_t))
+    return rates, desc, t_med + t_b + t_t
+
+
+def cpu_mix_value(mix, rates):
+    """Evaluations per second of the whole mix at the sampled per-kind CPU rates."""
+    bls_ev = sum(c["nf"] for c in mix if c["kind"] == "bls")
+    tls_ev = sum(c["x"].size for c in mix if c["kind"] == "tls")
+    samples = sum(c["x"].size for c in mix)
+    t = bls_ev / rates["bls"] + tls_ev / rates["tls"] + samples / rates["medfilt_samples"]
+    return (bls_ev + tls_ev) / t
+
+
+def ragged_cpu_baseline(mix, seconds=6.0):
+    threads = os.cpu_count() or 1
+    rates, desc, _ = cpu_mix_rates(mix, threads, seconds)
+    return {"value": cpu_mix_value(mix, rates), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": desc, "rates": rates}
+
+
+def run_ragged_reference(args, rank, world):
+    if rank != 0:
+        return
+    nc = args.nq or NCURVES
+    mix = make_mix(nc, 4000)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_mix_rates(mix[:40], threads, 0.2)
+    vals, total = [], 0.0
+    desc = ""
+    for k in range(args.steps):
+        rates, desc, dt = cpu_mix_rates(mix[200 * k:], threads, 1.5)
+        vals.append(cpu_mix_value(mix, rates))
+        total += dt
+    value = float(np.median(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": ragged_config(nc),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "per step: " + desc},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ragged(args, rank, world, local_rank):
+    import torch
+    import torch.distributed as dist
+    from gtrap_gb300 import _build, batch as B
+
+    _build.build()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    nc = args.nq or NCURVES
+    mix = make_mix(nc, 4000 + 100000 * rank)
+    bat = build_batch(mix, local_rank)
+    stream = torch.cuda.current_stream(dev)
+    B.autotune(bat)
+    graphs = bat.capture_stages()
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    marks = []
+
+    def step(timed=False):
+        graphs["prep"].replay()
+        if timed:
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+        graphs["bls"].replay()
+        if timed:
+            b.record(stream)
+            marks.append((a, b))
+        graphs["tls"].replay()
+
+    for _ in range(args.warmup):
+        step()
+    barrier()
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    start.record(stream)
+    for _ in range(args.steps):
+        step(timed=True)
+    end.record(stream)
+    barrier()
+    clk = clocks.stop()
+    ms = start.elapsed_time(end) / args.steps
+    bls_ms = float(np.mean([a.elapsed_time(b) for a, b in marks]))
+    t = torch.tensor([ms, bls_ms], device=dev, dtype=torch.float64)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms, bls_ms = float(t[0]), float(t[1])
+    evals_rank = bat.bls_evals + bat.tls_evals
+    evals = evals_rank * world
+    value = evals / (ms / 1e3)
+    ref = [bat.bls_result(k) for k in range(0, bat.n_bls, max(1, bat.n_bls // 64))]
+    ref_t = [bat.tls_result(k) for k in range(0, bat.n_tls, max(1, bat.n_tls // 64))]
+
+    plain = None
+    if not args.no_plain:
+        # the same requests, one plain launch sequence per curve (warm-up on a few curves)
+        B.run_plain(bat, bls_curves=range(min(8, bat.n_bls)), tls_curves=range(min(8, bat.n_tls)))
+        barrier()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        w0 = time.perf_counter()
+        s.record(stream)
+        B.run_plain(bat)
+        e.record(stream)
+        barrier()
+        pw = time.perf_counter() - w0
+        pms = torch.tensor([max(s.elapsed_time(e), 1e3 * pw)], device=dev, dtype=torch.float64)
+        if world > 1:
+            dist.all_reduce(pms, op=dist.ReduceOp.MAX)
+        same = all(np.array_equal(x, y) for a, k in zip(ref, range(0, bat.n_bls, max(1, bat.n_bls // 64)))
+                   for x, y in zip(a, bat.bls_result(k)))
+        same = same and all(np.array_equal(x, y) for a, k in zip(ref_t, range(0, bat.n_tls, max(1, bat.n_tls // 64)))
+                            for x, y in zip(a, bat.tls_result(k)))
+        plain = {"value": evals / (float(pms[0]) / 1e3), "unit": UNIT, "ms_per_step": float(pms[0]),
+                 "what": "same requests through the plain per-curve entry points (gfilter, get_offset, "
+                         "geebls or gtls per curve), one pass",
+                 "bit_identical_sampled_outputs": bool(same)}
+        step()  # restore the batch's own outputs
+
+    e2e = None
+    if not args.no_e2e:
+        h_t = bat.t.cpu().pin_memory()
+        h_x = bat.x.cpu().pin_memory()
+        h_b = [torch.empty(a.numel(), dtype=a.dtype).pin_memory() for a in (bat.blsp, bat.ph1, bat.ph2)]
+        h_o = [torch.empty(a.numel(), dtype=a.dtype).pin_memory() for a in bat.tls_outs]
+
+        def e2e_step():
+            bat.t.copy_(h_t, non_blocking=True)
+            bat.x.copy_(h_x, non_blocking=True)
+            step()
+            for h, a in zip(h_b, (bat.blsp, bat.ph1, bat.ph2)):
+                h.copy_(a, non_blocking=True)
+            for h, a in zip(h_o, bat.tls_outs):
+                h.copy_(a, non_blocking=True)
+
+        e2e_step()
+        barrier()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        for _ in range(args.steps):
+            e2e_step()
+        e.record(stream)
+        barrier()
+        ems = torch.tensor([s.elapsed_time(e) / args.steps], device=dev, dtype=torch.float64)
+        if world > 1:
+            dist.all_reduce(ems, op=dist.ReduceOp.MAX)
+        h2d = (h_t.numel() + h_x.numel()) * 4
+        d2h = sum(h.numel() * h.element_size() for h in h_b + h_o)
+        e2e = {"value": evals / (float(ems[0]) / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "ms_per_step": float(ems[0]),
+               "api": "gtrap_gb300.batch.RaggedBatch (graph replays) with pinned host buffers"}
+
+    if rank != 0:
+        return
+    peak = fp32_peak_tflops(dev)
+    flop_per_eval = 7.0 * NB * (KMA - max(KMI, 1))   # s, kk, N-kk, den, s^2 and an FMA compare
+    achieved = flop_per_eval * bat.bls_evals / (bls_ms / 1e3) / 1e12
+    traffic = None
+    prof = _profile("bls_queue_ragged_traffic.json")
+    if prof and prof.get("dram_bytes_per_sample_frequency"):
+        unit_work = float(sum(int(r["n"]) * int(r["nf"]) for r in bat.bls_table))
+        traffic = prof["dram_bytes_per_sample_frequency"] * unit_work
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+i64", "data": "synthetic",
+            "config": ragged_config(nc, bat) | {"parallelism": "replicas x%d (curves sharded)" % world},
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "bls_queue_kernel (persistent BLS fold + scan)", "kernel_ms": bls_ms,
+                         "kernel_share": bls_ms / ms,
+                         "peak_source": "live FP32 FMA-chain probe on this GPU (MEASURED_PEAKS.json has no FP32 figure)",
+                         "flop_per_eval": flop_per_eval},
+            "gpu_launches": 6 * args.steps,
+            "clocks": clk}
+    if plain:
+        line["plain"] = plain
+    if e2e:
+        line["e2e"] = e2e
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = ragged_cpu_baseline(mix)
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------- served workload
+
+def run_served(args, rank, world, local_rank):
+    """Offered Poisson load swept over fractions of the measured saturation; one JSON line
+    with the saturation throughput and p50/p99 latency per offered load, beside the plain
+    per-request server."""
+    import torch
+    from gtrap_gb300 import _build, serve as S, synth
+
+    _build.build()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    npool = args.nq or 1500
+    pool = [S.Request.from_curve(c) for c in synth.ragged_mix(npool, seed=5000 + 100000 * rank,
+                                                                n_range=(1000, 70000))]
+    srv = S.TransitServer(detrend_r=R_MEDIAN, hbm_budget=100e9)
+    for r in pool[:40]:
+        srv.submit(r)
+    srv.run_until_idle()
+    t0 = time.perf_counter()
+    for r in pool:
+        srv.submit(r, t0)
+    res = srv.run_until_idle()
+    sat = S.latency_summary(res, time.perf_counter() - t0)
+    plain = S.PlainServer(detrend_r=R_MEDIAN)
+    for r in pool[:10]:
+        plain.process(r)
+    t0 = time.perf_counter()
+    pres = [plain.process(r, t0) for r in pool[:300]]
+    psat = S.latency_summary(pres, time.perf_counter() - t0)
+    sweep = []
+    for frac in (0.1, 0.2, 0.3, 0.4, 0.5, 0.6, 0.7, 0.8, 0.9, 1.0, 1.1, 1.2):
+        rate = frac * sat["req_per_s"]
+        m = min(npool, max(200, int(rate * 1.5)))
+        offs = S.poisson_trace(m, rate, seed=int(frac * 1000))
+        s = S.latency_summary(S.serve_trace(srv, pool[:m], offs))
+        prate = frac * sat["req_per_s"]
+        pm = min(300, max(60, int(prate * 0.5)))
+        ps = S.latency_summary(S.serve_trace(plain, pool[:pm], S.poisson_trace(pm, prate, seed=int(frac * 1000))))
+        sweep.append({"offered_frac": frac, "offered_req_per_s": rate, "requests": m,
+                      "served_req_per_s": s["req_per_s"], "p50_ms": s["p50_ms"], "p99_ms": s["p99_ms"],
+                      "evals_per_s": s["evals_per_s"],
+                      "plain": {"requests": pm, "served_req_per_s": ps["req_per_s"],
+                                "p50_ms": ps["p50_ms"], "p99_ms": ps["p99_ms"]}})
+    if rank != 0:
+        return
+    line = {"metric": METRIC, "value": sat["evals_per_s"], "unit": UNIT, "n_gpus": world,
+            "steps": 1, "warmup": 1, "ms_per_step": 1e3 * npool / sat["req_per_s"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64",
+            "data": "synthetic",
+            "config": {"workload": "served: Poisson arrivals of single-curve BLS/GTLS requests (50/50, "
+                                   "detrended), n log-uniform [1000, 70000], nf 2k-32k, HBM budget 100 GB",
+                       "pool": npool, "depth": srv.depth, "bls_tiles_per_step": srv.bls_tiles,
+                       "tls_tiles_per_step": srv.tls_tiles},
+            "saturation": sat, "plain_saturation": psat, "sweep": sweep,
+            "hbm_high_water_bytes": srv.hbm_high_water()}
     print(json.dumps(line), flush=True)
 
 
@@ -309,7 +670,10 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
-        run_reference(args, rank, world)
+        if args.workload == "masked":
+            run_masked_reference(args, rank, world)
+        else:
+            run_ragged_reference(args, rank, world)
         return
     if world > 1:
         import torch
@@ -317,7 +681,8 @@ def main():
         torch.cuda.set_device(local_rank)
         dist.init_process_group("nccl")
     try:
-        run_ours(args, rank, world, local_rank)
+        {"ragged": run_ragged, "masked": run_masked, "served": run_served}[args.workload](
+            args, rank, world, local_rank)
     finally:
         if world > 1:
             import torch.distributed as dist

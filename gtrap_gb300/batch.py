@@ -352,6 +352,23 @@ class RaggedBatch:
         self.graph = g
         return g
 
+    def capture_stages(self) -> dict:
+        """Capture prep, BLS and GTLS as three graphs ({"prep", "bls", "tls"}), so that events
+        recorded between their replays time each stage."""
+        side = torch.cuda.Stream(self.device)
+        side.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(side):
+            self.launch()
+        torch.cuda.current_stream(self.device).wait_stream(side)
+        graphs = {}
+        for name, fn in (("prep", self.launch_prep), ("bls", self.launch_bls), ("tls", self.launch_tls)):
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, capture_error_mode="thread_local"):
+                fn()
+            graphs[name] = g
+        self.stage_graphs = graphs
+        return graphs
+
     # -- results ------------------------------------------------------------------------
     def bls_result(self, k: int):
         """(blsp, phase1, phase2) of BLS request k as numpy arrays (synchronises)."""
@@ -439,10 +456,11 @@ def autotune(batch: RaggedBatch, F_candidates=(2, 3, 4, 5, 6, 8, 12), bps_candid
 
 
 # -- plain baseline ---------------------------------------------------------------------------
-def run_plain(batch: RaggedBatch, stream=None):
+def run_plain(batch: RaggedBatch, stream=None, bls_curves=None, tls_curves=None):
     """The same requests through the plain per-curve entry points (one gfilter, offset and
     geebls or gtls launch sequence per curve, as a caller of the reference does for curves
-    with different lengths or grids), writing into the batch's output arrays."""
+    with different lengths or grids), writing into the batch's output arrays.  ``bls_curves``
+    and ``tls_curves`` restrict the run to those request indices."""
     if not batch.built:
         batch.build()
     dev = batch.device
@@ -450,7 +468,7 @@ def run_plain(batch: RaggedBatch, stream=None):
     s = batch.bls_spec
     ntrue = torch.from_numpy(batch.bls_table["ntrue"].astype(np.int32)).to(dev) if batch.n_bls else None
     given = torch.from_numpy(batch.bls_table["offset"].astype(np.float32)).to(dev) if batch.n_bls else None
-    for k in range(batch.n_bls):
+    for k in (range(batch.n_bls) if bls_curves is None else bls_curves):
         a, n = int(offs[k]), int(offs[k + 1] - offs[k])
         x = batch.x[a:a + n].view(n, 1)
         t = batch.t[a:a + n].view(n, 1)
@@ -463,7 +481,7 @@ def run_plain(batch: RaggedBatch, stream=None):
                    out=(batch.blsp[o:o + nf].view(1, nf), batch.ph1[o:o + nf].view(1, nf),
                         batch.ph2[o:o + nf].view(1, nf)), stream=stream)
     ts = batch.tls_spec
-    for k in range(batch.n_tls):
+    for k in (range(batch.n_tls) if tls_curves is None else tls_curves):
         j = batch.n_bls + k
         a, n = int(offs[j]), int(offs[j + 1] - offs[j])
         x = batch.x[a:a + n].view(n, 1)
