@@ -318,6 +318,12 @@ __device__ __forceinline__ unsigned long long pack_key(float pw, int i, int e) {
          (unsigned long long)(0xffffffffu - (((unsigned)i << 15) | (unsigned)e));
 }
 
+// Shared layout of a frequency's histogram / prefix entries (8 bytes each): within every
+// aligned block of 8 entries the slot is XOR-permuted by bits 4..6 of the index, so that a
+// warp whose lanes touch entries 8*lane + r (the prefix pass) spreads over all 16 bank pairs,
+// while 32 consecutive entries still map onto the same aligned 32-entry block.
+__device__ __forceinline__ int swz(int e) { return e ^ ((e >> 4) & 7); }
+
 __device__ __forceinline__ void group_bar(int id, int nthreads) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
@@ -396,8 +402,11 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
         unsigned *h = h32;
         for (uint32_t f = 0; f < nfrem; ++f) {
           const uint32_t bin = MODE == 0 ? (uint32_t)(ph >> shift) : (uint32_t)__umul64hi(ph, (unsigned long long)nb);
-          atomicAdd(h + 2 * bin, wS);
-          atomicAdd(h + 2 * bin + 1, wC);
+          // S in the low word for bins with bit 4 clear, in the high word otherwise, so that
+          // the S (and the C) updates of a warp reach all 32 banks
+          const uint32_t w = 2u * (uint32_t)swz((int)bin) + ((bin >> 4) & 1u);
+          atomicAdd(h + w, wS);
+          atomicAdd(h + (w ^ 1u), wC);
           ph += ab[u].y;
           h += 2 * a.region;
         }
@@ -414,8 +423,9 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
       for (uint32_t f = 0; f < nfrem; ++f) {
         const uint32_t bin = ref_bin(t, f);
         if (bin < (uint32_t)nb) {
-          atomicAdd(h + 2 * bin, wS);
-          atomicAdd(h + 2 * bin + 1, wC);
+          const uint32_t w = 2u * (uint32_t)swz((int)bin) + ((bin >> 4) & 1u);
+          atomicAdd(h + w, wS);
+          atomicAdd(h + (w ^ 1u), wC);
         } else {
           atomicAdd(drop_cnt + f, 1u);
         }
@@ -439,7 +449,7 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
         bin = ref_bin(__ldg(Tq + k), f);
         if (bin >= (uint32_t)nb) continue;
       }
-      atomicAdd(Hf + bin, inc);
+      atomicAdd(Hf + swz((int)bin), inc);
     }
   };
   __syncthreads();
@@ -474,7 +484,12 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
       const bool fast = pass == 0;
       unsigned long long hv[R];
 #pragma unroll
-      for (int r = 0; r < R; ++r) hv[r] = (i0 + r < nb) ? H[i0 + r] : 0ull;
+      for (int r = 0; r < R; ++r) {
+        const int b = i0 + r;
+        unsigned long long v = b < nb ? H[swz(b)] : 0ull;
+        if (fast && ((b >> 4) & 1)) v = (v << 32) | (v >> 32);  // S back in the low word
+        hv[r] = v;
+      }
       group_bar(1 + g, Tg);
       sxv = 0;
       scv = 0;
@@ -540,22 +555,24 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
     for (int r = 0; r < R; ++r) {
       const int e = i0 + r + 1;
       if (e <= nb) {
-        P[e] = make_float2(__ll2float_rn(ex + px[r]), (float)(ec + pc[r]));
-        if (e <= kma) P[nb + e] = make_float2(__ll2float_rn(tx + ex + px[r]), (float)(tc + ec + pc[r]));
+        P[swz(e)] = make_float2(__ll2float_rn(ex + px[r]), (float)(ec + pc[r]));
+        if (e <= kma) P[swz(nb + e)] = make_float2(__ll2float_rn(tx + ex + px[r]), (float)(tc + ec + pc[r]));
       }
     }
   }
   if (tid < 64) { best_key[tid] = 0ull; best_thr[tid] = 0u; }
   __syncthreads();
 
-  // ---- per 32-entry chunk of end bins: maximum and minimum of the flux prefix
+  // ---- per 32-entry chunk of end bins: maximum and minimum of the flux prefix (a chunk is
+  // one aligned 32-entry block, whatever the slot order inside it)
   const int elast = nb + kma;  // last written prefix entry
   for (int item = warp; item < (int)nfrem * nchunk; item += kThreads / 32) {
     const int f = item / nchunk, c = item - f * nchunk;
     const float2 *P = reinterpret_cast<const float2 *>(sm + (size_t)f * a.region);
-    const int e = 32 * c + lane;
-    const float v = e <= elast ? P[e].x : 0.0f;
-    float mx = e <= elast ? v : -INFINITY, mn = e <= elast ? v : INFINITY;
+    const int q = 32 * c + lane;
+    const bool ok = swz(q) <= elast;
+    const float v = ok ? P[q].x : 0.0f;
+    float mx = ok ? v : -INFINITY, mn = ok ? v : INFINITY;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
@@ -563,9 +580,8 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
     }
     if (lane == 0) reinterpret_cast<float2 *>(sm + (size_t)f * a.region)[lp + c] = make_float2(mx, mn);
   }
-  // ---- seed every frequency's threshold with the widest window of every start
   auto window_power = [&](const float2 *P, int i, int e, float &pw) -> bool {
-    const float2 Pi = P[i], Pe = P[e];
+    const float2 Pi = P[swz(i)], Pe = P[swz(e)];
     const float s = Pe.x - Pi.x;
     const float kk = Pe.y - Pi.y;
     const float den = kk * ((Nf + Pi.y) - Pe.y);
@@ -573,22 +589,44 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
     pw = __fdiv_rn(s * s, den);
     return pw > 0.0f;
   };
+  // ---- seed every frequency's running best with real windows: for every start, widths
+  // kma, kma/2, kma/4, kma/8 and kma/16 (at least kmi + 1).  Quotients are approximate while
+  // the warp picks its best window; only that window's power is computed exactly and
+  // published, so the seed is the exact power of a real window (a valid lower bound of the
+  // maximum) and may itself be the answer.
   if (kma > kmi) {
     const int per_f = (nb + 31) & ~31;  // whole warps per frequency
     for (int idx = tid; idx < (int)nfrem * per_f; idx += kThreads) {
       const int f = idx / per_f, i = idx - f * per_f;
       const float2 *P = reinterpret_cast<const float2 *>(sm + (size_t)f * a.region);
-      float pw = 0.0f;
-      if (i < nb && !window_power(P, i, i + kma, pw)) pw = 0.0f;
-      unsigned long long key = pw > 0.0f ? pack_key(pw, i, i + kma) : 0ull;
+      float pa = 0.0f;
+      int kb = 0;
+      if (i < nb) {
+        const float2 Pi = P[swz(i)];
+        const float Ni = Nf + Pi.y;
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const unsigned long long ok = __shfl_xor_sync(0xffffffffu, key, o);
-        key = ok > key ? ok : key;
+        for (int m = 0; m < 5; ++m) {
+          const int k = max(kma >> m, kmi + 1);
+          const float2 Pe = P[swz(i + k)];
+          const float s = Pe.x - Pi.x;
+          const float kk = Pe.y - Pi.y;
+          const float den = kk * (Ni - Pe.y);
+          const float s2 = s * s;
+          const float q = den > 0.0f ? __fdividef(s2, den) : (den == 0.0f && s2 > 0.0f ? INFINITY : 0.0f);
+          if (kk > kkmi_f && q > pa) { pa = q; kb = k; }
+        }
       }
-      if (lane == 0 && key) {
-        atomicMax(best_thr + f, (unsigned)(key >> 32));
-        atomicMax(best_key + f, key);
+      // warp argmax of the approximate powers (lowest lane on ties)
+      float wp = pa;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) wp = fmaxf(wp, __shfl_xor_sync(0xffffffffu, wp, o));
+      const unsigned who = __ballot_sync(0xffffffffu, pa == wp && wp > 0.0f);
+      if (who && lane == __ffs(who) - 1) {
+        float pw;
+        if (window_power(P, i, i + kb, pw)) {
+          atomicMax(best_thr + f, __float_as_uint(pw));
+          atomicMax(best_key + f, pack_key(pw, i, i + kb));
+        }
       }
     }
   }
@@ -601,7 +639,9 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
   // (den = kk (N - kk) is concave in kk), and units whose bound is below the frequency's shared
   // running best (times the pre-test slack) cannot hold the maximum.  A warp takes four
   // consecutive start groups; each lane bounds one (start group, chunk) unit, and the warp then
-  // evaluates the surviving units together, one end bin per lane.
+  // evaluates the surviving units together, one end bin per lane.  A start group is one
+  // aligned 8-entry block: its entries are read with four 16-byte broadcast loads and used in
+  // slot order (slot j holds start s0 + (j ^ h), h = the block's swizzle).
   const int ntask_f = (nb + kRS - 1) / kRS;          // start groups per frequency
   const int ngrp_f = (ntask_f + 3) / 4;              // warp jobs per frequency
   const int njob = (kma > kmi) ? (int)nfrem * ngrp_f : 0;
@@ -610,140 +650,153 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
     const int f = job / ngrp_f;
     const int t0 = (job - f * ngrp_f) * 4;
     const float2 *P = reinterpret_cast<const float2 *>(sm + (size_t)f * a.region);
-    const float2 *CM = P + lp;
-    // this lane's start group for bounding
-    const int kb = lane >> 3, mb = lane & 7;
-    const int sb = (t0 + kb) * kRS;
-    const bool grp_ok = t0 + kb < ntask_f;
-    int b_elo = 0, b_ehi = -1;
-    float b_ysmin = 0.0f, b_ysmax = 0.0f, b_c0 = 0.0f, b_cl = 0.0f;
-    if (grp_ok) {
-      const int nrs_b = min(kRS, nb - sb);
-      b_elo = sb + kmi + 1;
-      b_ehi = min(sb + nrs_b - 1 + kma, elast);
-      b_ysmin = INFINITY;
-      b_ysmax = -INFINITY;
-      for (int r = 0; r < nrs_b; ++r) {
-        const float y = P[sb + r].x;
-        b_ysmin = fminf(b_ysmin, y);
-        b_ysmax = fmaxf(b_ysmax, y);
-      }
-      b_c0 = P[sb].y;
-      b_cl = P[sb + nrs_b - 1].y;
-    }
     for (int cbase = 0; cbase < span_chunks; cbase += 8) {
-      // bound of unit (start group kb, chunk c) on this lane
-      const float thr = __uint_as_float(best_thr[f]) * kSlack;
-      const int c = (b_elo >> 5) + cbase + mb;
-      bool keep = false;
-      if (grp_ok && c <= (b_ehi >> 5)) {
-        const int ce_lo = max(32 * c, b_elo), ce_hi = min(32 * c + 31, b_ehi);
-        const float kk_hi = P[ce_hi].y - b_c0;
-        if (kk_hi > kkmi_f) {
-          const float kk_lo = fmaxf(P[ce_lo].y - b_cl, kkmi_f + 1.0f);
-          const float den_min = fminf(kk_lo * (Nf - kk_lo), kk_hi * (Nf - kk_hi));
-          const float2 cm = CM[c];
-          const float smax = fmaxf(cm.x - b_ysmin, b_ysmax - cm.y);
-          keep = !(den_min > 0.0f && smax * smax < thr * den_min);
-        }
-      }
-      unsigned live = __ballot_sync(0xffffffffu, keep);
-      int cur = -1;  // start group whose registers are loaded
-      float ys[kRS] = {}, beta[kRS] = {}, gamma[kRS] = {};
-      float blo = 0.0f, c0 = 0.0f, clast = 0.0f, bpow = 0.0f;
-      int bi = INT_MAX, be = INT_MAX, s0 = 0, nrs = 0, elo = 0, ehi = -1;
-      auto coeffs = [&]() {
+      unsigned live;
+      {
+        // bound of unit (start group kb, chunk c) on this lane
+        const int kb = lane >> 3, mb = lane & 7;
+        const int sb = (t0 + kb) * kRS;
+        bool keep = false;
+        if (t0 + kb < ntask_f) {
+          const int nrs_b = min(kRS, nb - sb);
+          const int b_elo = sb + kmi + 1;
+          const int b_ehi = min(sb + nrs_b - 1 + kma, elast);
+          const int c = (b_elo >> 5) + cbase + mb;
+          if (c <= (b_ehi >> 5)) {
+            const float4 *Q = reinterpret_cast<const float4 *>(P + sb);
+            const int hb = (sb >> 4) & 7;
+            float ysmin = INFINITY, ysmax = -INFINITY;
 #pragma unroll
-        for (int r = 0; r < kRS; ++r) {
-          const float cr = P[s0 + r].y;
-          const float ar = cr - c0, br = (Nf + cr) - c0;
-          beta[r] = -blo * (ar + br);
-          gamma[r] = (blo * ar) * br;
+            for (int q = 0; q < kRS / 2; ++q) {
+              const float4 v = Q[q];
+              if (((2 * q) ^ hb) < nrs_b) { ysmin = fminf(ysmin, v.x); ysmax = fmaxf(ysmax, v.x); }
+              if (((2 * q + 1) ^ hb) < nrs_b) { ysmin = fminf(ysmin, v.z); ysmax = fmaxf(ysmax, v.z); }
+            }
+            const float thr = __uint_as_float(best_thr[f]) * kSlack;
+            const int ce_lo = max(32 * c, b_elo), ce_hi = min(32 * c + 31, b_ehi);
+            const float kk_hi = P[swz(ce_hi)].y - P[swz(sb)].y;
+            if (kk_hi > kkmi_f) {
+              const float kk_lo = fmaxf(P[swz(ce_lo)].y - P[swz(sb + nrs_b - 1)].y, kkmi_f + 1.0f);
+              const float den_min = fminf(kk_lo * (Nf - kk_lo), kk_hi * (Nf - kk_hi));
+              const float2 cm = P[lp + c];
+              const float smax = fmaxf(cm.x - ysmin, ysmax - cm.y);
+              keep = !(den_min > 0.0f && smax * smax < thr * den_min);
+            }
+          }
+        }
+        live = __ballot_sync(0xffffffffu, keep);
+      }
+      float ys[kRS] = {}, beta[kRS] = {}, gamma[kRS] = {};
+      float blo = 0.0f, c0 = 0.0f, bpow = 0.0f;
+      int bk = INT_MAX;  // best window of this lane: (start << 15) | end
+      int s0 = -1;       // first start of the loaded group (-1: none)
+      bool improved = false;
+      // pre-test coefficients of the loaded group at threshold blo, in slot order
+      auto coeffs = [&]() {
+        const float4 *Q = reinterpret_cast<const float4 *>(P + s0);
+#pragma unroll
+        for (int q = 0; q < kRS / 2; ++q) {
+          const float4 v = Q[q];
+          const float a0 = v.y - c0, b0 = (Nf + v.y) - c0;
+          const float a1 = v.w - c0, b1 = (Nf + v.w) - c0;
+          beta[2 * q] = -blo * (a0 + b0);
+          gamma[2 * q] = (blo * a0) * b0;
+          beta[2 * q + 1] = -blo * (a1 + b1);
+          gamma[2 * q + 1] = (blo * a1) * b1;
         }
       };
-      // exact evaluation of (start s0 + r, end e): pre-test, then the rounded quotient
-      auto consider = [&](int r, float2 Pe, int e) {
-        const float cr = P[s0 + r].y;
-        const float s = Pe.x - ys[r];
+      // exact evaluation of (slot j, end e): pre-test, then the rounded quotient
+      auto consider = [&](int j, float2 Pe, int e) {
+        const int i = s0 + (j ^ ((s0 >> 4) & 7));
+        const float cr = P[s0 + j].y;
+        const float s = Pe.x - ys[j];
         const float kk = Pe.y - cr;
         const float den = kk * ((Nf + cr) - Pe.y);
         const float s2 = s * s;
         // den <= 0 (a window holding every sample) gives an infinite or negative power
-        if (r < nrs && kk > kkmi_f && (den <= 0.0f || fmaf(-blo, den, s2) >= 0.0f)) {
+        if (i < nb && kk > kkmi_f && (den <= 0.0f || fmaf(-blo, den, s2) >= 0.0f)) {
           const float pw = __fdiv_rn(s2, den);
-          if (pw > 0.0f && better(pw, s0 + r, e, bpow, bi, be)) {
+          const int key = (i << 15) | e;
+          if (pw > 0.0f && (pw > bpow || (pw == bpow && key < bk))) {
             bpow = pw;
-            bi = s0 + r;
-            be = e;
+            bk = key;
+            improved = true;
           }
         }
       };
       auto flush = [&]() {  // warp best of the loaded start group into the frequency record
-        if (!__any_sync(0xffffffffu, bi != INT_MAX)) return;
+        if (!__any_sync(0xffffffffu, bk != INT_MAX)) return;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
           const float op = __shfl_down_sync(0xffffffffu, bpow, o);
-          const int oi = __shfl_down_sync(0xffffffffu, bi, o);
-          const int oe = __shfl_down_sync(0xffffffffu, be, o);
-          if (better(op, oi, oe, bpow, bi, be)) { bpow = op; bi = oi; be = oe; }
+          const int ok = __shfl_down_sync(0xffffffffu, bk, o);
+          if (op > bpow || (op == bpow && ok < bk)) { bpow = op; bk = ok; }
         }
-        if (lane == 0 && bi != INT_MAX) atomicMax(best_key + f, pack_key(bpow, bi, be));
+        if (lane == 0 && bk != INT_MAX) atomicMax(best_key + f, pack_key(bpow, bk >> 15, bk & 0x7fff));
         bpow = 0.0f;
-        bi = be = INT_MAX;
+        bk = INT_MAX;
       };
       while (live) {
         const int src = __ffs(live) - 1;
         live &= live - 1;
         const int k = src >> 3;
-        const int cc = (((t0 + k) * kRS + kmi + 1) >> 5) + cbase + (src & 7);
-        if (k != cur) {
-          if (cur >= 0) flush();
-          cur = k;
+        if ((t0 + k) * kRS != s0) {
+          if (s0 >= 0) flush();
           s0 = (t0 + k) * kRS;
-          nrs = min(kRS, nb - s0);
-          elo = s0 + kmi + 1;
-          ehi = min(s0 + nrs - 1 + kma, elast);
-#pragma unroll
-          for (int r = 0; r < kRS; ++r) ys[r] = P[s0 + r].x;  // entries up to nb + kRS - 1 exist
-          c0 = P[s0].y;
-          clast = P[s0 + nrs - 1].y;
+          const float4 *Q = reinterpret_cast<const float4 *>(P + s0);
+          c0 = P[swz(s0)].y;
           blo = __uint_as_float(best_thr[f]) * kSlack;
-          coeffs();
+#pragma unroll
+          for (int q = 0; q < kRS / 2; ++q) {  // entries up to nb + kRS - 1 exist
+            const float4 v = Q[q];
+            ys[2 * q] = v.x;
+            ys[2 * q + 1] = v.z;
+            const float a0 = v.y - c0, b0 = (Nf + v.y) - c0;
+            const float a1 = v.w - c0, b1 = (Nf + v.w) - c0;
+            beta[2 * q] = -blo * (a0 + b0);
+            gamma[2 * q] = (blo * a0) * b0;
+            beta[2 * q + 1] = -blo * (a1 + b1);
+            gamma[2 * q + 1] = (blo * a1) * b1;
+          }
         } else {
           const float gb = __uint_as_float(best_thr[f]) * kSlack;
           if (gb > blo) { blo = gb; coeffs(); }
         }
-        const int e = 32 * cc + lane;
-        const float before = bpow;
+        const int cc = ((s0 + kmi + 1) >> 5) + cbase + (src & 7);
+        const int nrs = min(kRS, nb - s0);
+        const int hs = (s0 >> 4) & 7;
+        const int q = 32 * cc + lane;   // physical entry; its logical end bin:
+        const int e = swz(q);
+        improved = false;
         // interior: every (lane, start) has k in range; otherwise windows outside
         // (kmi, kma] or past the last end are masked before the fast test
         const bool interior = nrs == kRS && 32 * cc >= s0 + kRS + kmi && 32 * cc + 31 <= s0 + kma;
-        if (interior || (e >= elo && e <= ehi)) {
-          const float2 Pe = P[e];
+        if (interior || (e >= s0 + kmi + 1 && e <= min(s0 + nrs - 1 + kma, elast))) {
+          const float2 Pe = P[q];
           const float u = Pe.y - c0;
           const float G = (blo * u) * u;
           const unsigned base = (unsigned)(e - s0 - kmi - 1);
           unsigned neg = 0xffffffffu;
 #pragma unroll
-          for (int r = 0; r < kRS; ++r) {
-            const float s = Pe.x - ys[r];
-            const float t = fmaf(s, s, fmaf(u, beta[r], G + gamma[r]));
-            const bool in = interior || base - (unsigned)r < (unsigned)(kma - kmi);
+          for (int j = 0; j < kRS; ++j) {
+            const float s = Pe.x - ys[j];
+            const float t = fmaf(s, s, fmaf(u, beta[j], G + gamma[j]));
+            const bool in = interior || base - (unsigned)(j ^ hs) < (unsigned)(kma - kmi);
             neg &= in ? __float_as_uint(t) : 0x80000000u;
           }
           if (!(neg >> 31)) {  // kk and the exact pre-test are checked in consider
 #pragma unroll
-            for (int r = 0; r < kRS; ++r) {
-              const float s = Pe.x - ys[r];
-              const float t = fmaf(s, s, fmaf(u, beta[r], G + gamma[r]));
-              const bool in = interior || base - (unsigned)r < (unsigned)(kma - kmi);
-              if (in && !(t < 0.0f)) consider(r, Pe, e);
+            for (int j = 0; j < kRS; ++j) {
+              const float s = Pe.x - ys[j];
+              const float t = fmaf(s, s, fmaf(u, beta[j], G + gamma[j]));
+              const bool in = interior || base - (unsigned)(j ^ hs) < (unsigned)(kma - kmi);
+              if (in && !(t < 0.0f)) consider(j, Pe, e);
             }
           }
         }
-        if (bpow != before) atomicMax(best_thr + f, __float_as_uint(bpow));
+        if (improved) atomicMax(best_thr + f, __float_as_uint(bpow));
       }
-      if (cur >= 0) flush();
+      if (s0 >= 0) flush();
     }
   }
   __syncthreads();
