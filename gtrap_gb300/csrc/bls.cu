@@ -563,22 +563,28 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
   if (tid < 64) { best_key[tid] = 0ull; best_thr[tid] = 0u; }
   __syncthreads();
 
-  // ---- per 32-entry chunk of end bins: maximum and minimum of the flux prefix (a chunk is
-  // one aligned 32-entry block, whatever the slot order inside it)
+  // ---- per 32-entry chunk of end bins: maximum and minimum of the flux prefix (float2 at
+  // entry lp + c) and the count prefix at the chunk's last entry (float at lp + nchunk, index c);
+  // a chunk is one aligned 32-entry block, whatever the slot order inside it
   const int elast = nb + kma;  // last written prefix entry
   for (int item = warp; item < (int)nfrem * nchunk; item += kThreads / 32) {
     const int f = item / nchunk, c = item - f * nchunk;
     const float2 *P = reinterpret_cast<const float2 *>(sm + (size_t)f * a.region);
     const int q = 32 * c + lane;
     const bool ok = swz(q) <= elast;
-    const float v = ok ? P[q].x : 0.0f;
-    float mx = ok ? v : -INFINITY, mn = ok ? v : INFINITY;
+    const float2 v = ok ? P[q] : make_float2(0.0f, 0.0f);
+    float mx = ok ? v.x : -INFINITY, mn = ok ? v.x : INFINITY;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
       mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
     }
-    if (lane == 0) reinterpret_cast<float2 *>(sm + (size_t)f * a.region)[lp + c] = make_float2(mx, mn);
+    const float clast = __shfl_sync(0xffffffffu, v.y, swz(min(32 * c + 31, elast)) - 32 * c);
+    if (lane == 0) {
+      unsigned long long *R = sm + (size_t)f * a.region + lp;
+      reinterpret_cast<float2 *>(R)[c] = make_float2(mx, mn);
+      reinterpret_cast<float *>(R + nchunk)[c] = clast;
+    }
   }
   auto window_power = [&](const float2 *P, int i, int e, float &pw) -> bool {
     const float2 Pi = P[swz(i)], Pe = P[swz(e)];
@@ -590,7 +596,7 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
     return pw > 0.0f;
   };
   // ---- seed every frequency's running best with real windows: for every start, widths
-  // kma, kma/2, kma/4, kma/8 and kma/16 (at least kmi + 1).  Quotients are approximate while
+  // kma, kma/4 and kma/16 (at least kmi + 1).  Quotients are approximate while
   // the warp picks its best window; only that window's power is computed exactly and
   // published, so the seed is the exact power of a real window (a valid lower bound of the
   // maximum) and may itself be the answer.
@@ -605,7 +611,7 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
         const float2 Pi = P[swz(i)];
         const float Ni = Nf + Pi.y;
 #pragma unroll
-        for (int m = 0; m < 5; ++m) {
+        for (int m = 0; m < 6; m += 2) {
           const int k = max(kma >> m, kmi + 1);
           const float2 Pe = P[swz(i + k)];
           const float s = Pe.x - Pi.x;
@@ -646,47 +652,56 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
   const int ngrp_f = (ntask_f + 3) / 4;              // warp jobs per frequency
   const int njob = (kma > kmi) ? (int)nfrem * ngrp_f : 0;
   const int span_chunks = ((kRS - 1 + kma - kmi - 1) >> 5) + 2;   // chunks one start group touches
+  float ys[kRS] = {}, beta[kRS] = {}, gamma[kRS] = {};
   for (int job = warp; job < njob; job += kThreads / 32) {
     const int f = job / ngrp_f;
     const int t0 = (job - f * ngrp_f) * 4;
     const float2 *P = reinterpret_cast<const float2 *>(sm + (size_t)f * a.region);
+    const float2 *CM = reinterpret_cast<const float2 *>(sm + (size_t)f * a.region + lp);
+    const float *CL = reinterpret_cast<const float *>(sm + (size_t)f * a.region + lp + nchunk);
     for (int cbase = 0; cbase < span_chunks; cbase += 8) {
       unsigned live;
       {
-        // bound of unit (start group kb, chunk c) on this lane
+        // the job's 32 starts, one per lane (an aligned 32-entry block): per group of 8 the
+        // minimum and maximum flux prefix and the count prefix at its first and last start
         const int kb = lane >> 3, mb = lane & 7;
         const int sb = (t0 + kb) * kRS;
+        const int nrs_b = min(kRS, nb - sb);
+        float g_min, g_max, g_c0, g_cl;
+        {
+          const int si = t0 * kRS + lane;
+          const float2 Ps = si < lp ? P[swz(si)] : make_float2(0.0f, 0.0f);
+          g_min = si < nb ? Ps.x : INFINITY;
+          g_max = si < nb ? Ps.x : -INFINITY;
+#pragma unroll
+          for (int o = 1; o < 8; o <<= 1) {
+            g_min = fminf(g_min, __shfl_xor_sync(0xffffffffu, g_min, o));
+            g_max = fmaxf(g_max, __shfl_xor_sync(0xffffffffu, g_max, o));
+          }
+          g_c0 = __shfl_sync(0xffffffffu, Ps.y, lane & ~7);
+          g_cl = __shfl_sync(0xffffffffu, Ps.y, (lane & ~7) + max(nrs_b, 1) - 1);
+        }
+        // bound of unit (start group kb, chunk c) on this lane; the count prefix at the last
+        // entry of chunks c - 1 and c widens [kk_lo, kk_hi], which only loosens the bound
         bool keep = false;
         if (t0 + kb < ntask_f) {
-          const int nrs_b = min(kRS, nb - sb);
           const int b_elo = sb + kmi + 1;
           const int b_ehi = min(sb + nrs_b - 1 + kma, elast);
           const int c = (b_elo >> 5) + cbase + mb;
           if (c <= (b_ehi >> 5)) {
-            const float4 *Q = reinterpret_cast<const float4 *>(P + sb);
-            const int hb = (sb >> 4) & 7;
-            float ysmin = INFINITY, ysmax = -INFINITY;
-#pragma unroll
-            for (int q = 0; q < kRS / 2; ++q) {
-              const float4 v = Q[q];
-              if (((2 * q) ^ hb) < nrs_b) { ysmin = fminf(ysmin, v.x); ysmax = fmaxf(ysmax, v.x); }
-              if (((2 * q + 1) ^ hb) < nrs_b) { ysmin = fminf(ysmin, v.z); ysmax = fmaxf(ysmax, v.z); }
-            }
+            const float2 cm = CM[c];
             const float thr = __uint_as_float(best_thr[f]) * kSlack;
-            const int ce_lo = max(32 * c, b_elo), ce_hi = min(32 * c + 31, b_ehi);
-            const float kk_hi = P[swz(ce_hi)].y - P[swz(sb)].y;
+            const float kk_hi = CL[c] - g_c0;
             if (kk_hi > kkmi_f) {
-              const float kk_lo = fmaxf(P[swz(ce_lo)].y - P[swz(sb + nrs_b - 1)].y, kkmi_f + 1.0f);
+              const float kk_lo = fmaxf((c > 0 ? CL[c - 1] : 0.0f) - g_cl, kkmi_f + 1.0f);
               const float den_min = fminf(kk_lo * (Nf - kk_lo), kk_hi * (Nf - kk_hi));
-              const float2 cm = P[lp + c];
-              const float smax = fmaxf(cm.x - ysmin, ysmax - cm.y);
+              const float smax = fmaxf(cm.x - g_min, g_max - cm.y);
               keep = !(den_min > 0.0f && smax * smax < thr * den_min);
             }
           }
         }
         live = __ballot_sync(0xffffffffu, keep);
       }
-      float ys[kRS] = {}, beta[kRS] = {}, gamma[kRS] = {};
       float blo = 0.0f, c0 = 0.0f, bpow = 0.0f;
       int bk = INT_MAX;  // best window of this lane: (start << 15) | end
       int s0 = -1;       // first start of the loaded group (-1: none)
@@ -922,7 +937,8 @@ int make_plan(uint32_t nb, uint32_t kma, uint32_t nf, uint32_t F_req, Plan *p) {
   // per chunk
   const uint32_t last = nb + (kma > (uint32_t)kRS ? kma : (uint32_t)kRS);
   const uint32_t lp = (last + 1 + 31) / 32 * 32;
-  uint32_t region = lp + lp / 32;
+  // prefix entries, one float2 (max, min) per chunk, one float (last count) per chunk
+  uint32_t region = lp + lp / 32 + (lp / 32 + 1) / 2;
   region = (region + 1) & ~1u;  // 16-byte multiple for the zero fill
   const uint32_t G = kThreads / Tg;
   const size_t per_f = (size_t)region * 8;
@@ -1162,15 +1178,21 @@ int gtrap_bls_run(const gtrap_bls_curve *curves, const gtrap_bls_segment *segs, 
   qa.counter = counter;
   cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), stream);
   if (e != cudaSuccess) return fail(GTRAP_ERR_CUDA, "bls_run: cudaMemsetAsync: %s", cudaGetErrorString(e));
-  if (blocks == 0) {
-    const int per_sm = (size_t)gtrap::smem_per_sm() >= 2 * (p.smem + 4096) ? 2 : 1;
-    blocks = (uint32_t)(gtrap::sm_count() * per_sm);
-  }
   const int mode = !exact ? 2 : (gtrap::is_pow2(nb) ? 0 : 1);
   const void *fn;
+  // blocks == 0: as many as fit on the SMs at once (the queue keeps them busy)
 #define GTRAP_BLS_QLAUNCH(RR, MM)                                                          \
   fn = (const void *)bls_queue_kernel<RR, MM>;                                              \
   GTRAP_TRY(gtrap::ensure_smem(fn, p.smem, "bls_run"));                                     \
+  if (blocks == 0) {                                                                        \
+    int per_sm = 0;                                                                         \
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bls_queue_kernel<RR, MM>,    \
+                                                      kThreads, p.smem) != cudaSuccess) {   \
+      cudaGetLastError();                                                                   \
+      per_sm = 1;                                                                           \
+    }                                                                                       \
+    blocks = (uint32_t)(gtrap::sm_count() * (per_sm > 0 ? per_sm : 1));                     \
+  }                                                                                         \
   bls_queue_kernel<RR, MM><<<blocks, kThreads, p.smem, stream>>>(sh, qa);
   if (p.R == 8) {
     if (mode == 0) { GTRAP_BLS_QLAUNCH(8, 0) } else if (mode == 1) { GTRAP_BLS_QLAUNCH(8, 1) } else { GTRAP_BLS_QLAUNCH(8, 2) }

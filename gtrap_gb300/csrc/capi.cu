@@ -17,6 +17,11 @@ int g_sm_count[kMaxDevices];
 int g_smem_optin[kMaxDevices];
 int g_smem_sm[kMaxDevices];
 std::mutex g_attr_mutex;
+constexpr size_t kMaxFuncs = 256;
+const void *g_static_fn[kMaxFuncs];
+int g_static_dev[kMaxFuncs];
+size_t g_static_sz[kMaxFuncs];
+size_t g_static_n = 0;
 
 int current_device() {
   int dev = 0;
@@ -70,10 +75,34 @@ int smem_per_sm() {
 }
 
 int ensure_smem(const void *func, size_t bytes, const char *what) {
+  // static shared memory of the kernel counts against the same per-block limit
+  size_t static_bytes = 0;
+  {
+    std::lock_guard<std::mutex> lock(g_attr_mutex);
+    int dev = current_device();
+    size_t k = 0;
+    for (; k < g_static_n && !(g_static_fn[k] == func && g_static_dev[k] == dev); ++k) {}
+    if (k == g_static_n) {
+      cudaFuncAttributes fa;
+      if (cudaFuncGetAttributes(&fa, func) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(GTRAP_ERR_CUDA, "%s: cudaFuncGetAttributes failed", what);
+      }
+      if (g_static_n < kMaxFuncs) {
+        g_static_fn[g_static_n] = func;
+        g_static_dev[g_static_n] = dev;
+        g_static_sz[g_static_n] = fa.sharedSizeBytes;
+        ++g_static_n;
+      }
+      static_bytes = fa.sharedSizeBytes;
+    } else {
+      static_bytes = g_static_sz[k];
+    }
+  }
+  if (bytes + static_bytes > (size_t)max_smem_optin())
+    return fail(GTRAP_ERR_INVALID_ARG, "%s: needs %zu + %zu bytes of shared memory, device allows %d",
+                what, bytes, static_bytes, max_smem_optin());
   if (bytes <= 48 * 1024) return GTRAP_OK;
-  if (bytes > (size_t)max_smem_optin())
-    return fail(GTRAP_ERR_INVALID_ARG, "%s: needs %zu bytes of shared memory, device allows %d",
-                what, bytes, max_smem_optin());
   // The attribute is per function and per device; setting it again is harmless, and
   // the call is cheap next to a launch, so it is simply repeated (also during capture).
   std::lock_guard<std::mutex> lock(g_attr_mutex);

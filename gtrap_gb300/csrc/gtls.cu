@@ -486,7 +486,10 @@ int gtrap_gtls_run(const gtrap_tls_curve *curves, const gtrap_tls_segment *segs,
   if (e != cudaSuccess) return fail(GTRAP_ERR_CUDA, "gtls_run: cudaMemsetAsync: %s", cudaGetErrorString(e));
   if (blocks == 0) {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gtls_queue_kernel, kTlsThreads, smem);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gtls_queue_kernel, kTlsThreads, smem) != cudaSuccess) {
+      cudaGetLastError();
+      per_sm = 1;
+    }
     blocks = (uint32_t)(gtrap::sm_count() * (per_sm > 0 ? per_sm : 1));
   }
   gtls_queue_kernel<<<blocks, kTlsThreads, smem, stream>>>(qa);

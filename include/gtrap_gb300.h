@@ -171,7 +171,7 @@ int gtrap_bls_prepare(gtrap_bls_curve *curves, uint32_t ncurves, uint32_t max_n,
                       const float *x, uint64_t total_samples, void *pool, size_t pool_bytes,
                       uint32_t flags, gtrap_stream_t stream);
 /* Run the listed tiles: persistent blocks pop items from a device counter (zeroed by the
- * call).  blocks = 0 picks one or two blocks per SM.  t is needed only with
+ * call).  blocks = 0 picks as many as fit on the SMs at once.  t is needed only with
  * GTRAP_BLS_PHASE_FP32_REF.  phase pointers may be NULL. */
 int gtrap_bls_run(const gtrap_bls_curve *curves, const gtrap_bls_segment *segs, const uint32_t *cum,
                   uint32_t nseg, const float *t, const void *pool, size_t pool_bytes,
