@@ -399,16 +399,21 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
         const unsigned wS = (unsigned)(xq[u] >> 10);
         const unsigned wC = ((unsigned)(xq[u] & 1023) << 12) | 1u;
         unsigned long long ph = ab[u].x + (unsigned long long)j0 * ab[u].y;
-        unsigned *h = h32;
-        for (uint32_t f = 0; f < nfrem; ++f) {
+        // S in the low word for bins with bit 4 clear, in the high word otherwise, so that
+        // the S (and the C) updates of a warp reach all 32 banks
+        auto add = [&](unsigned *h) {
           const uint32_t bin = MODE == 0 ? (uint32_t)(ph >> shift) : (uint32_t)__umul64hi(ph, (unsigned long long)nb);
-          // S in the low word for bins with bit 4 clear, in the high word otherwise, so that
-          // the S (and the C) updates of a warp reach all 32 banks
           const uint32_t w = 2u * (uint32_t)swz((int)bin) + ((bin >> 4) & 1u);
           atomicAdd(h + w, wS);
           atomicAdd(h + (w ^ 1u), wC);
           ph += ab[u].y;
-          h += 2 * a.region;
+        };
+        if (nfrem <= 8) {
+#pragma unroll
+          for (uint32_t f = 0; f < 8; ++f)
+            if (f < nfrem) add(h32 + f * 2 * a.region);
+        } else {
+          for (uint32_t f = 0; f < nfrem; ++f) add(h32 + f * 2 * a.region);
         }
       }
     }
@@ -551,13 +556,30 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
     }
     // P[e] = (flux prefix, count prefix) over bins [0, e) of the wrapped axis, e <= nb + kma
     if (gtid == 0) P[0] = make_float2(0.0f, 0.0f);
+    float vmx = __ll2float_rn(ex), vmn = vmx;  // flux prefix over entries i0 .. i0 + R - 1
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       const int e = i0 + r + 1;
+      const float v = __ll2float_rn(ex + px[r]);
+      if (r < R - 1) { vmx = fmaxf(vmx, v); vmn = fminf(vmn, v); }
       if (e <= nb) {
-        P[swz(e)] = make_float2(__ll2float_rn(ex + px[r]), (float)(ec + pc[r]));
+        P[swz(e)] = make_float2(v, (float)(ec + pc[r]));
         if (e <= kma) P[swz(nb + e)] = make_float2(__ll2float_rn(tx + ex + px[r]), (float)(tc + ec + pc[r]));
       }
+    }
+    // chunk statistics of the chunks below nb (entries 32c .. 32c + 31 < nb) from the 32 / R
+    // threads that hold them; the rest come from the chunk pass below
+    constexpr int kTpc = 32 / R;
+#pragma unroll
+    for (int o = 1; o < kTpc; o <<= 1) {
+      vmx = fmaxf(vmx, __shfl_xor_sync(0xffffffffu, vmx, o));
+      vmn = fminf(vmn, __shfl_xor_sync(0xffffffffu, vmn, o));
+    }
+    const int cch = gtid / kTpc;
+    if (gtid % kTpc == kTpc - 1 && cch < (nb >> 5)) {
+      unsigned long long *Rc = H + lp;
+      reinterpret_cast<float2 *>(Rc)[cch] = make_float2(vmx, vmn);
+      reinterpret_cast<float *>(Rc + nchunk)[cch] = (float)(ec + pc[R - 2]);
     }
   }
   if (tid < 64) { best_key[tid] = 0ull; best_thr[tid] = 0u; }
@@ -567,8 +589,10 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
   // entry lp + c) and the count prefix at the chunk's last entry (float at lp + nchunk, index c);
   // a chunk is one aligned 32-entry block, whatever the slot order inside it
   const int elast = nb + kma;  // last written prefix entry
-  for (int item = warp; item < (int)nfrem * nchunk; item += kThreads / 32) {
-    const int f = item / nchunk, c = item - f * nchunk;
+  const int c_lo = nb >> 5;                  // chunks below nb were done in the prefix pass
+  const int nrest = max(0, min(nchunk, elast / 32 + 1) - c_lo);
+  for (int item = warp; item < (int)nfrem * nrest; item += kThreads / 32) {
+    const int f = item / nrest, c = c_lo + (item - f * nrest);
     const float2 *P = reinterpret_cast<const float2 *>(sm + (size_t)f * a.region);
     const int q = 32 * c + lane;
     const bool ok = swz(q) <= elast;
