@@ -36,6 +36,10 @@ namespace {
 
 using gtrap::fail;
 
+#ifndef GTRAP_TLS_MINB
+#define GTRAP_TLS_MINB 4  // blocks per SM the register budget is sized for
+#endif
+
 constexpr int kWarps = 8;
 constexpr int kTlsThreads = kWarps * 32;
 constexpr int kMaxStage = 7000;  // staged samples: nsc + 31
@@ -361,7 +365,7 @@ __device__ __forceinline__ void gtls_tile(const TlsArgs &a, const int e0) {
 }
 
 // Plain launch over an [n, nq] image: block = (epoch tile, curve), curves fastest.
-__global__ void __launch_bounds__(kTlsThreads) gtls_kernel(const TlsArgs img, const int nq) {
+__global__ void __launch_bounds__(kTlsThreads, GTRAP_TLS_MINB) gtls_kernel(const TlsArgs img, const int nq) {
   __shared__ TlsArgs v;
   const int tile = blockIdx.x / nq;
   const int q = blockIdx.x - tile * nq;
@@ -386,7 +390,7 @@ struct TlsQueue {
   uint32_t *counter;
 };
 
-__global__ void __launch_bounds__(kTlsThreads) gtls_queue_kernel(const TlsQueue qa) {
+__global__ void __launch_bounds__(kTlsThreads, GTRAP_TLS_MINB) gtls_queue_kernel(const TlsQueue qa) {
   __shared__ uint32_t item_s;
   __shared__ TlsArgs v;
   const uint32_t total = qa.cum[qa.nseg];
