@@ -209,3 +209,44 @@ def fp32_peak_probe(iters=4096, stream=None):
     flops = C.c_double(0.0)
     N.call("gtrap_probe_fp32_peak", as_ptr(sink), int(iters), C.byref(flops), stream_handle(stream))
     return sink, flops.value
+
+
+# Record layout of gtrap_peak_stats (include/gtrap_gb300.h).
+import numpy as _np
+
+PEAK_STATS = _np.dtype([("maxsn", "<f4"), ("argmax", "<u4"), ("lent", "<u4"), ("npeaks", "<u4"),
+                        ("median", "<f8"), ("std", "<f8"), ("far", "<f8"), ("pssn", "<f8"),
+                        ("diff", "<f8"), ("medc", "<f8"), ("stdc", "<f8")])
+assert PEAK_STATS.itemsize == 72
+
+
+def peakstat(sn: torch.Tensor, off: torch.Tensor, n: torch.Tensor, stride: int, max_n: int,
+             mpd: int = 10, ntop: int = 4, k: int = 8, stream=None):
+    """Peak statistics of S/N series on the device (gtrap/gtls.py:245-273 with detect_peaks):
+    series q is ``sn[off[q] + e*stride]``, e < n[q].  Returns (stats as a uint8 device tensor
+    of ``PEAK_STATS`` records, peak indices [nq, k] int32, peak heights [nq, k] float32)."""
+    require_cuda()
+    sn = _f32(sn, "sn")
+    nq = int(off.numel())
+    dev = sn.device
+    stats = torch.empty(nq * PEAK_STATS.itemsize, dtype=torch.uint8, device=dev)
+    idx = torch.empty((nq, max(k, 1)), dtype=torch.int32, device=dev)
+    val = torch.empty((nq, max(k, 1)), dtype=torch.float32, device=dev)
+    N.call("gtrap_peakstat", as_ptr(sn), as_ptr(off), as_ptr(n), int(stride), nq, int(max_n),
+           int(mpd), int(ntop), int(k), as_ptr(stats), as_ptr(idx), as_ptr(val),
+           stream_handle(stream))
+    return stats, idx[:, :k], val[:, :k]
+
+
+def stats_to_numpy(stats: torch.Tensor):
+    """``PEAK_STATS`` records of a stats tensor from :func:`peakstat` (synchronises)."""
+    return _np.frombuffer(stats.cpu().numpy().tobytes(), PEAK_STATS)
+
+
+def tls_peakstat(tlssn: torch.Tensor, mpd: int = 10, ntop: int = 4, k: int = 8, stream=None):
+    """Peak statistics of every curve of a GTLS output image ``tlssn[nt, nq]``."""
+    tlssn = _f32(tlssn, "tlssn")
+    nt, nq = tlssn.shape
+    off = torch.arange(nq, dtype=torch.int64, device=tlssn.device)
+    n = torch.full((nq,), nt, dtype=torch.int32, device=tlssn.device)
+    return peakstat(tlssn, off, n, nq, nt, mpd, ntop, k, stream)

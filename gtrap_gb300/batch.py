@@ -369,6 +369,16 @@ class RaggedBatch:
         self.stage_graphs = graphs
         return graphs
 
+    def tls_peakstat(self, mpd: int = 10, ntop: int = 4, k: int = 8, stream=None):
+        """Peak statistics of every GTLS request's S/N series on the device (see
+        :func:`gtrap_gb300.api.peakstat`); returns (stats, peak indices, peak heights)."""
+        if not self.n_tls:
+            raise ValueError("no GTLS requests in the batch")
+        tt = self.tls_table
+        off = torch.from_numpy(tt["out"].astype(np.int64)).to(self.device)
+        n = torch.from_numpy(tt["nt"].astype(np.int32)).to(self.device)
+        return api.peakstat(self.tls_outs[0], off, n, 1, int(tt["nt"].max()), mpd, ntop, k, stream)
+
     # -- results ------------------------------------------------------------------------
     def bls_result(self, k: int):
         """(blsp, phase1, phase2) of BLS request k as numpy arrays (synchronises)."""

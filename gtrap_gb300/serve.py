@@ -15,7 +15,9 @@ in device-resident arenas sized by an HBM budget, and runs in steps.  A step
    ``gtrap_gtls_run``), so tiles of many requests run side by side and a long request spans
    several steps while newer requests join, and
 4. when a request's last tile has run, copies its outputs to the host on a second copy stream
-   and frees its memory.
+   and frees its memory.  With ``tls_peaks`` a GTLS request returns only its peak statistics
+   (``gtrap_peakstat``, computed on the device in the step that finishes it) instead of its
+   five output series.
 
 The host prepares step k+1 while step k runs (at most ``depth`` steps in flight).  Each
 request's result is bit-identical to a solo run: the kernels treat every curve and tile
@@ -82,7 +84,8 @@ class Result:
     arrival: float
     admitted: float
     done: float
-    outputs: tuple   # bls: (blsp, phase1, phase2); tls: (sn, w, t0, l, hmax)
+    outputs: tuple   # bls: (blsp, phase1, phase2); tls: (sn, w, t0, l, hmax), or with
+    #                  tls_peaks (PEAK_STATS record, peak indices, peak heights)
     evals: int
 
     @property
@@ -154,6 +157,7 @@ class _Live:
     last_step: int = -1
     result: tuple = ()
     d2h_event: object = None
+    pk_slot: int = -1      # row in its finishing step's peak-statistics buffers
 
 
 @dataclass
@@ -161,6 +165,7 @@ class _Step:
     index: int
     event: object
     finishing: list = field(default_factory=list)
+    peaks: tuple = ()      # (stats, idx, val) device buffers of the GTLS requests it finishes
 
 
 class TransitServer:
@@ -174,7 +179,7 @@ class TransitServer:
     def __init__(self, bls: BlsSpec = BlsSpec(), tls: TlsSpec = TlsSpec(), detrend_r: int = 24,
                  hbm_budget: float = 100e9, sample_share: float = 0.8, bls_tiles: int | None = None,
                  tls_tiles: int | None = None, F: int | None = None, max_requests: int = 1 << 16,
-                 depth: int = 2, device=None):
+                 depth: int = 2, tls_peaks: dict | None = None, device=None):
         require_cuda()
         self.dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         self.bls_spec, self.tls_spec = bls, tls
@@ -184,6 +189,7 @@ class TransitServer:
         self.bls_tiles = int(bls_tiles) if bls_tiles else sms * 2 * 8
         self.tls_tiles = int(tls_tiles) if tls_tiles else sms * 64
         self.depth = max(1, int(depth))
+        self.tls_peaks = None if tls_peaks is None else dict(mpd=10, ntop=4, k=8) | dict(tls_peaks)
         budget = int(hbm_budget)
         self.sample_cap = int(budget * sample_share) // SAMPLE_BYTES // ALIGN * ALIGN
         self.out_cap = int(budget * (1.0 - sample_share)) // OUTPUT_BYTES // ALIGN * ALIGN
@@ -405,9 +411,19 @@ class TransitServer:
                 N.call("gtrap_gtls_run", as_ptr(self.tls_table), p_tsg, p_tcum, len(tls_segs[0]),
                        as_ptr(self.t), as_ptr(self.resid), ts.nw, ts.nl, self.max_tls_nsc, ts.mode,
                        ts.flags, 0, as_ptr(self.counters[1:2]), *[as_ptr(a) for a in self.o], h)
+            fin_tls = [lv for lv in self.live_tls if lv.next_tile >= lv.tiles and lv.last_step < 0]
+            pk = ()
+            if self.tls_peaks and fin_tls:
+                for j, lv in enumerate(fin_tls):
+                    lv.pk_slot = j
+                po = torch.tensor([lv.ooff for lv in fin_tls], dtype=torch.int64).pin_memory().to(self.dev, non_blocking=True)
+                pn = torch.tensor([lv.req.n for lv in fin_tls], dtype=torch.int32).pin_memory().to(self.dev, non_blocking=True)
+                c = self.tls_peaks
+                pk = api.peakstat(self.o[0], po, pn, 1, max(lv.req.n for lv in fin_tls), c["mpd"],
+                                  c["ntop"], c["k"], stream=st)
             ev = torch.cuda.Event()
             ev.record(st)
-        step = _Step(si, ev)
+        step = _Step(si, ev, peaks=pk)
         step._keep = devbuf  # staging stays alive until the step has run
         for live in (self.live_bls, self.live_tls):
             for lv in live:
@@ -427,11 +443,18 @@ class TransitServer:
             with torch.cuda.stream(self.d2h):
                 for lv in step.finishing:
                     m, o = lv.req.outputs, lv.ooff
-                    k = 3 if lv.req.kind == "bls" else 5
+                    if lv.req.kind == "tls" and lv.pk_slot >= 0:
+                        st_, idx, val = step.peaks
+                        for t_ in step.peaks:  # keep the buffers until the copies have run
+                            t_.record_stream(self.d2h)
+                        rs = api.PEAK_STATS.itemsize
+                        srcs = (st_[lv.pk_slot * rs:(lv.pk_slot + 1) * rs], idx[lv.pk_slot], val[lv.pk_slot])
+                    else:
+                        srcs = [self.o[j][o:o + m] for j in range(3 if lv.req.kind == "bls" else 5)]
                     outs = []
-                    for j in range(k):
-                        h = torch.empty(m, dtype=torch.float32, pin_memory=True)
-                        h.copy_(self.o[j][o:o + m], non_blocking=True)
+                    for src in srcs:
+                        h = torch.empty(src.numel(), dtype=src.dtype, pin_memory=True)
+                        h.copy_(src, non_blocking=True)
                         outs.append(h)
                     lv.result = tuple(outs)
                     ev = torch.cuda.Event()
@@ -446,6 +469,9 @@ class TransitServer:
                 res = lv.result
                 if lv.req.kind == "bls":
                     res = (res[0].numpy(), res[1].numpy().view(np.int32), res[2].numpy().view(np.int32))
+                elif lv.pk_slot >= 0:
+                    res = (np.frombuffer(res[0].numpy().tobytes(), api.PEAK_STATS)[0], res[1].numpy(),
+                           res[2].numpy())
                 else:
                     res = tuple(a.numpy() for a in res)
                 self.samples.free(lv.soff, lv.req.n)

@@ -243,6 +243,36 @@ int gtrap_gtls_run(const gtrap_tls_curve *curves, const gtrap_tls_segment *segs,
                    float *tlshmax, gtrap_stream_t stream);
 
 /* ---------------------------------------------------------------------------
+ * Peak statistics of S/N series on the device.  Replaces the host epilogue of the GTLS
+ * drivers (gtrap/gtls.py:245-273) with detect_peaks (gtrap/detect_peaks.py:104-143, edge
+ * 'rising', threshold 0, no minimum height): per curve q, the series x[e] =
+ * sn[off[q] + e*stride], e < n[q] (an [nt, nq] image: off[q] = q, stride = nq; packed GTLS
+ * outputs: the curve's output offset, stride 1).  Fills stats[q] and the k highest peaks
+ * (height desc, index asc) in peak_idx/peak_val[q*k .. q*k+k) (UINT32_MAX / 0 past npeaks).
+ * Peaks on equal heights are ranked by index where detect_peaks' unstable sort leaves the
+ * order open.  max_n: longest series (at most gtrap_peakstat_max_samples()).
+ * ------------------------------------------------------------------------- */
+typedef struct {
+  float maxsn;      /* max(x) */
+  uint32_t argmax;  /* first index of the maximum */
+  uint32_t lent;    /* count of x > 0 */
+  uint32_t npeaks;  /* peaks after the +-mpd suppression */
+  double median;    /* median(x), mean of the two middle values for even n */
+  double std;       /* population std of the x > 0 */
+  double far;       /* (maxsn - median) / std */
+  double pssn;      /* (top peak - medc) / stdc; +inf when npeaks <= ntop */
+  double diff;      /* (ntop-th peak - median) / std; 0 when npeaks <= ntop */
+  double medc;      /* median of the peaks after the ntop highest */
+  double stdc;      /* population std of the peaks after the ntop highest */
+} gtrap_peak_stats; /* 72 bytes */
+
+size_t gtrap_peakstat_max_samples(void);
+int gtrap_peakstat(const float *sn, const uint64_t *off, const uint32_t *n, uint64_t stride,
+                   uint32_t ncurves, uint32_t max_n, uint32_t mpd, uint32_t ntop, uint32_t k,
+                   gtrap_peak_stats *stats, uint32_t *peak_idx, float *peak_val,
+                   gtrap_stream_t stream);
+
+/* ---------------------------------------------------------------------------
  * Measurement helpers (used by the benchmark to report roofline fractions).
  * ------------------------------------------------------------------------- */
 /* FP32 issue peak: launches a register-resident FMA-chain kernel; *flops receives the

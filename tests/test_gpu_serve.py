@@ -90,3 +90,23 @@ def test_plain_server_and_trace(solo):
         _eq(r.outputs, ref[r.rid])
     summ = S.latency_summary(res)
     assert summ["p99_ms"] >= summ["p50_ms"] > 0
+
+
+def test_server_returns_tls_peaks(solo):
+    """With tls_peaks, a GTLS request returns its peak statistics, equal to those of its full
+    S/N series from the solo run."""
+    from oracle import peaks as P
+    reqs, ref = solo
+    srv = _server(tls_peaks=dict(mpd=10, ntop=4, k=5))
+    rids = [srv.submit(r) for r in reqs]
+    res = {r.rid: r for r in srv.run_until_idle()}
+    for k, rid in enumerate(rids):
+        if reqs[k].kind == "bls":
+            _eq(res[rid].outputs, ref[k])
+            continue
+        rec, idx, val = res[rid].outputs
+        want = P.peakstat(ref[k][0], 10, 4)
+        assert rec["npeaks"] == want["npeaks"] and rec["argmax"] == want["argmax"]
+        m = min(5, want["npeaks"])
+        np.testing.assert_array_equal(idx[:m], want["peaks"][:m])
+        assert rec["median"] == want["median"]
