@@ -243,6 +243,26 @@ int gtrap_gtls_run(const gtrap_tls_curve *curves, const gtrap_tls_segment *segs,
                    float *tlshmax, gtrap_stream_t stream);
 
 /* ---------------------------------------------------------------------------
+ * Light-curve packer.  Replaces the array part of the loaders (throw_kepintarray,
+ * gtrap/read_keplerlc.py:123-146, and the zig-zag fill and ntrue of load_keplc,
+ * :36-47; throw_tessintarray and load_tesstic, gtrap/read_tesstic.py:11-85, 114-146).
+ * Curve q's raw samples are cno/t/flux[soff[q] .. soff[q] + m[q]) (device arrays; cno int64
+ * cadence numbers, t double times, flux float with NaN = missing).  Row j of its destination
+ * column is lc/tu[doff[q] + j*dstride], j < dn[q] ([n, nq] image: doff[q] = q, dstride = nq,
+ * dn[q] = n; packed arrays: dstride = 1).  A sample goes to row cno - cno[soff[q]] with flux
+ * and time t - t[soff[q]] (rel_time != 0) or t, rounded once to float; rows without a sample
+ * hold fill_flux / fill_time (the loaders use 1.002 and -1000).  Then ntrue[q] = rows whose
+ * time is not negative, and rows whose time is negative get the column's minimum (even j)
+ * or maximum (odd j) flux.  t0[q] receives the subtracted time.  A sample whose row falls
+ * outside [0, dn[q]) is not written and sets status[q] = 1 (the reference exits).
+ * ------------------------------------------------------------------------- */
+int gtrap_pack_curves(const int64_t *cno, const double *t, const float *flux, const uint64_t *soff,
+                      const uint32_t *m, uint32_t ncurves, uint32_t max_m, float *lc, float *tu,
+                      const uint64_t *doff, const uint32_t *dn, uint64_t dstride, uint32_t max_dn,
+                      float fill_flux, float fill_time, int32_t rel_time, uint32_t *ntrue,
+                      double *t0, int32_t *status, gtrap_stream_t stream);
+
+/* ---------------------------------------------------------------------------
  * Peak statistics of S/N series on the device.  Replaces the host epilogue of the GTLS
  * drivers (gtrap/gtls.py:245-273) with detect_peaks (gtrap/detect_peaks.py:104-143, edge
  * 'rising', threshold 0, no minimum height): per curve q, the series x[e] =

@@ -254,3 +254,14 @@ def test_detect_peaks_restatement_matches_reference_golden():
             mine = [st["maxsn"], st["argmax"], st["std"], st["median"], st["far"], st["npeaks"],
                     st["pssn"], st["diff"], st["medc"], st["stdc"]]
             np.testing.assert_allclose(mine, ref, rtol=2e-6, atol=1e-6)
+
+
+def test_packer_restatement_matches_reference_golden():
+    """oracle.packer against the reference's throw_kepintarray + zig-zag fill + ntrue."""
+    from oracle import packer
+    g = np.load(GOLDEN / "packer_golden.npz")
+    for k in range(12):
+        lc, tu, ntrue, t0 = packer.pack_column(g["cno%d" % k], g["t%d" % k], g["f%d" % k], int(g["n%d" % k]))
+        np.testing.assert_array_equal(lc, g["lc%d" % k])
+        np.testing.assert_array_equal(tu, g["tu%d" % k])
+        assert ntrue == int(g["ntrue%d" % k])
