@@ -60,6 +60,8 @@ _SIGNATURES = {
                              f32, f32, i32, u32, vp]),
     "gtrap_pack_curves": (C.c_int, [vp, vp, vp, vp, vp, u32, u32, vp, vp, vp, vp, u64, u32, f32, f32,
                                     i32, vp, vp, vp, vp]),
+    "gtrap_picktrap": (C.c_int, [vp, vp, vp, vp, u64, vp, vp, vp, u32, f64, f64, i32, i32, i32, vp, vp,
+                                 vp, vp, vp]),
     "gtrap_peakstat_max_samples": (sz, []),
     "gtrap_peakstat": (C.c_int, [vp, vp, vp, u64, u32, u32, u32, u32, u32, vp, vp, vp, vp]),
     "gtrap_probe_fp32_peak": (C.c_int, [vp, u32, C.POINTER(C.c_double), vp]),

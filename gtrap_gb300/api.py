@@ -250,3 +250,39 @@ def tls_peakstat(tlssn: torch.Tensor, mpd: int = 10, ntop: int = 4, k: int = 8, 
     off = torch.arange(nq, dtype=torch.int64, device=tlssn.device)
     n = torch.full((nq,), nt, dtype=torch.int32, device=tlssn.device)
     return peakstat(tlssn, off, n, nq, nt, mpd, ntop, k, stream)
+
+
+def picktrap(lc: torch.Tensor, tu: torch.Tensor, curve, T0, W, *, off=None, n=None, stride=None,
+             alpha=2.0, daytopix=48.0, contcrit=84, nx=128, stream=None):
+    """Cleaned, W-normalised windows around candidates (pick_Wnormalized_cleaned_lc_direct,
+    gtrap/picktrap.py:27-172) on the device.
+
+    ``lc``/``tu`` are an ``[n, nq]`` image (default) or flat packed arrays with per-curve
+    ``off``/``n`` (and ``stride`` 1); ``curve``, ``T0``, ``W`` give each candidate's curve,
+    time and width.  Returns (wnc [ncand, nx] float64, gapx [ncand, nx] float64, prec [ncand],
+    status [ncand]) as device tensors."""
+    require_cuda()
+    lc = _f32(lc, "lc")
+    tu = _f32(tu, "tu")
+    dev = lc.device
+    if off is None:
+        nt, nq = lc.shape
+        off = torch.arange(nq, dtype=torch.int64, device=dev)
+        n = torch.full((nq,), nt, dtype=torch.int32, device=dev)
+        stride = nq
+    cq = torch.as_tensor(curve, dtype=torch.int32).to(dev)
+    t0 = torch.as_tensor(T0, dtype=torch.float32).to(dev)
+    w = torch.as_tensor(W, dtype=torch.float32).to(dev)
+    nc = int(cq.numel())
+    wmax = float(w.max()) if nc else 0.0
+    wid = int(_np.float32(alpha) * _np.float32(wmax) * _np.float32(daytopix))
+    max_get = max(2, 2 * int(1.11 * alpha * wid) + 2)
+    wnc = torch.empty((nc, nx), dtype=torch.float64, device=dev)
+    gapx = torch.empty((nc, nx), dtype=torch.float64, device=dev)
+    prec = torch.empty(nc, dtype=torch.int32, device=dev)
+    status = torch.empty(nc, dtype=torch.int32, device=dev)
+    N.call("gtrap_picktrap", as_ptr(lc), as_ptr(tu), as_ptr(off), as_ptr(n), int(stride),
+           as_ptr(cq), as_ptr(t0), as_ptr(w), nc, float(alpha), float(daytopix), int(contcrit),
+           int(nx), int(max_get), as_ptr(wnc), as_ptr(gapx), as_ptr(prec), as_ptr(status),
+           stream_handle(stream))
+    return wnc, gapx, prec, status

@@ -263,6 +263,22 @@ int gtrap_pack_curves(const int64_t *cno, const double *t, const float *flux, co
                       double *t0, int32_t *status, gtrap_stream_t stream);
 
 /* ---------------------------------------------------------------------------
+ * Candidate windows for the classifier.  Replaces pick_Wnormalized_cleaned_lc_direct
+ * (gtrap/picktrap.py:27-172) for a batch of candidates: candidate c lies on curve curve[c]
+ * (series lc/tu[off[q] + e*stride], e < n[q]) at time T0[c] with width W[c] (days).  Writes
+ * the cleaned, z-normalised window interpolated onto nx points to wnc[c*nx ..], the
+ * interpolated gap flags to gapx[c*nx ..] (both double), the pre-classifier flag prec[c], and
+ * status[c] (0 ok; 1 no positive time at or after T0; 2 a gap with no positive neighbour
+ * anywhere, left uncleaned where the reference loops forever; 3 window longer than max_get
+ * samples).  The reference's defaults are alpha 2, daytopix 48, contcrit 84, nx 128.
+ * ------------------------------------------------------------------------- */
+int gtrap_picktrap(const float *lc, const float *tu, const uint64_t *off, const uint32_t *n,
+                   uint64_t stride, const uint32_t *curve, const float *T0, const float *W,
+                   uint32_t ncand, double alpha, double daytopix, int32_t contcrit, int32_t nx,
+                   int32_t max_get, double *wnc, double *gapx, int32_t *prec, int32_t *status,
+                   gtrap_stream_t stream);
+
+/* ---------------------------------------------------------------------------
  * Peak statistics of S/N series on the device.  Replaces the host epilogue of the GTLS
  * drivers (gtrap/gtls.py:245-273) with detect_peaks (gtrap/detect_peaks.py:104-143, edge
  * 'rising', threshold 0, no minimum height): per curve q, the series x[e] =

@@ -265,3 +265,15 @@ def test_packer_restatement_matches_reference_golden():
         np.testing.assert_array_equal(lc, g["lc%d" % k])
         np.testing.assert_array_equal(tu, g["tu%d" % k])
         assert ntrue == int(g["ntrue%d" % k])
+
+
+def test_picktrap_restatement_matches_reference_golden():
+    """oracle.picktrap against the reference's pick_Wnormalized_cleaned_lc_direct."""
+    from oracle import picktrap
+    g = np.load(GOLDEN / "picktrap_golden.npz")
+    for m in range(int(g["count"])):
+        k, T0, W = g["c%d" % m]
+        w, tx, gx, prec, status = picktrap.pick(g["lc%d" % int(k)], g["tu%d" % int(k)], np.float32(T0), np.float32(W))
+        np.testing.assert_allclose(w, g["w%d" % m], rtol=1e-12, atol=1e-12)
+        np.testing.assert_allclose(gx, g["g%d" % m], rtol=1e-12, atol=1e-12)
+        assert bool(prec) == bool(g["p%d" % m]) and status == 0
