@@ -106,6 +106,22 @@ def _profile(name):
         return None
 
 
+def smem_atomic_peak(dev):
+    """Shared-memory atomic peak in fold updates per second (two 32-bit adds per update)."""
+    import torch
+    from gtrap_gb300 import api
+    stream = torch.cuda.current_stream(dev)
+    _, upd = api.smem_atomic_peak_probe()
+    torch.cuda.synchronize(dev)
+    ps, pe = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ps.record(stream)
+    for _ in range(3):
+        api.smem_atomic_peak_probe()
+    pe.record(stream)
+    torch.cuda.synchronize(dev)
+    return upd * 3 / (ps.elapsed_time(pe) / 1e3)
+
+
 def fp32_peak_tflops(dev):
     """FP32 FMA issue peak of this GPU, measured live (MEASURED_PEAKS.json has no FP32 figure)."""
     import torch
@@ -584,6 +600,13 @@ def run_ragged(args, rank, world, local_rank):
     if prof and prof.get("dram_bytes_per_sample_frequency"):
         unit_work = float(sum(int(r["n"]) * int(r["nf"]) for r in bat.bls_table))
         traffic = prof["dram_bytes_per_sample_frequency"] * unit_work
+    # second roofline leg: the fold's sample updates against the shared-atomic peak
+    dev_table = np.frombuffer(bat.bls_curves.cpu().numpy().tobytes(), B.BLS_CURVE)
+    updates = float((dev_table["nv"].astype(np.float64) * dev_table["nf"]).sum())
+    apeak = smem_atomic_peak(dev)
+    fold_leg = {"bound": "smem_atomics", "achieved": updates / (bls_ms / 1e3), "peak": apeak,
+                "unit": "sample updates/s", "frac": updates / (bls_ms / 1e3) / apeak,
+                "peak_source": "live probe: two 32-bit shared atomics per update on random bins"}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+i64", "data": "synthetic",
@@ -593,7 +616,7 @@ def run_ragged(args, rank, world, local_rank):
                          "kernel": "bls_queue_kernel (persistent BLS fold + scan)", "kernel_ms": bls_ms,
                          "kernel_share": bls_ms / ms,
                          "peak_source": "live FP32 FMA-chain probe on this GPU (MEASURED_PEAKS.json has no FP32 figure)",
-                         "flop_per_eval": flop_per_eval},
+                         "flop_per_eval": flop_per_eval, "fold": fold_leg},
             "gpu_launches": 6 * args.steps,
             "clocks": clk}
     if plain:

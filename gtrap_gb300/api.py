@@ -203,6 +203,14 @@ def gtls(lc, tu, nt, nw, nl, nsc, wmax, dw, deltat, *, mode=0, t0min=0.0, dt=0.0
     return out
 
 
+def smem_atomic_peak_probe(iters=2048, stream=None):
+    """Launch the shared-memory atomic probe; returns (sink tensor, update count)."""
+    sink = torch.empty(1 << 16, dtype=torch.int32, device="cuda")
+    upd = C.c_double(0.0)
+    N.call("gtrap_probe_smem_atomic_peak", as_ptr(sink), int(iters), C.byref(upd), stream_handle(stream))
+    return sink, upd.value
+
+
 def fp32_peak_probe(iters=4096, stream=None):
     """Launch the FP32 FMA probe; returns (sink tensor, flop count)."""
     sink = torch.empty(1 << 20, dtype=torch.float32, device="cuda")

@@ -131,9 +131,41 @@ __global__ void __launch_bounds__(256) fp32_probe_kernel(float *sink, uint32_t i
   float s = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
   if (s == 1234.5f) sink[blockIdx.x * blockDim.x + threadIdx.x] = s;  // never true; keeps the work
 }
+// Shared-memory atomic issue peak for the BLS fold's pattern: per update two 32-bit atomic
+// adds to random bins of one of four 2048-bin histograms (64 KB per block, two blocks per SM).
+constexpr int kAtomBins = 2048, kAtomHist = 4;
+__global__ void __launch_bounds__(512) atomic_probe_kernel(unsigned *sink, uint32_t iters) {
+  extern __shared__ unsigned hist[];
+  for (int i = threadIdx.x; i < 2 * kAtomBins * kAtomHist; i += blockDim.x) hist[i] = 0;
+  __syncthreads();
+  unsigned long long x = 0x9E3779B97F4A7C15ull * (blockIdx.x * blockDim.x + threadIdx.x + 1);
+  for (uint32_t it = 0; it < iters; ++it) {
+    x = x * 6364136223846793005ull + 1442695040888963407ull;
+    unsigned long long ph = x;
+#pragma unroll
+    for (int f = 0; f < kAtomHist; ++f) {
+      const unsigned b = (unsigned)(ph >> 53) & (kAtomBins - 1);
+      atomicAdd(hist + f * 2 * kAtomBins + 2 * b, (unsigned)x);
+      atomicAdd(hist + f * 2 * kAtomBins + 2 * b + 1, 1u);
+      ph += 0x9E3779B97F4A7C15ull;
+    }
+  }
+  __syncthreads();
+  if (hist[threadIdx.x] == 0x12345678u) sink[blockIdx.x] = 1u;  // keeps the work
+}
 }  // namespace
 
 extern "C" {
+
+int gtrap_probe_smem_atomic_peak(unsigned *sink, uint32_t iters, double *updates, gtrap_stream_t stream) {
+  if (!sink || iters == 0) return gtrap::fail(GTRAP_ERR_INVALID_ARG, "probe: bad arguments");
+  const size_t smem = 2 * kAtomBins * kAtomHist * sizeof(unsigned);
+  GTRAP_TRY(gtrap::ensure_smem((const void *)atomic_probe_kernel, smem, "atomic_probe"));
+  const int blocks = gtrap::sm_count() * 2;
+  atomic_probe_kernel<<<blocks, 512, smem, stream>>>(sink, iters);
+  if (updates) *updates = (double)blocks * 512.0 * (double)iters * kAtomHist;
+  return gtrap::check_launch("atomic_probe_kernel");
+}
 
 const char *gtrap_last_error(void) { return gtrap::g_last_error; }
 
