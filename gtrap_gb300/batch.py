@@ -10,7 +10,7 @@ float32 time and flux arrays (curve q = samples ``[off[q], off[q] + n[q])``).  O
 3. quantisation and exact phase encoding of the BLS samples (``gtrap_bls_prepare``),
 4. one persistent BLS launch that pops (curve, frequency tile) items from a device work
    queue (``gtrap_bls_run``; the geebls statistic, include/geebls.h:35-165), and
-5. one persistent GTLS launch over (curve, 32-epoch tile) items (``gtrap_gtls_run``; the
+5. one persistent GTLS launch over (curve, 64-epoch tile) items (``gtrap_gtls_run``; the
    gtls statistic, include/gtls_simple.h:51-404),
 
 so the whole sequence can be captured in a CUDA graph (:meth:`RaggedBatch.capture`) and
@@ -41,7 +41,7 @@ TLS_CURVE = np.dtype([("off", "<u8"), ("out", "<u8"), ("nt", "<i4"), ("nsc", "<i
 SEGMENT = np.dtype([("curve", "<u4"), ("tile0", "<u4")])
 assert BLS_CURVE.itemsize == 56 and TLS_CURVE.itemsize == 40 and SEGMENT.itemsize == 8
 
-TLS_TILE = 32  # epochs per GTLS work item
+TLS_TILE = 64  # epochs per GTLS work item
 
 
 @dataclass(frozen=True)

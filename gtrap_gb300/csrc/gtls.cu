@@ -9,9 +9,10 @@
 // keeps the best S/N = H/sqrt(chi^2/(N-3)) of windows whose fill factor exceeds 0.75.
 // Cost: O(nl * window) per thread, and the CTA has only nw threads.
 //
-// GB300 design: a CTA covers 32 consecutive epochs (one per lane) of one curve; its
-// warps take widths in turn, so the lanes of a warp share W and do the same amount of
-// work.  The union of the 32 scoops is staged once in shared memory (times rounded
+// GB300 design: a CTA covers 64 consecutive epochs of one curve, as two halves of 32 (one
+// epoch per lane); its warps take (half, width) units, so the lanes of a warp share W and do
+// the same amount of work, and each warp pairs wide with narrow widths across the halves so
+// the warps finish together.  The union of the 64 scoops is staged once in shared memory (times rounded
 // through (t + 1000) - 1000 exactly as the reference's scoop gather does), with exact
 // count prefixes and double-float prefix sums of x and x^2.  For each (epoch, width):
 //  * binary searches give the window [tStart, tEnd] (mean), the A..E range and the two
@@ -42,7 +43,9 @@ using gtrap::fail;
 
 constexpr int kWarps = 8;
 constexpr int kTlsThreads = kWarps * 32;
-constexpr int kMaxStage = 7000;  // staged samples: nsc + 31
+constexpr int kTE = 64;          // epochs per tile
+constexpr int kHalves = kTE / 32;
+constexpr int kMaxStage = 7000;  // staged samples: nsc + kTE - 1
 
 // One curve as a tile sees it: sample s at lc[s*stride], epoch e's outputs at [e*ostride].
 struct TlsArgs {
@@ -83,17 +86,17 @@ __device__ __forceinline__ double df_diff_d(float bh, float bl, float ah, float 
   return ((double)bh - (double)ah) + ((double)bl - (double)al);
 }
 
-// 32 consecutive epochs [e0, e0 + 32) of one curve, by the whole block.
+// kTE consecutive epochs [e0, e0 + kTE) of one curve, by the whole block.
 __device__ __forceinline__ void gtls_tile(const TlsArgs &a, const int e0) {
   extern __shared__ __align__(16) float st[];
-  __shared__ float red_sn[kWarps][32], red_l[kWarps][32], red_h[kWarps][32];
-  __shared__ int red_w[kWarps][32];
+  __shared__ float red_sn[kWarps][kTE], red_l[kWarps][kTE], red_h[kWarps][kTE];
+  __shared__ int red_w[kWarps][kTE];
   __shared__ float xref;
 
   const int nsch = a.nsc / 2;
   // staged sample range [base, base + S) in sample indices, clipped to [0, nt)
   const int first = e0 - nsch;
-  const int last = min(e0 + 31, a.nt - 1) - nsch + a.nsc;  // exclusive
+  const int last = min(e0 + kTE - 1, a.nt - 1) - nsch + a.nsc;  // exclusive
   const int base = max(first, 0);
   const int S = max(0, min(last, a.nt) - base);
 
@@ -199,44 +202,55 @@ __device__ __forceinline__ void gtls_tile(const TlsArgs &a, const int e0) {
   }
   __syncthreads();
 
-  // ---- per (epoch, width)
+  // ---- per (epoch, width).  Units (half, width): half h covers epochs e0 + 32h + lane, and
+  // the warps take the units (0, 0 .. nw-1), (1, nw-1 .. 0) round robin, so that the widths
+  // of each warp add up to about the same work (the walks of a unit cost about W).  Each unit
+  // merges its best template into the warp's row of the reduction arrays.
   const float xr = xref;
-  const int e = e0 + lane;
-  const bool eok = e < a.nt;
-  const float ef = (float)e;
-  const float dte = __fmul_rn(a.deltat, ef);
   const bool t_fma = a.t_fma;
-  auto tt = [&](int s) -> float {
-    const float v = tq[s];
-    return t_fma ? __fmaf_rn(-a.deltat, ef, v) : __fsub_rn(v, dte);
-  };
-  // scoop of epoch e in staged indices; c0 is scoop slot 0 (negative before the series)
-  const int c0 = e - nsch - base;
-  const int lo = max(e - nsch, 0) - base;
-  const int hi = min(e - nsch + a.nsc, a.nt) - base;
-  auto ub = [&](float tau) -> int {  // first s in [lo, hi) with tt(s) > tau
-    int x0 = lo, x1 = hi;
-    while (x0 < x1) {
-      const int mid = (x0 + x1) >> 1;
-      if (tt(mid) > tau) x1 = mid; else x0 = mid + 1;
-    }
-    return x0;
-  };
-  auto lb = [&](float tau) -> int {  // first s in [lo, hi) with tt(s) >= tau
-    int x0 = lo, x1 = hi;
-    while (x0 < x1) {
-      const int mid = (x0 + x1) >> 1;
-      if (tt(mid) >= tau) x1 = mid; else x0 = mid + 1;
-    }
-    return x0;
-  };
-
-  float best_sn = 0.0f, best_l = 0.0f, best_h = 0.0f;
-  int best_w = INT_MAX;
   const int nl = a.nl;
   const float crit_w = a.deltat;
-
-  for (int wi = warp; wi < a.nw && eok && lo < hi; wi += kWarps) {
+#pragma unroll
+  for (int h = 0; h < kHalves; ++h) {
+    red_sn[warp][32 * h + lane] = 0.0f;
+    red_w[warp][32 * h + lane] = INT_MAX;
+    red_l[warp][32 * h + lane] = 0.0f;
+    red_h[warp][32 * h + lane] = 0.0f;
+  }
+  for (int u = warp; u < kHalves * a.nw; u += kWarps) {
+    const int half = u / a.nw;
+    const int wi = (half & 1) ? (half + 1) * a.nw - 1 - u : u - half * a.nw;
+    const int e = e0 + 32 * half + lane;
+    const bool eok = e < a.nt;
+    const float ef = (float)e;
+    const float dte = __fmul_rn(a.deltat, ef);
+    auto tt = [&](int s) -> float {
+      const float v = tq[s];
+      return t_fma ? __fmaf_rn(-a.deltat, ef, v) : __fsub_rn(v, dte);
+    };
+    // scoop of epoch e in staged indices; c0 is scoop slot 0 (negative before the series)
+    const int c0 = e - nsch - base;
+    const int lo = max(e - nsch, 0) - base;
+    const int hi = min(e - nsch + a.nsc, a.nt) - base;
+    auto ub = [&](float tau) -> int {  // first s in [lo, hi) with tt(s) > tau
+      int x0 = lo, x1 = hi;
+      while (x0 < x1) {
+        const int mid = (x0 + x1) >> 1;
+        if (tt(mid) > tau) x1 = mid; else x0 = mid + 1;
+      }
+      return x0;
+    };
+    auto lb = [&](float tau) -> int {  // first s in [lo, hi) with tt(s) >= tau
+      int x0 = lo, x1 = hi;
+      while (x0 < x1) {
+        const int mid = (x0 + x1) >> 1;
+        if (tt(mid) >= tau) x1 = mid; else x0 = mid + 1;
+      }
+      return x0;
+    };
+    float best_sn = 0.0f, best_l = 0.0f, best_h = 0.0f;
+    int best_w = INT_MAX;
+    if (eok && lo < hi) do {
     const float wf = (float)wi;
     const float W = a.w_fma ? __fmaf_rn(-a.dw, wf, a.wmax) : __fsub_rn(a.wmax, __fmul_rn(a.dw, wf));
     if (!(W > 0.0f)) continue;
@@ -337,30 +351,36 @@ __device__ __forceinline__ void gtls_tile(const TlsArgs &a, const int e0) {
         }
       }
     }
-  }
-
-  red_sn[warp][lane] = best_sn;
-  red_w[warp][lane] = best_w;
-  red_l[warp][lane] = best_l;
-  red_h[warp][lane] = best_h;
-  __syncthreads();
-  if (warp == 0 && eok) {
-    for (int k = 1; k < kWarps; ++k) {
-      const float s = red_sn[k][lane];
-      const int w = red_w[k][lane];
-      if (s > best_sn || (s == best_sn && w < best_w)) {
-        best_sn = s; best_w = w; best_l = red_l[k][lane]; best_h = red_h[k][lane];
-      }
+    } while (0);
+    const int r = 32 * half + lane;
+    if (best_sn > red_sn[warp][r] || (best_sn == red_sn[warp][r] && best_w < red_w[warp][r])) {
+      red_sn[warp][r] = best_sn; red_w[warp][r] = best_w; red_l[warp][r] = best_l; red_h[warp][r] = best_h;
     }
-    if (best_w == INT_MAX || !(best_sn > 0.0f)) { best_sn = 0.0f; best_w = 0; best_l = 0.0f; best_h = 0.0f; }
-    const float wf = (float)best_w;
-    const float W = a.w_fma ? __fmaf_rn(-a.dw, wf, a.wmax) : __fsub_rn(a.wmax, __fmul_rn(a.dw, wf));
-    const size_t k = (size_t)e * a.ostride;
-    a.sn[k] = best_sn;
-    a.t0[k] = dte;
-    a.w[k] = W;
-    a.l[k] = best_l;
-    a.h[k] = best_h;
+  }
+  __syncthreads();
+  if (warp < kHalves) {
+    const int r = 32 * warp + lane;
+    const int e = e0 + r;
+    if (e < a.nt) {
+      float best_sn = 0.0f, best_l = 0.0f, best_h = 0.0f;
+      int best_w = INT_MAX;
+      for (int k = 0; k < kWarps; ++k) {
+        const float s = red_sn[k][r];
+        const int w = red_w[k][r];
+        if (s > best_sn || (s == best_sn && w < best_w)) {
+          best_sn = s; best_w = w; best_l = red_l[k][r]; best_h = red_h[k][r];
+        }
+      }
+      if (best_w == INT_MAX || !(best_sn > 0.0f)) { best_sn = 0.0f; best_w = 0; best_l = 0.0f; best_h = 0.0f; }
+      const float wf = (float)best_w;
+      const float W = a.w_fma ? __fmaf_rn(-a.dw, wf, a.wmax) : __fsub_rn(a.wmax, __fmul_rn(a.dw, wf));
+      const size_t k = (size_t)e * a.ostride;
+      a.sn[k] = best_sn;
+      a.t0[k] = __fmul_rn(a.deltat, (float)e);
+      a.w[k] = W;
+      a.l[k] = best_l;
+      a.h[k] = best_h;
+    }
   }
 }
 
@@ -375,7 +395,7 @@ __global__ void __launch_bounds__(kTlsThreads, GTRAP_TLS_MINB) gtls_kernel(const
     v.sn += q; v.w += q; v.t0 += q; v.l += q; v.h += q;
   }
   __syncthreads();
-  gtls_tile(v, tile * 32);
+  gtls_tile(v, tile * kTE);
 }
 
 // Persistent launch over a device work queue of (curve, epoch tile) items of a packed batch.
@@ -407,7 +427,7 @@ __global__ void __launch_bounds__(kTlsThreads, GTRAP_TLS_MINB) gtls_queue_kernel
     }
     const gtrap_tls_segment sg = qa.segs[lo];
     const gtrap_tls_curve c = qa.curves[sg.curve];
-    const int e0 = (int)(sg.tile0 + (it - qa.cum[lo])) * 32;
+    const int e0 = (int)(sg.tile0 + (it - qa.cum[lo])) * kTE;
     if (e0 >= c.nt) continue;  // uniform across the block
     if (threadIdx.x == 0) {
       v.lc = qa.x + c.off; v.tu = qa.t + c.off;
@@ -423,7 +443,7 @@ __global__ void __launch_bounds__(kTlsThreads, GTRAP_TLS_MINB) gtls_queue_kernel
 }
 
 size_t tls_smem(int nsc) {
-  const int S = nsc + 31;
+  const int S = nsc + kTE - 1;
   return (size_t)S * 8 + (size_t)(S + 1) * 20 + 64;
 }
 
@@ -442,11 +462,11 @@ int gtrap_gtls(float *tlssn, float *tlsw, float *tlst0, float *tlsl, float *tlsh
     return fail(GTRAP_ERR_INVALID_ARG, "gtls: null pointer");
   if (nw < 1 || nw > 1024) return fail(GTRAP_ERR_INVALID_ARG, "gtls: nw=%d must be in [1, 1024]", nw);
   if (nl < 1 || nl > 4096) return fail(GTRAP_ERR_INVALID_ARG, "gtls: nl=%d must be in [1, 4096]", nl);
-  if (nsc < 1 || nsc + 31 > kMaxStage)
-    return fail(GTRAP_ERR_INVALID_ARG, "gtls: nsc=%d must be in [1, %d]", nsc, kMaxStage - 31);
+  if (nsc < 1 || nsc + kTE - 1 > kMaxStage)
+    return fail(GTRAP_ERR_INVALID_ARG, "gtls: nsc=%d must be in [1, %d]", nsc, kMaxStage - kTE + 1);
   if (mode != 0 && mode != 1) return fail(GTRAP_ERR_INVALID_ARG, "gtls: mode must be 0 or 1");
   if (!(deltat > 0.0f)) return fail(GTRAP_ERR_INVALID_ARG, "gtls: deltat must be positive");
-  const long long tiles = ((long long)nt + 31) / 32;
+  const long long tiles = ((long long)nt + kTE - 1) / kTE;
   if (tiles * nq >= (1LL << 31)) return fail(GTRAP_ERR_INVALID_ARG, "gtls: grid too large");
   const size_t smem = tls_smem(nsc);
   GTRAP_TRY(gtrap::ensure_smem((const void *)gtls_kernel, smem, "gtls"));
@@ -473,8 +493,8 @@ int gtrap_gtls_run(const gtrap_tls_curve *curves, const gtrap_tls_segment *segs,
     return fail(GTRAP_ERR_INVALID_ARG, "gtls_run: null pointer");
   if (nw < 1 || nw > 1024) return fail(GTRAP_ERR_INVALID_ARG, "gtls_run: nw=%d must be in [1, 1024]", nw);
   if (nl < 1 || nl > 4096) return fail(GTRAP_ERR_INVALID_ARG, "gtls_run: nl=%d must be in [1, 4096]", nl);
-  if (max_nsc < 1 || max_nsc + 31 > kMaxStage)
-    return fail(GTRAP_ERR_INVALID_ARG, "gtls_run: max_nsc=%d must be in [1, %d]", max_nsc, kMaxStage - 31);
+  if (max_nsc < 1 || max_nsc + kTE - 1 > kMaxStage)
+    return fail(GTRAP_ERR_INVALID_ARG, "gtls_run: max_nsc=%d must be in [1, %d]", max_nsc, kMaxStage - kTE + 1);
   if (mode != 0 && mode != 1) return fail(GTRAP_ERR_INVALID_ARG, "gtls_run: mode must be 0 or 1");
   const size_t smem = tls_smem(max_nsc);
   GTRAP_TRY(gtrap::ensure_smem((const void *)gtls_queue_kernel, smem, "gtls_run"));

@@ -10,7 +10,7 @@ in device-resident arenas sized by an HBM budget, and runs in steps.  A step
 2. detrends the newly admitted curves (``gtrap_gfilter_packed``), computes their BLS offsets
    and encodes their BLS samples (``gtrap_bls_offsets``, ``gtrap_bls_prepare``),
 3. runs a bounded slice of work: up to ``bls_tiles`` (curve, frequency tile) items and
-   ``tls_tiles`` (curve, 32-epoch tile) items taken from the oldest in-flight requests, in one
+   ``tls_tiles`` (curve, 64-epoch tile) items taken from the oldest in-flight requests, in one
    persistent BLS launch and one persistent GTLS launch (``gtrap_bls_run``,
    ``gtrap_gtls_run``), so tiles of many requests run side by side and a long request spans
    several steps while newer requests join, and

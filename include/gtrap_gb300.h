@@ -218,9 +218,9 @@ int gtrap_gtls(float *tlssn, float *tlsw, float *tlst0, float *tlsl, float *tlsh
                float deltat, int32_t mode, uint32_t flags, gtrap_stream_t stream);
 
 /* Packed (ragged) GTLS batches, persistent launch over a device work queue of (curve,
- * 32-epoch tile) items.  No counterpart in the reference; the statistic is the one of
+ * 64-epoch tile) items.  No counterpart in the reference; the statistic is the one of
  * gtrap_gtls.  Curve q's sample s is t[off + s], x[off + s]; epoch e's outputs are at
- * [out + e].  Segments and cum as for the BLS batches (tile t = epochs [32t, 32t + 32)).
+ * [out + e].  Segments and cum as for the BLS batches (tile t = epochs [64t, 64t + 64)).
  * max_nsc: largest nsc of the batch (sizes the shared memory). */
 typedef struct {
   uint64_t off;     /* first sample in the packed time and flux arrays */
