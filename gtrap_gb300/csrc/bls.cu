@@ -625,13 +625,13 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
   // published, so the seed is the exact power of a real window (a valid lower bound of the
   // maximum) and may itself be the answer.
   if (kma > kmi) {
-    const int per_f = (nb + 31) & ~31;  // whole warps per frequency
-    for (int idx = tid; idx < (int)nfrem * per_f; idx += kThreads) {
-      const int f = idx / per_f, i = idx - f * per_f;
+    // each thread takes the starts tid, tid + kThreads, ... of one frequency at a time and
+    // keeps its best; one warp argmax and one exact quotient per warp and frequency
+    for (uint32_t f = 0; f < nfrem; ++f) {
       const float2 *P = reinterpret_cast<const float2 *>(sm + (size_t)f * a.region);
       float pa = 0.0f;
-      int kb = 0;
-      if (i < nb) {
+      int ib = 0, kb = 0;
+      for (int i = tid; i < nb; i += kThreads) {
         const float2 Pi = P[swz(i)];
         const float Ni = Nf + Pi.y;
 #pragma unroll
@@ -643,7 +643,7 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
           const float den = kk * (Ni - Pe.y);
           const float s2 = s * s;
           const float q = den > 0.0f ? __fdividef(s2, den) : (den == 0.0f && s2 > 0.0f ? INFINITY : 0.0f);
-          if (kk > kkmi_f && q > pa) { pa = q; kb = k; }
+          if (kk > kkmi_f && q > pa) { pa = q; ib = i; kb = k; }
         }
       }
       // warp argmax of the approximate powers (lowest lane on ties)
@@ -653,9 +653,9 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
       const unsigned who = __ballot_sync(0xffffffffu, pa == wp && wp > 0.0f);
       if (who && lane == __ffs(who) - 1) {
         float pw;
-        if (window_power(P, i, i + kb, pw)) {
+        if (window_power(P, ib, ib + kb, pw)) {
           atomicMax(best_thr + f, __float_as_uint(pw));
-          atomicMax(best_key + f, pack_key(pw, i, i + kb));
+          atomicMax(best_key + f, pack_key(pw, ib, ib + kb));
         }
       }
     }
