@@ -17,8 +17,11 @@ launch sequence per curve); ``e2e`` repeats the step with the light curves copie
 pinned host memory and every spectrum copied back inside the timed region.
 
 ``--workload masked``: 1024 Kepler-like curves x 65,536 samples, detrend + masked BLS over
-16,384 frequencies (the plain image entry points).  ``--workload served``: the
-continuous-batching server under Poisson arrivals (p50/p99 latency per offered load).
+16,384 frequencies (the plain image entry points).  ``--workload plain``: plain BLS on 64
+curves x 4096 samples, 4096 frequencies, nb 1024 (geebls_simple).  ``--workload tls``: GTLS
+in the reference's semantics on 4096 TESS-like curves x 18,000 epochs (8 widths x 16 ingress
+widths per epoch).  ``--workload served``: the continuous-batching server under Poisson
+arrivals (p50/p99 latency per offered load).
 
 ``--impl reference`` times the reference's algorithm on the host CPU (the FP64 C
 restatement of geebls and gtls with scipy's median filter, all host threads) on a bounded
@@ -61,7 +64,7 @@ def parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--workload", default="ragged", choices=["ragged", "masked", "served"])
+    p.add_argument("--workload", default="ragged", choices=["ragged", "masked", "served", "plain", "tls"])
     p.add_argument("--nq", type=int, default=None,
                    help="curves per GPU (default: 10,000 ragged, 1024 masked)")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -628,6 +631,72 @@ def run_ragged(args, rank, world, local_rank):
     print(json.dumps(line), flush=True)
 
 
+# ----------------------------------------------------------------------------- image workloads
+
+def _timed(fn, steps, warmup, dev, world):
+    import torch
+    import torch.distributed as dist
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(warmup):
+        fn()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record(stream)
+    for _ in range(steps):
+        fn()
+    e.record(stream)
+    torch.cuda.synchronize(dev)
+    clk = clocks.stop()
+    t = torch.tensor([s.elapsed_time(e) / steps], device=dev, dtype=torch.float64)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t[0]), clk
+
+
+def run_image(args, rank, world, local_rank):
+    """Config 1 (plain BLS) or config 3 (GTLS, reference semantics) through the image entry
+    points, inputs resident (evaluations: (curve, frequency) or (curve, epoch))."""
+    import torch
+    from gtrap_gb300 import _build, api, synth
+    _build.build()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    d = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    if args.workload == "plain":
+        nq = args.nq or 64
+        wl = synth.plain_bls(nq=nq, seed=1000 + 100000 * rank)
+        lc, tu = d(wl.lc), d(wl.tu)
+        fn = lambda: api.geebls_simple(lc, tu, wl.nf, wl.nb, wl.kma, wl.kmi, wl.kkmi, wl.fmin, wl.df)
+        evals = nq * wl.nf
+        cfg = {"workload": "plain BLS (geebls_simple): %d curves x 4096 samples, nf 4096, nb 1024, "
+                           "qmi 0.005, qma 0.1" % nq, "curves_per_gpu": nq,
+               "l2": "inputs 1 MiB (fit in L2; the kernel is compute bound)"}
+    else:
+        nq = args.nq or 4096
+        lcn, tun, _ = synth.tess_like(nq=nq, n=18000, seed=3000 + 100000 * rank)
+        g = synth.tls_grid()
+        lc, tu = d(lcn), d(tun)
+        fn = lambda: api.gtls(lc, tu, 18000, g["nw"], g["nl"], g["nsc"], g["wmax"], g["dw"], g["deltat"])
+        evals = nq * 18000
+        cfg = {"workload": "GTLS (reference semantics): %d TESS-like curves x 18000 epochs, nw 8 "
+                           "(8 h .. 0.5 h), nl 16, nsc %d; 128 templates per (curve, epoch)"
+                           % (nq, g["nsc"]), "curves_per_gpu": nq, "templates_per_eval": 128,
+               "l2": "inputs %d MiB per GPU exceed L2" % (2 * nq * 18000 * 4 >> 20)}
+    ms, clk = _timed(fn, args.steps, args.warmup, dev, world)
+    if rank != 0:
+        return
+    line = {"metric": METRIC, "value": evals * world / (ms / 1e3), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64" if args.workload == "plain" else "f32",
+            "data": "synthetic", "config": cfg | {"parallelism": "replicas x%d" % world},
+            "gpu_launches": (3 if args.workload == "plain" else 1) * args.steps, "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 # ----------------------------------------------------------------------------- served workload
 
 def run_served(args, rank, world, local_rank):
@@ -704,7 +773,8 @@ def main():
         torch.cuda.set_device(local_rank)
         dist.init_process_group("nccl")
     try:
-        {"ragged": run_ragged, "masked": run_masked, "served": run_served}[args.workload](
+        {"ragged": run_ragged, "masked": run_masked, "served": run_served, "plain": run_image,
+         "tls": run_image}[args.workload](
             args, rank, world, local_rank)
     finally:
         if world > 1:
