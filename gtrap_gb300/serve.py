@@ -433,34 +433,41 @@ class TransitServer:
         self.live_bls = [lv for lv in self.live_bls if lv.last_step < 0]
         self.live_tls = [lv for lv in self.live_tls if lv.last_step < 0]
         self.steps.append(step)
+        self._issue_copies(step)
         return done
 
+    def _issue_copies(self, step):
+        """Queue the output copies of the requests a step finishes on the copy stream, behind
+        the step's kernels (the host does not wait for the step to see that it has run)."""
+        if not step.finishing:
+            return
+        self.d2h.wait_event(step.event)
+        with torch.cuda.stream(self.d2h):
+            for lv in step.finishing:
+                m, o = lv.req.outputs, lv.ooff
+                if lv.req.kind == "tls" and lv.pk_slot >= 0:
+                    st_, idx, val = step.peaks
+                    for t_ in step.peaks:  # keep the buffers until the copies have run
+                        t_.record_stream(self.d2h)
+                    rs = api.PEAK_STATS.itemsize
+                    srcs = (st_[lv.pk_slot * rs:(lv.pk_slot + 1) * rs], idx[lv.pk_slot], val[lv.pk_slot])
+                else:
+                    srcs = [self.o[j][o:o + m] for j in range(3 if lv.req.kind == "bls" else 5)]
+                outs = []
+                for src in srcs:
+                    h = torch.empty(src.numel(), dtype=src.dtype, pin_memory=True)
+                    h.copy_(src, non_blocking=True)
+                    outs.append(h)
+                lv.result = tuple(outs)
+                ev = torch.cuda.Event()
+                ev.record(self.d2h)
+                lv.d2h_event = ev
+        self.draining.extend(step.finishing)
+
     def poll(self) -> list:
-        """Start output copies of requests whose last step finished; return completed results."""
+        """Retire finished steps and return the requests whose outputs have arrived."""
         while self.steps and self.steps[0].event.query():
-            step = self.steps.popleft()
-            self.d2h.wait_event(step.event)
-            with torch.cuda.stream(self.d2h):
-                for lv in step.finishing:
-                    m, o = lv.req.outputs, lv.ooff
-                    if lv.req.kind == "tls" and lv.pk_slot >= 0:
-                        st_, idx, val = step.peaks
-                        for t_ in step.peaks:  # keep the buffers until the copies have run
-                            t_.record_stream(self.d2h)
-                        rs = api.PEAK_STATS.itemsize
-                        srcs = (st_[lv.pk_slot * rs:(lv.pk_slot + 1) * rs], idx[lv.pk_slot], val[lv.pk_slot])
-                    else:
-                        srcs = [self.o[j][o:o + m] for j in range(3 if lv.req.kind == "bls" else 5)]
-                    outs = []
-                    for src in srcs:
-                        h = torch.empty(src.numel(), dtype=src.dtype, pin_memory=True)
-                        h.copy_(src, non_blocking=True)
-                        outs.append(h)
-                    lv.result = tuple(outs)
-                    ev = torch.cuda.Event()
-                    ev.record(self.d2h)
-                    lv.d2h_event = ev
-            self.draining.extend(step.finishing)
+            self.steps.popleft()
         out = []
         keep = []
         for lv in self.draining:
@@ -491,7 +498,7 @@ class TransitServer:
         if len(self.steps) >= self.depth:
             self.steps[0].event.synchronize()
             return
-        dt = 0.0002
+        dt = 0.00005
         if until is not None:
             dt = max(0.0, min(dt, until - time.perf_counter()))
         if self.draining and not self.steps and until is None:

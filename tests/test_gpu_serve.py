@@ -52,7 +52,8 @@ def test_mixed_equals_solo(solo):
     for _ in range(3):
         srv.step()
     rids += [srv.submit(r) for r in reqs[4:]]   # arrive while the first ones run
-    res = {r.rid: r for r in srv.run_until_idle()}
+    srv.run_until_idle()
+    res = {r.rid: r for r in srv.results}       # including results returned by the steps above
     assert srv.step_count > 3 and len(res) == len(reqs)
     for k, rid in enumerate(rids):
         _eq(res[rid].outputs, ref[k])
