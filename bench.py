@@ -20,8 +20,10 @@ pinned host memory and every spectrum copied back inside the timed region.
 16,384 frequencies (the plain image entry points).  ``--workload plain``: plain BLS on 64
 curves x 4096 samples, 4096 frequencies, nb 1024 (geebls_simple).  ``--workload tls``: GTLS
 in the reference's semantics on 4096 TESS-like curves x 18,000 epochs (8 widths x 16 ingress
-widths per epoch).  ``--workload served``: the continuous-batching server under Poisson
-arrivals (p50/p99 latency per offered load).
+widths per epoch).  ``--workload tlsfold``: the folded trapezoid search (an extension) on the
+same curves: 8192 periods (0.5 .. 12 d) x 8 durations (0.5 .. 8 h) x 2048 phase bins.
+``--workload served``: the continuous-batching server under Poisson arrivals (p50/p99
+latency per offered load).
 
 ``--impl reference`` times the reference's algorithm on the host CPU (the FP64 C
 restatement of geebls and gtls with scipy's median filter, all host threads) on a bounded
@@ -64,7 +66,8 @@ def parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--workload", default="ragged", choices=["ragged", "masked", "served", "plain", "tls"])
+    p.add_argument("--workload", default="ragged",
+                   choices=["ragged", "masked", "served", "plain", "tls", "tlsfold"])
     p.add_argument("--nq", type=int, default=None,
                    help="curves per GPU (default: 10,000 ragged, 1024 masked)")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -666,7 +669,22 @@ def run_image(args, rank, world, local_rank):
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
     d = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
-    if args.workload == "plain":
+    if args.workload == "tlsfold":
+        nq = args.nq or 4096
+        lcn, tun, _ = synth.tess_like(nq=nq, n=18000, seed=3000 + 100000 * rank)
+        lc, tu = d(lcn), d(tun)
+        off = torch.zeros(nq, dtype=torch.float32, device=dev)
+        nf, fmin = 8192, 1.0 / 12.0
+        df = (2.0 - fmin) / (nf - 1)
+        durs = np.linspace(0.5, 8.0, 8).astype(np.float32) / 24.0
+        fn = lambda: api.tls_fold(lc, tu, off, nf, 2048, fmin, df, durs, lfrac=0.2, dmax=1024)
+        evals = nq * nf
+        cfg = {"workload": "folded trapezoid search (extension): %d TESS-like curves x 18000 samples, "
+                           "8192 periods 0.5..12 d, 8 durations 0.5..8 h, 2048 phase bins, ingress "
+                           "0.2 of the duration; (curve, period) evaluations of 8 x 2048 templates"
+                           % nq, "curves_per_gpu": nq, "templates_per_eval": 8 * 2048,
+               "l2": "inputs %d MiB per GPU exceed L2" % (2 * nq * 18000 * 4 >> 20)}
+    elif args.workload == "plain":
         nq = args.nq or 64
         wl = synth.plain_bls(nq=nq, seed=1000 + 100000 * rank)
         lc, tu = d(wl.lc), d(wl.tu)
@@ -774,7 +792,7 @@ def main():
         dist.init_process_group("nccl")
     try:
         {"ragged": run_ragged, "masked": run_masked, "served": run_served, "plain": run_image,
-         "tls": run_image}[args.workload](
+         "tls": run_image, "tlsfold": run_image}[args.workload](
             args, rank, world, local_rank)
     finally:
         if world > 1:

@@ -60,6 +60,9 @@ _SIGNATURES = {
                              f32, f32, i32, u32, vp]),
     "gtrap_pack_curves": (C.c_int, [vp, vp, vp, vp, vp, u32, u32, vp, vp, vp, vp, u64, u32, f32, f32,
                                     i32, vp, vp, vp, vp]),
+    "gtrap_tls_fold_workspace_size": (sz, [u32, u32]),
+    "gtrap_tls_fold": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, u32, u32, u32, u32, f32, f32, vp, u32, f32,
+                                 u32, vp, sz, vp]),
     "gtrap_picktrap": (C.c_int, [vp, vp, vp, vp, u64, vp, vp, vp, u32, f64, f64, i32, i32, i32, vp, vp,
                                  vp, vp, vp]),
     "gtrap_peakstat_max_samples": (sz, []),

@@ -294,3 +294,31 @@ def picktrap(lc: torch.Tensor, tu: torch.Tensor, curve, T0, W, *, off=None, n=No
            int(nx), int(max_get), as_ptr(wnc), as_ptr(gapx), as_ptr(prec), as_ptr(status),
            stream_handle(stream))
     return wnc, gapx, prec, status
+
+
+def tls_fold(lc, tu, offset_, nf, nb, fmin, df, durations, *, lfrac=0.2, dmax=None, out=None,
+             stream=None):
+    """Folded trapezoid search (gtrap_tls_fold): for each curve of ``lc[n, nq]`` and each
+    f_j = fmin + j*df, the best trapezoid (durations in days, ingress fraction ``lfrac``) over
+    nb phase bins.  Returns (tsr [nq, nf], start bin, duration index, depth)."""
+    require_cuda()
+    lc = _f32(lc, "lc")
+    tu = _f32(tu, "tu")
+    offset_ = _f32(offset_, "offset")
+    n, nq = lc.shape
+    dmax = nb // 2 if dmax is None else int(dmax)
+    w = _np.ascontiguousarray(durations, dtype=_np.float32)
+    dev = lc.device
+    if out is None:
+        out = (torch.empty((nq, nf), dtype=torch.float32, device=dev),
+               torch.empty((nq, nf), dtype=torch.int32, device=dev),
+               torch.empty((nq, nf), dtype=torch.int32, device=dev),
+               torch.empty((nq, nf), dtype=torch.float32, device=dev))
+    tsr, st, du, dep = out
+    need = N.fn("gtrap_tls_fold_workspace_size")(n, nq)
+    ws = workspace(need, slot="tls_fold")
+    N.call("gtrap_tls_fold", as_ptr(tsr), as_ptr(st), as_ptr(du), as_ptr(dep), as_ptr(lc), as_ptr(tu),
+           as_ptr(offset_), n, nq, int(nf), int(nb), float(fmin), float(df),
+           w.ctypes.data_as(C.c_void_p), int(w.size), float(lfrac), int(dmax), as_ptr(ws), ws.numel(),
+           stream_handle(stream))
+    return tsr, st, du, dep

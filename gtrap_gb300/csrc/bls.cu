@@ -1138,6 +1138,25 @@ int pool_carve(void *pool, size_t pool_bytes, uint64_t total, uint32_t flags, in
 
 }  // namespace
 
+// Quantisation and exact phase encoding of an [n, nq] image for other folded searches
+// (gtrap_tls_fold): the prep of gtrap_geebls with a caller-chosen bound on |quantised flux|.
+namespace gtrap {
+int bls_prep_image(const float *lc, const float *tu, const float *offset, uint32_t n, uint32_t nq,
+                   float fmin, float df, double xq_max, int32_t *sx, uint32_t *nv, int32_t *X,
+                   ulonglong2 *AB, cudaStream_t stream) {
+  PrepArgs pa;
+  pa.lc = lc; pa.tu = tu; pa.offset = offset;
+  pa.sx = sx; pa.nv = nv; pa.X = X; pa.AB = AB; pa.T = nullptr;
+  pa.n = n; pa.nq = nq; pa.n_eff = n;
+  pa.fmin = fmin; pa.df = df; pa.xq_max = xq_max;
+  pa.full = 1; pa.exact = 1;
+  bls_scale_kernel<<<(nq + 31) / 32, dim3(32, 32), 0, stream>>>(pa);
+  GTRAP_TRY(check_launch("bls_scale_kernel"));
+  bls_pack_kernel<<<dim3((nq + 31) / 32, (n + 31) / 32), dim3(32, 8), 0, stream>>>(pa);
+  return check_launch("bls_pack_kernel");
+}
+}  // namespace gtrap
+
 extern "C" {
 
 uint32_t gtrap_bls_tile_frequencies(uint32_t nb, uint32_t kma) {

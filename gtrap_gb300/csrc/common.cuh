@@ -45,6 +45,12 @@ struct Carver {
 
 inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
+// Quantised flux (|xq| <= xq_max, INT32_MIN for masked samples) and exact phase pairs of an
+// [n, nq] image, curve-major; sx/nv receive each curve's scale exponent and valid count.
+int bls_prep_image(const float *lc, const float *tu, const float *offset, uint32_t n, uint32_t nq,
+                   float fmin, float df, double xq_max, int32_t *sx, uint32_t *nv, int32_t *X,
+                   ulonglong2 *AB, cudaStream_t stream);
+
 inline bool is_pow2(uint32_t x) { return x && !(x & (x - 1)); }
 
 inline int ilog2u(uint32_t x) {

@@ -263,6 +263,25 @@ int gtrap_pack_curves(const int64_t *cno, const double *t, const float *flux, co
                       double *t0, int32_t *status, gtrap_stream_t stream);
 
 /* ---------------------------------------------------------------------------
+ * Folded trapezoid search (an extension: no counterpart in the reference, whose gtls
+ * searches single events).  For curve q and f_j = fmin + j*df, the samples of lc/tu [n, nq]
+ * (mask t < 0, flux - offset[q]) are folded into nb phase bins exactly as gtrap_geebls folds
+ * them, and every trapezoid template (duration durations[d] days -> D = rint(W f nb) bins,
+ * ingress and egress of L = max(1, rint(lfrac D)) bins each, at most D/2; start bin i < nb)
+ * is fitted: TSR^2 = (sum S tau - m sum C tau)^2 / (N sum C tau^2 - (sum C tau)^2), the BLS
+ * signal residue for a box.  Outputs [nq, nf]: tsr = max TSR (flux units), start bin,
+ * duration index and least-squares depth of the best template (larger TSR, then lower d,
+ * then lower i).  durations: host array of nd <= 32 values; templates with D < 2 or
+ * D > dmax (<= nb) are skipped.  nb a power of two in [32, 4096], n < 2^20.
+ * ------------------------------------------------------------------------- */
+size_t gtrap_tls_fold_workspace_size(uint32_t n, uint32_t nq);
+int gtrap_tls_fold(float *tsr, uint32_t *start, uint32_t *dur, float *depth, const float *lc,
+                   const float *tu, const float *offset, uint32_t n, uint32_t nq, uint32_t nf,
+                   uint32_t nb, float fmin, float df, const float *durations, uint32_t nd,
+                   float lfrac, uint32_t dmax, void *workspace, size_t workspace_bytes,
+                   gtrap_stream_t stream);
+
+/* ---------------------------------------------------------------------------
  * Candidate windows for the classifier.  Replaces pick_Wnormalized_cleaned_lc_direct
  * (gtrap/picktrap.py:27-172) for a batch of candidates: candidate c lies on curve curve[c]
  * (series lc/tu[off[q] + e*stride], e < n[q]) at time T0[c] with width W[c] (days).  Writes

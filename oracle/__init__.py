@@ -26,7 +26,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 LIB = BUILD / "liboracle.so"
-SOURCES = [HERE / "bls_oracle.c", HERE / "gtls_oracle.c"]
+SOURCES = [HERE / "bls_oracle.c", HERE / "gtls_oracle.c", HERE / "tlsfold_oracle.c"]
 
 _lib = None
 
@@ -129,6 +129,42 @@ def gtls(lc, tu, nt, nw, nl, nsc, wmax, dw, deltat, *, mode=0, w_fma=True, t_fma
                     int(bool(fix_a)), int(nthreads), _ptr(sn, C.c_double), _ptr(w, C.c_float), _ptr(t0, C.c_float),
                     _ptr(l, C.c_float), _ptr(h, C.c_double))
     return sn, w, t0, l, h
+
+
+def tls_fold(lc, tu, offset, nf, nb, fmin, df, durations, lfrac=0.2, dmax=None):
+    """FP64 folded trapezoid search (see tlsfold_oracle.c); returns (tsr, start, dur, depth,
+    pmax), each [nq, nf]."""
+    lib = _load()
+    lc = np.ascontiguousarray(lc, dtype=np.float32)
+    tu = np.ascontiguousarray(tu, dtype=np.float32)
+    off = np.ascontiguousarray(offset, dtype=np.float32)
+    w = np.ascontiguousarray(durations, dtype=np.float32)
+    n, nq = lc.shape
+    dmax = nb // 2 if dmax is None else dmax
+    tsr = np.empty((nq, nf)); depth = np.empty((nq, nf)); pmax = np.empty((nq, nf))
+    st = np.empty((nq, nf), np.uint32); du = np.empty((nq, nf), np.uint32)
+    f = lib.oracle_tls_fold
+    f.restype = C.c_int
+    r = f(_ptr(lc, C.c_float), _ptr(tu, C.c_float), _ptr(off, C.c_float), n, nq, int(nf), int(nb),
+          C.c_float(fmin), C.c_float(df), _ptr(w, C.c_float), int(w.size), C.c_float(lfrac), int(dmax),
+          _ptr(tsr, C.c_double), _ptr(st, C.c_uint32), _ptr(du, C.c_uint32), _ptr(depth, C.c_double),
+          _ptr(pmax, C.c_double))
+    if r:
+        raise ValueError("oracle_tls_fold rejected the arguments")
+    return tsr, st, du, depth, pmax
+
+
+def tls_fold_power(lc, tu, offset, q, j, nb, fmin, df, W, lfrac, dmax, i):
+    """FP64 TSR^2 of one folded-trapezoid template (for tie checks)."""
+    lib = _load()
+    lc = np.ascontiguousarray(lc, dtype=np.float32)
+    tu = np.ascontiguousarray(tu, dtype=np.float32)
+    off = np.ascontiguousarray(offset, dtype=np.float32)
+    n, nq = lc.shape
+    f = lib.oracle_tls_fold_power
+    f.restype = C.c_double
+    return f(_ptr(lc, C.c_float), _ptr(tu, C.c_float), _ptr(off, C.c_float), n, nq, int(q), int(j),
+             int(nb), C.c_float(fmin), C.c_float(df), C.c_float(W), C.c_float(lfrac), int(dmax), int(i))
 
 
 # ---------------------------------------------------------------------------- gfilter
