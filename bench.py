@@ -128,6 +128,22 @@ def smem_atomic_peak(dev):
     return upd * 3 / (ps.elapsed_time(pe) / 1e3)
 
 
+def smem_load_peak(dev):
+    """Shared-memory load bandwidth of this GPU in bytes/s (conflict-free 64-bit loads)."""
+    import torch
+    from gtrap_gb300 import api
+    stream = torch.cuda.current_stream(dev)
+    _, nbytes = api.smem_load_peak_probe()
+    torch.cuda.synchronize(dev)
+    ps, pe = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ps.record(stream)
+    for _ in range(3):
+        api.smem_load_peak_probe()
+    pe.record(stream)
+    torch.cuda.synchronize(dev)
+    return nbytes * 3 / (ps.elapsed_time(pe) / 1e3)
+
+
 def fp32_peak_tflops(dev):
     """FP32 FMA issue peak of this GPU, measured live (MEASURED_PEAKS.json has no FP32 figure)."""
     import torch
@@ -669,22 +685,7 @@ def run_image(args, rank, world, local_rank):
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
     d = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
-    if args.workload == "tlsfold":
-        nq = args.nq or 4096
-        lcn, tun, _ = synth.tess_like(nq=nq, n=18000, seed=3000 + 100000 * rank)
-        lc, tu = d(lcn), d(tun)
-        off = torch.zeros(nq, dtype=torch.float32, device=dev)
-        nf, fmin = 8192, 1.0 / 12.0
-        df = (2.0 - fmin) / (nf - 1)
-        durs = np.linspace(0.5, 8.0, 8).astype(np.float32) / 24.0
-        fn = lambda: api.tls_fold(lc, tu, off, nf, 2048, fmin, df, durs, lfrac=0.2, dmax=1024)
-        evals = nq * nf
-        cfg = {"workload": "folded trapezoid search (extension): %d TESS-like curves x 18000 samples, "
-                           "8192 periods 0.5..12 d, 8 durations 0.5..8 h, 2048 phase bins, ingress "
-                           "0.2 of the duration; (curve, period) evaluations of 8 x 2048 templates"
-                           % nq, "curves_per_gpu": nq, "templates_per_eval": 8 * 2048,
-               "l2": "inputs %d MiB per GPU exceed L2" % (2 * nq * 18000 * 4 >> 20)}
-    elif args.workload == "plain":
+    if args.workload == "plain":
         nq = args.nq or 64
         wl = synth.plain_bls(nq=nq, seed=1000 + 100000 * rank)
         lc, tu = d(wl.lc), d(wl.tu)
@@ -712,6 +713,162 @@ def run_image(args, rank, world, local_rank):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64" if args.workload == "plain" else "f32",
             "data": "synthetic", "config": cfg | {"parallelism": "replicas x%d" % world},
             "gpu_launches": (3 if args.workload == "plain" else 1) * args.steps, "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------- folded TLS
+
+TF_N, TF_NF, TF_NB, TF_DMAX, TF_LFRAC = 18000, 8192, 2048, 1024, 0.2
+TF_FMIN = 1.0 / 12.0
+TF_DF = (2.0 - TF_FMIN) / (TF_NF - 1)
+TF_DURS = (np.linspace(0.5, 8.0, 8) / 24.0).astype(np.float32)
+
+
+def tlsfold_config(nq):
+    return {"workload": "folded trapezoid search (extension): %d TESS-like curves x %d samples, "
+                        "%d periods 0.5..12 d, 8 durations 0.5..8 h, %d phase bins, ingress %.1f of "
+                        "the duration, longest template %d bins; (curve, period) evaluations of up to "
+                        "8 x %d templates" % (nq, TF_N, TF_NF, TF_NB, TF_LFRAC, TF_DMAX, TF_NB),
+            "curves_per_gpu": nq, "l2": "inputs %d MiB per GPU exceed L2" % (2 * nq * TF_N * 4 >> 20)}
+
+
+def tlsfold_valid_templates():
+    """Templates per frequency the kernel evaluates (2 <= D <= dmax), per frequency index."""
+    j = np.arange(TF_NF, dtype=np.float32)
+    f0 = (np.float32(TF_DF) * j + np.float32(TF_FMIN)).astype(np.float32)
+    D = np.rint(TF_DURS[None, :] * f0[:, None] * np.float32(TF_NB)).astype(np.int64)
+    return ((D >= 2) & (D <= TF_DMAX)).sum(axis=1)
+
+
+def tlsfold_cpu_sample(lcn, tun, threads, n_freqs):
+    """FP64 oracle (direct sums per template, OpenMP over frequencies) on one curve and
+    ``n_freqs`` frequencies spread over the whole grid.  Returns (evals/s, seconds)."""
+    import oracle
+    stride = max(1, TF_NF // n_freqs)
+    lc = np.ascontiguousarray(lcn[:, :1])
+    tu = np.ascontiguousarray(tun[:, :1])
+    off = np.zeros(1, np.float32)
+    t0 = time.perf_counter()
+    oracle.tls_fold(lc, tu, off, n_freqs, TF_NB, TF_FMIN, TF_DF * stride, TF_DURS, lfrac=TF_LFRAC,
+                    dmax=TF_DMAX)
+    dt = time.perf_counter() - t0
+    return n_freqs / dt, dt
+
+
+def run_tlsfold(args, rank, world, local_rank):
+    """Folded trapezoid search over the BLS phase bins (an extension without a reference
+    counterpart): inputs resident for ``value``; pinned host buffers for ``e2e``."""
+    import torch
+    import torch.distributed as dist
+    from gtrap_gb300 import _build, api, synth
+    _build.build()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    stream = torch.cuda.current_stream(dev)
+    nq = args.nq or 4096
+    lcn, tun, _ = synth.tess_like(nq=nq, n=TF_N, seed=3000 + 100000 * rank)
+    lc = torch.from_numpy(lcn).to(dev)
+    tu = torch.from_numpy(tun).to(dev)
+    off = torch.zeros(nq, dtype=torch.float32, device=dev)
+    outs = api.tls_fold(lc, tu, off, TF_NF, TF_NB, TF_FMIN, TF_DF, TF_DURS, lfrac=TF_LFRAC, dmax=TF_DMAX)
+    fn = lambda: api.tls_fold(lc, tu, off, TF_NF, TF_NB, TF_FMIN, TF_DF, TF_DURS, lfrac=TF_LFRAC,
+                              dmax=TF_DMAX, out=outs)
+    ms, clk = _timed(fn, args.steps, args.warmup, dev, world)
+    evals = nq * TF_NF
+    e2e = None
+    if not args.no_e2e:
+        h_lc, h_tu = torch.from_numpy(lcn).pin_memory(), torch.from_numpy(tun).pin_memory()
+        h_o = [torch.empty(a.shape, dtype=a.dtype).pin_memory() for a in outs]
+
+        def e2e_step():
+            lc.copy_(h_lc, non_blocking=True)
+            tu.copy_(h_tu, non_blocking=True)
+            fn()
+            for h, a in zip(h_o, outs):
+                h.copy_(a, non_blocking=True)
+
+        e2e_step()
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        for _ in range(args.steps):
+            e2e_step()
+        e.record(stream)
+        torch.cuda.synchronize(dev)
+        ems = torch.tensor([s.elapsed_time(e) / args.steps], device=dev, dtype=torch.float64)
+        if world > 1:
+            dist.all_reduce(ems, op=dist.ReduceOp.MAX)
+        e2e = {"value": evals * world / (float(ems[0]) / 1e3), "unit": UNIT,
+               "h2d_bytes_per_step": (h_lc.numel() + h_tu.numel()) * 4,
+               "d2h_bytes_per_step": sum(h.numel() * h.element_size() for h in h_o),
+               "ms_per_step": float(ems[0]), "api": "gtrap_gb300.api.tls_fold with pinned host buffers"}
+    if rank != 0:
+        return
+    # roofline: the template phase reads the moment arrays from shared memory; per template
+    # G (low words at three corners, high words at two), GS and K at three corners = 68 B,
+    # plus 20 B per start bin and frequency for the start corner
+    tpl = float(tlsfold_valid_templates().sum()) * nq * TF_NB
+    lds_bytes = tpl * 68.0 + float(evals) * TF_NB * 20.0
+    speak = smem_load_peak(dev)
+    achieved = lds_bytes / (ms / 1e3)
+    nv = float(np.count_nonzero(np.isfinite(lcn) & (tun >= 0)))
+    apeak = smem_atomic_peak(dev)
+    fold_leg = {"bound": "smem_atomics", "achieved": nv * TF_NF / (ms / 1e3), "peak": apeak,
+                "unit": "sample updates/s", "frac": nv * TF_NF / (ms / 1e3) / apeak,
+                "peak_source": "live probe: two 32-bit shared atomics per update on random bins"}
+    traffic = None
+    prof = _profile("tlsfold_traffic.json")
+    if prof and prof.get("dram_bytes_per_curve"):
+        traffic = prof["dram_bytes_per_curve"] * nq
+    line = {"metric": METRIC, "value": evals * world / (ms / 1e3), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64", "data": "synthetic",
+            "config": tlsfold_config(nq) | {"parallelism": "replicas x%d (curves sharded)" % world},
+            "roofline": {"bound": "smem", "achieved": achieved / 1e9, "peak": speak / 1e9, "unit": "GB/s",
+                         "frac": achieved / speak, "traffic": traffic,
+                         "kernel": "tlsfold_kernel (fold + moment arrays + templates)",
+                         "kernel_ms": ms, "templates_per_step": tpl,
+                         "algorithmic_bytes": "68 B of shared-memory loads per template + 20 B per "
+                                              "start bin and frequency",
+                         "peak_source": "live probe: conflict-free 64-bit shared-memory loads",
+                         "fold": fold_leg},
+            "gpu_launches": 2 * args.steps, "clocks": clk}
+    if e2e:
+        line["e2e"] = e2e
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        nfs = min(TF_NF, 256 * threads)
+        v, dt = tlsfold_cpu_sample(lcn, tun, threads, nfs)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": "1 curve x %d frequencies spread over the grid (FP64 oracle, "
+                                          "direct sums per template), %.1f s" % (nfs, dt)}
+    print(json.dumps(line), flush=True)
+
+
+def run_tlsfold_reference(args, rank, world):
+    """The extension has no reference implementation: the FP64 oracle port on the host."""
+    if rank != 0:
+        return
+    from gtrap_gb300 import synth
+    lcn, tun, _ = synth.tess_like(nq=2, n=TF_N, seed=3000)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        tlsfold_cpu_sample(lcn, tun, threads, threads)
+    vals, total = [], 0.0
+    for _ in range(args.steps):
+        v, dt = tlsfold_cpu_sample(lcn, tun, threads, 64 * threads)
+        vals.append(v)
+        total += dt
+    value = float(np.median(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": tlsfold_config(args.nq or 4096),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "per step 1 curve x %d frequencies (FP64 oracle)" % (64 * threads)},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
@@ -782,6 +939,8 @@ def main():
     if args.impl == "reference":
         if args.workload == "masked":
             run_masked_reference(args, rank, world)
+        elif args.workload == "tlsfold":
+            run_tlsfold_reference(args, rank, world)
         else:
             run_ragged_reference(args, rank, world)
         return
@@ -792,7 +951,7 @@ def main():
         dist.init_process_group("nccl")
     try:
         {"ragged": run_ragged, "masked": run_masked, "served": run_served, "plain": run_image,
-         "tls": run_image, "tlsfold": run_image}[args.workload](
+         "tls": run_image, "tlsfold": run_tlsfold}[args.workload](
             args, rank, world, local_rank)
     finally:
         if world > 1:

@@ -211,6 +211,14 @@ def smem_atomic_peak_probe(iters=2048, stream=None):
     return sink, upd.value
 
 
+def smem_load_peak_probe(iters=4096, stream=None):
+    """Launch the shared-memory load probe; returns (sink tensor, bytes read)."""
+    sink = torch.empty(1 << 16, dtype=torch.int64, device="cuda")
+    nbytes = C.c_double(0.0)
+    N.call("gtrap_probe_smem_load_peak", as_ptr(sink), int(iters), C.byref(nbytes), stream_handle(stream))
+    return sink, nbytes.value
+
+
 def fp32_peak_probe(iters=4096, stream=None):
     """Launch the FP32 FMA probe; returns (sink tensor, flop count)."""
     sink = torch.empty(1 << 20, dtype=torch.float32, device="cuda")

@@ -153,9 +153,36 @@ __global__ void __launch_bounds__(512) atomic_probe_kernel(unsigned *sink, uint3
   __syncthreads();
   if (hist[threadIdx.x] == 0x12345678u) sink[blockIdx.x] = 1u;  // keeps the work
 }
+
+// Shared-memory load bandwidth: conflict-free 64-bit loads (a warp reads 256 consecutive
+// bytes), eight independent loads in flight per thread, 64 KB per block, two blocks per SM.
+constexpr int kLdsWords = 8192, kLdsUnroll = 8;
+__global__ void __launch_bounds__(512) lds_probe_kernel(unsigned long long *sink, uint32_t iters) {
+  extern __shared__ unsigned long long words[];
+  for (int i = threadIdx.x; i < kLdsWords; i += blockDim.x) words[i] = 0x9E3779B97F4A7C15ull * (i + 1);
+  __syncthreads();
+  unsigned long long acc = 0;
+  uint32_t idx = threadIdx.x;
+  for (uint32_t it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int u = 0; u < kLdsUnroll; ++u) acc ^= words[(idx + u * 512u) & (kLdsWords - 1)];
+    idx += 32u;
+  }
+  if (acc == 0x12345678ull) sink[blockIdx.x] = acc;  // keeps the work
+}
 }  // namespace
 
 extern "C" {
+
+int gtrap_probe_smem_load_peak(unsigned long long *sink, uint32_t iters, double *bytes, gtrap_stream_t stream) {
+  if (!sink || iters == 0) return gtrap::fail(GTRAP_ERR_INVALID_ARG, "probe: bad arguments");
+  const size_t smem = kLdsWords * sizeof(unsigned long long);
+  GTRAP_TRY(gtrap::ensure_smem((const void *)lds_probe_kernel, smem, "lds_probe"));
+  const int blocks = gtrap::sm_count() * 2;
+  lds_probe_kernel<<<blocks, 512, smem, stream>>>(sink, iters);
+  if (bytes) *bytes = (double)blocks * 512.0 * (double)iters * kLdsUnroll * 8.0;
+  return gtrap::check_launch("lds_probe_kernel");
+}
 
 int gtrap_probe_smem_atomic_peak(unsigned *sink, uint32_t iters, double *updates, gtrap_stream_t stream) {
   if (!sink || iters == 0) return gtrap::fail(GTRAP_ERR_INVALID_ARG, "probe: bad arguments");

@@ -9,15 +9,22 @@
 // which is the BLS SR^2 = s^2 / (r (N - r)) for a box (tau in {0, 1}) and zero mean.  The
 // least-squares depth is -(sum S tau - m sum C tau) N / (N sum C tau^2 - (sum C tau)^2).
 //
-// One block per (curve, frequency).  The fold is the BLS fold (exact 64-bit phase, integer bin
-// sums of flux quantised to 20 bits, verified 32-bit words with a 64-bit refold when a bin
-// holds 2048 samples or more).  Exact integer prefix sums of C, S, C u, S u and C u^2 over the
-// phase axis extended by the longest template (u = 2b + 1: twice the bin centre) give every
-// template's three ramp and flat sums in O(1) and exactly; only the final ratio is rounded.
-// Template (duration d, start bin i): D = rint(W_d f nb) bins, L = max(1, rint(lfrac D))
-// bins of ingress and of egress (at most D / 2); tau = (u - 2i) / 2L on [i, i + L),
-// 1 on [i + L, i + D - L), (2(i + D) - u) / 2L on [i + D - L, i + D).  Durations with D < 2
-// or D > dmax bins are skipped.  Ties: larger TSR, then lower d, then lower i.
+// One block per (curve, group of F frequencies; F = 1 .. 3 by shared-memory room).  The fold is
+// the BLS fold (exact 64-bit phase, integer bin sums of flux quantised to 20 bits, verified
+// 32-bit words with a 64-bit refold when a bin holds 2048 samples or more), F histograms from
+// one read of each sample.  Per frequency, three exact integer moment arrays over the phase
+// axis extended by the longest template (x = 0 .. nb + dmax; bins past nb wrap),
+//   G[x] = sum_{b<x} C_b (2(x-b) - 1),  GS[x] = sum_{b<x} S_b (2(x-b) - 1),
+//   K[x] = sum_{b<x} C_b (2(x-b) - 1)^2,
+// give every template's weighted sums in O(1) and exactly: with ramp weights w = 2L tau
+// (2k + 1 on the k-th ingress bin, 2L on the flat bottom, mirrored on egress) and the corners
+// e1 = i + L, e2 = i + D - L, e3 = i + D,
+//   sum C w   = G[i] - G[e1] - G[e2] + G[e3],
+//   sum S w   = GS[i] - GS[e1] - GS[e2] + GS[e3],
+//   sum C w^2 = K[e3] - K[e2] + K[e1] - K[i] - 4L (G[e1] + G[e2]);
+// only the final ratio is rounded.  Template (duration d, start bin i): D = rint(W_d f nb)
+// bins, L = max(1, rint(lfrac D)) bins of ingress and of egress (at most D / 2).  Durations
+// with D < 2 or D > dmax bins are skipped.  Ties: larger TSR, then lower d, then lower i.
 #include "common.cuh"
 
 #include <math.h>
@@ -27,7 +34,10 @@ namespace {
 using gtrap::fail;
 
 constexpr int kTfThreads = 512;
+constexpr int kTfWarps = kTfThreads / 32;
 constexpr int kTfMaxDur = 32;
+constexpr int kTfMaxF = 3;
+constexpr int kTfBatch = 4;  // samples a thread loads before folding them
 constexpr int32_t kMaskedQ = INT32_MIN;
 constexpr double kTfXqMax = 1048575.0;  // |quantised flux| < 2^20
 
@@ -36,7 +46,8 @@ struct TfArgs {
   const ulonglong2 *AB;      // [nq, n] exact phase pairs
   const int32_t *sx;         // [nq]
   const uint32_t *nv;        // [nq]
-  uint32_t n, nq, nf, nb, dmax, nd;
+  uint32_t n, nq, nf, nb, dmax, nd, ngroups;
+  uint32_t pbytes;           // bytes of the moment arrays (16-byte multiple)
   int lognb;
   float fmin, df, lfrac;
   float W[kTfMaxDur];        // durations (days)
@@ -48,206 +59,334 @@ __device__ __forceinline__ long long shfl_up_ll(long long v, int o) {
   return (long long)__shfl_up_sync(0xffffffffu, (unsigned long long)v, o);
 }
 
+// int64 -> float without the 64-bit conversion instruction (it issues on the FP64 pipe, which is
+// narrow on this part): v = hi 2^32 + lo with a signed low word, joined by one rounding FMA.
+// Exact rounding below 2^31 in magnitude, within 0.75 ulp above (|v| < 2^55).
+__device__ __forceinline__ float i64_to_f32(long long v) {
+  const int lo = (int)(uint32_t)v;
+  const int hi = (int)((v - lo) >> 32);
+  return __fmaf_rn((float)hi, 4294967296.0f, (float)lo);
+}
+
+// Moment entry x in shared memory: a 16-byte word (GS[x], K[x] | Ghi[x] << 48) and the low
+// word of G[x] in a separate array: five wavefronts a warp for one corner of 32 templates.
+// K < N (2x)^2 < 2^48 and G < 2N x < 2^35 for n < 2^20 samples and x <= 8192, so the high
+// word of G fits above K.
+constexpr unsigned long long kM48 = (1ull << 48) - 1;
+
+__device__ __forceinline__ longlong2 pack_entry(long long gs, long long k, long long g) {
+  return make_longlong2(gs, (long long)((unsigned long long)k | ((unsigned long long)g >> 32) << 48));
+}
+__device__ __forceinline__ long long entry_k(long long y) { return (long long)((unsigned long long)y & kM48); }
+__device__ __forceinline__ long long entry_g(long long y, uint32_t lo) {
+  return (long long)((((unsigned long long)y >> 48) << 32) | lo);
+}
+
+// Shared memory: the moment entries GSK[E] (16 bytes) and Glo[E] (4 bytes) in the first
+// pbytes; histogram f (nb flux words, then nb counts) at pbytes - 8 nb + 8 nb f.  Histogram 0 lies inside the moment arrays and is read into
+// registers before they are written; later histograms lie past them.  A frequency whose bins
+// need 64-bit flux sums refolds them into the first 8 nb bytes, below histogram 0.
+template <int F, int RM>
 __global__ void __launch_bounds__(kTfThreads, 2) tlsfold_kernel(const TfArgs a) {
   extern __shared__ __align__(16) unsigned char smraw[];
-  __shared__ long long wsum[5][kTfThreads / 32];
-  __shared__ unsigned long long best_s;
+  __shared__ long long wsum[4][kTfWarps];
+  __shared__ uint32_t wsumc[kTfWarps];
+  __shared__ long long wbase[4][kTfWarps + 1];
+  __shared__ uint32_t wbasec[kTfWarps + 1];
+  __shared__ int sDL[F][kTfMaxDur];  // D | L << 16, 0 when skipped
+  __shared__ unsigned long long best_s[F];
   __shared__ int s_bad;
-  const uint32_t q = blockIdx.x / a.nf, j = blockIdx.x - q * a.nf;
+  const uint32_t q = blockIdx.x / a.ngroups, j0 = (blockIdx.x - q * a.ngroups) * F;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int nb = (int)a.nb, E = nb + (int)a.dmax + 1;  // prefix entries 0 .. nb + dmax
-  // histogram (two 32-bit words per bin, or 64-bit flux sums after a refold) aliases the
-  // start of the prefix arrays: it is read completely before they are written
-  uint32_t *hS = reinterpret_cast<uint32_t *>(smraw), *hC = hS + nb;
-  unsigned long long *hS64 = reinterpret_cast<unsigned long long *>(hC + nb);
-  long long *PS = reinterpret_cast<long long *>(smraw);
-  long long *PSU = PS + E, *PCU = PSU + E, *PCU2 = PCU + E;
-  int32_t *PC = reinterpret_cast<int32_t *>(PCU2 + E);
-
+  const int nb = (int)a.nb, E = nb + (int)a.dmax + 1;
+  longlong2 *GSK = reinterpret_cast<longlong2 *>(smraw);
+  uint32_t *Glo = reinterpret_cast<uint32_t *>(GSK + E);
+  uint32_t *hist = reinterpret_cast<uint32_t *>(smraw + a.pbytes) - 2 * nb;
+  unsigned long long *S64 = reinterpret_cast<unsigned long long *>(smraw);
   const int32_t *Xq = a.X + (size_t)q * a.n;
   const ulonglong2 *ABq = a.AB + (size_t)q * a.n;
   const int shift = 64 - a.lognb;
-  for (int b = tid; b < 2 * nb; b += kTfThreads) hS[b] = 0u;
-  if (tid == 0) s_bad = 0;
-  __syncthreads();
-  // ---- fold
-  for (uint32_t k = tid; k < a.n; k += kTfThreads) {
-    const int32_t xq = __ldg(Xq + k);
-    if (xq == kMaskedQ) continue;
-    const ulonglong2 ab = __ldg(ABq + k);
-    const uint32_t bin = (uint32_t)((ab.x + (unsigned long long)j * ab.y) >> shift);
-    atomicAdd(hS + bin, (uint32_t)xq);
-    atomicAdd(hC + bin, 1u);
-  }
-  __syncthreads();
-  // 32-bit flux sums are exact while a bin holds fewer than 2048 samples (|xq| < 2^20)
-  for (int b = tid; b < nb; b += kTfThreads)
-    if (hC[b] >= 2048u) s_bad = 1;
-  __syncthreads();
-  const bool wide = s_bad != 0;
-  if (wide) {
-    for (int b = tid; b < nb; b += kTfThreads) hS64[b] = 0ull;
-    __syncthreads();
-    for (uint32_t k = tid; k < a.n; k += kTfThreads) {
-      const int32_t xq = __ldg(Xq + k);
-      if (xq == kMaskedQ) continue;
-      const ulonglong2 ab = __ldg(ABq + k);
-      const uint32_t bin = (uint32_t)((ab.x + (unsigned long long)j * ab.y) >> shift);
-      atomicAdd(hS64 + bin, (unsigned long long)(long long)xq);
-    }
-    __syncthreads();
-  }
-  // ---- exact prefix sums over bins (R consecutive bins per thread, block scan)
-  const int R = (nb + kTfThreads - 1) / kTfThreads;  // <= 8
-  const int b0 = tid * R;
-  long long vc[8], vs[8];
-#pragma unroll
-  for (int r = 0; r < 8; ++r) {
-    const int b = b0 + r;
-    const bool ok = r < R && b < nb;
-    vc[r] = ok ? (long long)hC[b] : 0;
-    vs[r] = ok ? (wide ? (long long)hS64[b] : (long long)(int32_t)hS[b]) : 0;
-  }
-  long long t5[5] = {0, 0, 0, 0, 0};  // this thread's sums of C, S, C u, S u, C u^2
-#pragma unroll
-  for (int r = 0; r < 8; ++r) {
-    const long long u = 2LL * (b0 + r) + 1;
-    t5[0] += vc[r]; t5[1] += vs[r]; t5[2] += vc[r] * u; t5[3] += vs[r] * u; t5[4] += vc[r] * u * u;
-  }
-  long long inc[5];
-#pragma unroll
-  for (int v = 0; v < 5; ++v) {
-    long long x = t5[v];
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const long long y = shfl_up_ll(x, o);
-      if (lane >= o) x += y;
-    }
-    inc[v] = x;
-    if (lane == 31) wsum[v][warp] = x;
-  }
-  __syncthreads();  // every thread has read its bins: the prefix arrays may now be written
-  long long ex[5];
-#pragma unroll
-  for (int v = 0; v < 5; ++v) {
-    long long base = 0;
-    for (int w = 0; w < warp; ++w) base += wsum[v][w];
-    ex[v] = base + inc[v] - t5[v];
-  }
-  if (tid == 0) { PC[0] = 0; PS[0] = 0; PCU[0] = 0; PSU[0] = 0; PCU2[0] = 0; }
-  {
-    long long c = ex[0], s = ex[1], cu = ex[2], su = ex[3], cu2 = ex[4];
-#pragma unroll
-    for (int r = 0; r < 8; ++r) {
-      const int b = b0 + r;
-      if (r < R && b < nb) {
-        const long long u = 2LL * b + 1;
-        c += vc[r]; s += vs[r]; cu += vc[r] * u; su += vs[r] * u; cu2 += vc[r] * u * u;
-        PC[b + 1] = (int32_t)c; PS[b + 1] = s; PCU[b + 1] = cu; PSU[b + 1] = su; PCU2[b + 1] = cu2;
-      }
-    }
-  }
-  __syncthreads();
-  // extension past nb: bin b + nb is bin b at coordinate u + 2nb
-  {
-    const long long tc = PC[nb], ts = PS[nb], tcu = PCU[nb], tsu = PSU[nb], tcu2 = PCU2[nb];
-    const long long nb2 = 2LL * nb;
-    for (int e = tid + 1; e <= (int)a.dmax; e += kTfThreads) {
-      const long long c = PC[e], s = PS[e], cu = PCU[e];
-      PC[nb + e] = (int32_t)(tc + c);
-      PS[nb + e] = ts + s;
-      PCU[nb + e] = tcu + cu + nb2 * c;
-      PSU[nb + e] = tsu + PSU[e] + nb2 * s;
-      PCU2[nb + e] = tcu2 + PCU2[e] + 2 * nb2 * cu + nb2 * nb2 * c;
-    }
-  }
-  if (tid == 0) best_s = 0ull;
-  __syncthreads();
 
-  // ---- templates
-  const float Nf = (float)a.nv[q];
-  const long long Nl = (long long)PC[nb];
-  const float mean = Nl > 0 ? (float)PS[nb] / (float)Nl : 0.0f;
-  const float f0 = __fmaf_rn(a.df, (float)j, a.fmin);
-  float bp = 0.0f;
-  unsigned long long bkey = 0ull;
-  for (uint32_t d = 0; d < a.nd; ++d) {
-    const int D = (int)rintf(a.W[d] * f0 * (float)nb);
-    if (D < 2 || D > (int)a.dmax) continue;
-    int L = max(1, (int)rintf(a.lfrac * (float)D));
-    if (2 * L > D) L = D / 2;
-    const long long L2 = 2LL * L, L4 = 4LL * L * L;
-    for (int i = tid; i < nb; i += kTfThreads) {
-      const int e1 = i + L, e2 = i + D - L, e3 = i + D;
-      const long long iu = 2LL * i, ie = 2LL * e3;
-      // flat
-      const long long Cf = (long long)PC[e2] - PC[e1], Sf = PS[e2] - PS[e1];
-      // up ramp [i, e1)
-      const long long Cu = (long long)PC[e1] - PC[i], Su = PS[e1] - PS[i];
-      const long long CUu = PCU[e1] - PCU[i], SUu = PSU[e1] - PSU[i], CU2u = PCU2[e1] - PCU2[i];
-      // down ramp [e2, e3)
-      const long long Cd = (long long)PC[e3] - PC[e2], Sd = PS[e3] - PS[e2];
-      const long long CUd = PCU[e3] - PCU[e2], SUd = PSU[e3] - PSU[e2], CU2d = PCU2[e3] - PCU2[e2];
-      const long long A2 = L2 * Cf + (CUu - iu * Cu) + (ie * Cd - CUd);
-      const long long N2 = L2 * Sf + (SUu - iu * Su) + (ie * Sd - SUd);
-      const long long B4 = L4 * Cf + (CU2u - 2 * iu * CUu + iu * iu * Cu) + (ie * ie * Cd - 2 * ie * CUd + CU2d);
-      const float a2 = (float)A2;
-      const float num = (float)N2 - mean * a2;
-      const float den = Nf * (float)B4 - a2 * a2;
-      if (!(den > 0.0f)) continue;
-      const float p = num * num / den;
-      if (p > bp) {
-        bp = p;
-        bkey = ((unsigned long long)__float_as_uint(p) << 32) |
-               (0xffffffffu - (((unsigned)d << 24) | (unsigned)i));
-      }
-    }
-  }
-  // block argmax: larger TSR, then lower (d, i)
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const unsigned long long ok = __shfl_xor_sync(0xffffffffu, bkey, o);
-    bkey = ok > bkey ? ok : bkey;
-  }
-  if (lane == 0 && bkey) atomicMax(&best_s, bkey);
-  __syncthreads();
-  if (tid == 0) {
-    const size_t o = (size_t)q * a.nf + j;
-    const unsigned long long k = best_s;
-    if (!k) {
-      a.tsr[o] = 0.0f; a.depth[o] = 0.0f; a.start[o] = 0u; a.dur[o] = 0u;
-    } else {
-      const unsigned di = 0xffffffffu - (unsigned)(k & 0xffffffffull);
-      const int d = (int)(di >> 24), i = (int)(di & 0xffffffu);
+  for (int b = tid; b < 2 * nb * F; b += kTfThreads) hist[b] = 0u;
+  if (tid < F * 32) {
+    const int f = tid >> 5, d = tid & 31;
+    int v = 0;
+    if (d < (int)a.nd && j0 + f < a.nf) {
+      const float f0 = __fmaf_rn(a.df, (float)(j0 + f), a.fmin);
       const int D = (int)rintf(a.W[d] * f0 * (float)nb);
       int L = max(1, (int)rintf(a.lfrac * (float)D));
       if (2 * L > D) L = D / 2;
-      // the winner's depth, with the same sums
-      const int e1 = i + L, e2 = i + D - L, e3 = i + D;
-      const long long iu = 2LL * i, ie = 2LL * e3, L2 = 2LL * L, L4 = 4LL * L * L;
-      const long long A2 = L2 * ((long long)PC[e2] - PC[e1]) + ((PCU[e1] - PCU[i]) - iu * ((long long)PC[e1] - PC[i])) +
-                           (ie * ((long long)PC[e3] - PC[e2]) - (PCU[e3] - PCU[e2]));
-      const long long N2 = L2 * (PS[e2] - PS[e1]) + ((PSU[e1] - PSU[i]) - iu * (PS[e1] - PS[i])) +
-                           (ie * (PS[e3] - PS[e2]) - (PSU[e3] - PSU[e2]));
-      const long long B4 = L4 * ((long long)PC[e2] - PC[e1]) +
-                           ((PCU2[e1] - PCU2[i]) - 2 * iu * (PCU[e1] - PCU[i]) + iu * iu * ((long long)PC[e1] - PC[i])) +
-                           (ie * ie * ((long long)PC[e3] - PC[e2]) - 2 * ie * (PCU[e3] - PCU[e2]) + (PCU2[e3] - PCU2[e2]));
-      const double num = (double)N2 - (double)mean * (double)A2;
-      const double den = (double)Nf * (double)B4 - (double)A2 * (double)A2;
-      const double sc = ldexp(1.0, -a.sx[q]);
-      a.tsr[o] = (float)(sqrt((double)__uint_as_float((unsigned)(k >> 32))) * sc);
-      a.depth[o] = (float)(-num * (double)Nf * (double)L2 / den * sc);
-      a.start[o] = (uint32_t)i;
-      a.dur[o] = (uint32_t)d;
+      if (D >= 2 && D <= (int)a.dmax) v = D | (L << 16);
+    }
+    sDL[f][d] = v;
+  }
+  if (tid < F) best_s[tid] = 0ull;
+  if (tid == 0) s_bad = 0;
+  __syncthreads();
+  // ---- fold: F histograms from one read of each sample; kTfBatch samples' loads in flight
+  for (uint32_t k0 = tid; k0 < a.n; k0 += kTfBatch * kTfThreads) {
+    int32_t xq[kTfBatch];
+    ulonglong2 ab[kTfBatch];
+#pragma unroll
+    for (int u = 0; u < kTfBatch; ++u) {
+      const uint32_t k = k0 + u * kTfThreads;
+      xq[u] = k < a.n ? __ldg(Xq + k) : kMaskedQ;
+      ab[u] = k < a.n ? __ldg(ABq + k) : make_ulonglong2(0ull, 0ull);
+    }
+#pragma unroll
+    for (int u = 0; u < kTfBatch; ++u) {
+      if (xq[u] == kMaskedQ) continue;
+      unsigned long long ph = ab[u].x + (unsigned long long)j0 * ab[u].y;
+#pragma unroll
+      for (int f = 0; f < F; ++f) {
+        const uint32_t bin = (uint32_t)(ph >> shift);
+        atomicAdd(hist + 2 * nb * f + bin, (uint32_t)xq[u]);
+        atomicAdd(hist + 2 * nb * f + nb + bin, 1u);
+        ph += ab[u].y;
+      }
+    }
+  }
+  __syncthreads();
+
+  // RM = nb / 512 bins (and starts) a thread; RM = 1 also covers nb < 512, where the threads
+  // past nb hold none
+  const int b0 = tid * RM;
+  const float Nf = (float)a.nv[q];
+#pragma unroll 1
+  for (int f = 0; f < F; ++f) {
+    const uint32_t jf = j0 + f;
+    if (jf >= a.nf) break;
+    const uint32_t *hS = hist + 2 * nb * f, *hC = hS + nb;
+    // ---- moments of this thread's RM bins: counts, flux sums, and their first moments in
+    // u = 2b + 1 (second moment for the counts), scanned over the block
+    uint32_t vc[RM];
+    long long vs[RM];
+    uint32_t tc, ic;
+    long long ts, tcu, tsu, tcu2, is, icu, isu, icu2;
+    auto moments = [&]() {
+      tc = 0; ts = 0; tcu = 0; tsu = 0; tcu2 = 0;
+#pragma unroll
+      for (int r = 0; r < RM; ++r) {
+        const uint32_t u = 2u * (uint32_t)(b0 + r) + 1u;
+        tc += vc[r]; ts += vs[r];
+        tcu += (long long)((unsigned long long)vc[r] * u);
+        tcu2 += (long long)((unsigned long long)vc[r] * (u * u));
+        tsu += vs[r] * (long long)u;
+      }
+      ic = tc; is = ts; icu = tcu; isu = tsu; icu2 = tcu2;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t yc = __shfl_up_sync(0xffffffffu, ic, o);
+        const long long ys = shfl_up_ll(is, o), ycu = shfl_up_ll(icu, o);
+        const long long ysu = shfl_up_ll(isu, o), ycu2 = shfl_up_ll(icu2, o);
+        if (lane >= o) { ic += yc; is += ys; icu += ycu; isu += ysu; icu2 += ycu2; }
+      }
+      if (lane == 31) {
+        wsumc[warp] = ic; wsum[0][warp] = is; wsum[1][warp] = icu; wsum[2][warp] = isu; wsum[3][warp] = icu2;
+      }
+    };
+#pragma unroll
+    for (int r = 0; r < RM; ++r) {
+      const int b = b0 + r;
+      const bool ok = RM > 1 || b < nb;
+      vc[r] = ok ? hC[b] : 0u;
+      vs[r] = ok ? (long long)(int32_t)hS[b] : 0;
+      if (vc[r] >= 2048u) s_bad = 1;  // 32-bit flux sums are exact below 2048 samples a bin
+    }
+    moments();
+    __syncthreads();
+    if (s_bad) {  // rare: refold this frequency's flux sums in 64 bits
+      for (int b = tid; b < nb; b += kTfThreads) S64[b] = 0ull;
+      __syncthreads();
+      for (uint32_t k = tid; k < a.n; k += kTfThreads) {
+        const int32_t xq = __ldg(Xq + k);
+        if (xq == kMaskedQ) continue;
+        const ulonglong2 ab = __ldg(ABq + k);
+        const uint32_t bin = (uint32_t)((ab.x + (unsigned long long)jf * ab.y) >> shift);
+        atomicAdd(S64 + bin, (unsigned long long)(long long)xq);
+      }
+      __syncthreads();
+#pragma unroll
+      for (int r = 0; r < RM; ++r) {
+        const int b = b0 + r;
+        vs[r] = (RM > 1 || b < nb) ? (long long)S64[b] : 0;
+      }
+      moments();
+      __syncthreads();
+    }
+    if (warp == 0) {  // scan of the warp totals
+      uint32_t c = lane < kTfWarps ? wsumc[lane] : 0u;
+      long long v0 = lane < kTfWarps ? wsum[0][lane] : 0, v1 = lane < kTfWarps ? wsum[1][lane] : 0;
+      long long v2 = lane < kTfWarps ? wsum[2][lane] : 0, v3 = lane < kTfWarps ? wsum[3][lane] : 0;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t yc = __shfl_up_sync(0xffffffffu, c, o);
+        const long long y0 = shfl_up_ll(v0, o), y1 = shfl_up_ll(v1, o);
+        const long long y2 = shfl_up_ll(v2, o), y3 = shfl_up_ll(v3, o);
+        if (lane >= o) { c += yc; v0 += y0; v1 += y1; v2 += y2; v3 += y3; }
+      }
+      if (lane < kTfWarps) {
+        wbasec[lane + 1] = c; wbase[0][lane + 1] = v0; wbase[1][lane + 1] = v1;
+        wbase[2][lane + 1] = v2; wbase[3][lane + 1] = v3;
+      }
+      if (lane == 0) { wbasec[0] = 0u; wbase[0][0] = 0; wbase[1][0] = 0; wbase[2][0] = 0; wbase[3][0] = 0; }
+    }
+    __syncthreads();
+    if (tid == 0) s_bad = 0;
+    {
+      // moments of the bins below b0, then the running values at x = b0:
+      // PC = sum C, M1 = sum C (x - b), K = sum C (2(x - b) - 1)^2, and PS, MS1 for the flux
+      const long long c = (long long)(wbasec[warp] + ic - tc);
+      const long long s = wbase[0][warp] + is - ts, cu = wbase[1][warp] + icu - tcu;
+      const long long su = wbase[2][warp] + isu - tsu, cu2 = wbase[3][warp] + icu2 - tcu2;
+      const long long x = b0;
+      long long pc = c, m1 = x * c - ((cu - c) >> 1), kk = 4 * x * x * c - 4 * x * cu + cu2;
+      long long ps = s, ms1 = x * s - ((su - s) >> 1);
+      if (tid == 0) { GSK[0] = make_longlong2(0, 0); Glo[0] = 0u; }
+      longlong2 ent[RM];
+      uint32_t glo[RM];
+#pragma unroll
+      for (int r = 0; r < RM; ++r) {  // x -> x + 1 over bin b0 + r
+        kk += (long long)vc[r] + 8 * m1;
+        pc += vc[r]; m1 += pc;
+        ps += vs[r]; ms1 += ps;
+        ent[r] = pack_entry(2 * ms1 - ps, kk, 2 * m1 - pc);
+        glo[r] = (uint32_t)(2 * m1 - pc);
+      }
+      if (RM == 2 || RM == 4) {
+        // lane-rotated order: each store instruction of a warp hits distinct banks
+#pragma unroll
+        for (int r = 0; r < RM; ++r) {
+          const int c = ((lane >> (RM == 4 ? 1 : 2)) + r) & (RM - 1);
+          const int c2 = ((lane >> (RM == 4 ? 3 : 4)) + r) & (RM - 1);
+          longlong2 v = ent[0];
+          uint32_t w = glo[0];
+#pragma unroll
+          for (int t = 1; t < RM; ++t) {
+            if (c == t) v = ent[t];
+            if (c2 == t) w = glo[t];
+          }
+          GSK[b0 + c + 1] = v;
+          Glo[b0 + c2 + 1] = w;
+        }
+      } else {
+#pragma unroll
+        for (int r = 0; r < RM; ++r)
+          if (RM > 1 || b0 + r < nb) { GSK[b0 + r + 1] = ent[r]; Glo[b0 + r + 1] = glo[r]; }
+      }
+    }
+    const long long Tc = (long long)wbasec[kTfWarps], Ts = wbase[0][kTfWarps];
+    __syncthreads();
+    // extension past nb: entry nb + e from entry e and the full-cycle sums
+    {
+      const longlong2 sn = GSK[nb];
+      const long long gn = entry_g(sn.y, Glo[nb]), kn = entry_k(sn.y);
+      for (int e = tid + 1; e <= (int)a.dmax; e += kTfThreads) {
+        const long long e2 = 2LL * e;
+        const longlong2 se = GSK[e];
+        const long long g = gn + e2 * Tc + entry_g(se.y, Glo[e]);
+        GSK[nb + e] = pack_entry(sn.x + e2 * Ts + se.x, kn + 2 * e2 * gn + e2 * e2 * Tc + entry_k(se.y), g);
+        Glo[nb + e] = (uint32_t)g;
+      }
+    }
+    __syncthreads();
+
+    // ---- templates
+    const float mean = Tc > 0 ? (float)Ts / (float)Tc : 0.0f;
+    float bp = 0.0f;
+    unsigned long long bkey = 0ull;
+    const int nd = (int)a.nd;
+    // start corners of this thread's starts i = tid + 512 r, kept over the durations
+    longlong2 si[RM];
+    uint32_t gi[RM];
+#pragma unroll
+    for (int r = 0; r < RM; ++r) {
+      const int i = min(tid + r * kTfThreads, nb - 1);
+      si[r] = GSK[i];
+      si[r].y = entry_k(si[r].y);
+      gi[r] = Glo[i];
+    }
+    for (int d = 0; d < nd; ++d) {
+      const int DL = sDL[f][d];
+      if (!DL) continue;
+      const int D = DL & 0xffff, L = DL >> 16;
+      const long long L4 = 4LL * L;
+#pragma unroll
+      for (int r = 0; r < RM; ++r) {
+        const int i = tid + r * kTfThreads;
+        if (RM == 1 && i >= nb) break;
+        const int e1 = i + L, e2 = i + D - L, e3 = i + D;
+        const longlong2 c1 = GSK[e1], c2 = GSK[e2], c3 = GSK[e3];
+        const uint32_t l1 = Glo[e1], l2 = Glo[e2];
+        // sum C w < dmax N < 2^32: exact in 32-bit wrap-around arithmetic
+        const uint32_t A2 = gi[r] - l1 - l2 + Glo[e3];
+        const long long N2 = si[r].x - c1.x - c2.x + c3.x;
+        const long long B4 = entry_k(c3.y) - entry_k(c2.y) + entry_k(c1.y) - si[r].y -
+                             L4 * (entry_g(c1.y, l1) + entry_g(c2.y, l2));
+        const float a2 = (float)A2;
+        const float num = i64_to_f32(N2) - mean * a2;
+        const float den = Nf * i64_to_f32(B4) - a2 * a2;
+        const float nn = num * num;
+        // cannot reach bp (the margin covers the rounding of the test): most templates stop here
+        if (!(den > 0.0f) || !(nn >= bp * den * 0.99999f)) continue;
+        const float p = nn / den;
+        const unsigned long long key = ((unsigned long long)__float_as_uint(p) << 32) |
+                                       (0xffffffffu - (((unsigned)d << 24) | (unsigned)i));
+        if (key > bkey) { bkey = key; bp = p; }
+      }
+    }
+    // block argmax: larger TSR, then lower (d, i)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long ok = __shfl_xor_sync(0xffffffffu, bkey, o);
+      bkey = ok > bkey ? ok : bkey;
+    }
+    if (lane == 0 && bkey) atomicMax(&best_s[f], bkey);
+    __syncthreads();
+    if (tid == 0) {  // the moment arrays stay intact until the next frequency's first barrier
+      const size_t o = (size_t)q * a.nf + jf;
+      const unsigned long long k = best_s[f];
+      if (!k) {
+        a.tsr[o] = 0.0f; a.depth[o] = 0.0f; a.start[o] = 0u; a.dur[o] = 0u;
+      } else {
+        const unsigned di = 0xffffffffu - (unsigned)(k & 0xffffffffull);
+        const int d = (int)(di >> 24), i = (int)(di & 0xffffffu);
+        const int DL = sDL[f][d], D = DL & 0xffff, L = DL >> 16;
+        const int e1 = i + L, e2 = i + D - L, e3 = i + D;
+        const longlong2 c0 = GSK[i], c1 = GSK[e1], c2 = GSK[e2], c3 = GSK[e3];
+        const long long g1 = entry_g(c1.y, Glo[e1]), g2 = entry_g(c2.y, Glo[e2]);
+        const long long A2 = entry_g(c0.y, Glo[i]) - g1 - g2 + entry_g(c3.y, Glo[e3]);
+        const long long N2 = c0.x - c1.x - c2.x + c3.x;
+        const long long B4 = entry_k(c3.y) - entry_k(c2.y) + entry_k(c1.y) - entry_k(c0.y) - 4LL * L * (g1 + g2);
+        const double num = (double)N2 - (double)mean * (double)A2;
+        const double den = (double)Nf * (double)B4 - (double)A2 * (double)A2;
+        const double sc = ldexp(1.0, -a.sx[q]);
+        a.tsr[o] = (float)(sqrt((double)__uint_as_float((unsigned)(k >> 32))) * sc);
+        a.depth[o] = (float)(-num * (double)Nf * (2.0 * L) / den * sc);
+        a.start[o] = (uint32_t)i;
+        a.dur[o] = (uint32_t)d;
+      }
     }
   }
 }
 
-size_t tf_smem(uint32_t nb, uint32_t dmax) {
-  const size_t E = (size_t)nb + dmax + 1;
-  const size_t prefix = E * (4 * 8 + 4);
-  const size_t hist = (size_t)nb * 8 + (size_t)nb * 8;  // two 32-bit words + 64-bit refold
-  return gtrap::align256(prefix > hist ? prefix : hist);
+size_t tf_pbytes(uint32_t nb, uint32_t dmax) {
+  return ((size_t)nb + dmax + 1) * 20 + 15 & ~size_t(15);
+}
+
+size_t tf_smem(uint32_t nb, uint32_t dmax, int F) {
+  return tf_pbytes(nb, dmax) + (size_t)(F - 1) * 8 * nb;
+}
+
+using TfKernel = void (*)(TfArgs);
+
+// nb = 4096 (8 bins a thread) leaves no room for a second histogram at two blocks an SM
+TfKernel tf_kernel(int F, int rm) {
+  static const TfKernel table[kTfMaxF][4] = {
+      {tlsfold_kernel<1, 1>, tlsfold_kernel<1, 2>, tlsfold_kernel<1, 4>, tlsfold_kernel<1, 8>},
+      {tlsfold_kernel<2, 1>, tlsfold_kernel<2, 2>, tlsfold_kernel<2, 4>, nullptr},
+      {tlsfold_kernel<3, 1>, tlsfold_kernel<3, 2>, tlsfold_kernel<3, 4>, nullptr}};
+  return table[F - 1][rm == 1 ? 0 : rm == 2 ? 1 : rm == 4 ? 2 : 3];
 }
 
 }  // namespace
@@ -273,7 +412,6 @@ int gtrap_tls_fold(float *tsr, uint32_t *start, uint32_t *dur, float *depth, con
   if (nd == 0 || nd > (uint32_t)kTfMaxDur) return fail(GTRAP_ERR_INVALID_ARG, "tls_fold: nd=%u must be in [1, %d]", nd, kTfMaxDur);
   if (dmax < 2 || dmax > nb) return fail(GTRAP_ERR_INVALID_ARG, "tls_fold: dmax=%u must be in [2, nb]", dmax);
   if (!(lfrac > 0.0f) || lfrac > 0.5f) return fail(GTRAP_ERR_INVALID_ARG, "tls_fold: lfrac must be in (0, 0.5]");
-  if ((uint64_t)nq * nf >= (1ull << 31)) return fail(GTRAP_ERR_INVALID_ARG, "tls_fold: nq*nf too large");
   if (!workspace || ((uintptr_t)workspace & 255))
     return fail(GTRAP_ERR_WORKSPACE, "tls_fold: workspace must be a 256-byte aligned device pointer");
   if (workspace_bytes < gtrap_tls_fold_workspace_size(n, nq))
@@ -288,12 +426,34 @@ int gtrap_tls_fold(float *tsr, uint32_t *start, uint32_t *dur, float *depth, con
   TfArgs a;
   a.X = X; a.AB = AB; a.sx = sx; a.nv = nv;
   a.n = n; a.nq = nq; a.nf = nf; a.nb = nb; a.dmax = dmax; a.nd = nd; a.lognb = ilog2u(nb);
+  a.pbytes = (uint32_t)tf_pbytes(nb, dmax);
   a.fmin = fmin; a.df = df; a.lfrac = lfrac;
   for (uint32_t d = 0; d < (uint32_t)kTfMaxDur; ++d) a.W[d] = d < nd ? durations[d] : 0.0f;  // host array
   a.tsr = tsr; a.depth = depth; a.start = start; a.dur = dur;
-  const size_t smem = tf_smem(nb, dmax);
-  GTRAP_TRY(ensure_smem((const void *)tlsfold_kernel, smem, "tls_fold"));
-  tlsfold_kernel<<<(unsigned)(nq * nf), kTfThreads, smem, stream>>>(a);
+  const int rm = nb >= 4096 ? 8 : nb >= 2048 ? 4 : nb >= 1024 ? 2 : 1;
+  // frequencies per block: the most (up to 3) that still keep two blocks on an SM, else 1
+  int F = 1;
+#ifdef GTRAP_TF_F
+  F = rm == 8 ? 1 : GTRAP_TF_F;
+#else
+  for (int c = kTfMaxF; c >= 2; --c) {
+    const TfKernel k = tf_kernel(c, rm);
+    if (!k) continue;
+    if (ensure_smem((const void *)k, tf_smem(nb, dmax, c), "tls_fold") != GTRAP_OK) continue;
+    int nblk = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nblk, k, kTfThreads, tf_smem(nb, dmax, c)) != cudaSuccess) {
+      cudaGetLastError();
+      continue;
+    }
+    if (nblk >= 2) { F = c; break; }
+  }
+#endif
+  a.ngroups = (nf + F - 1) / F;
+  if ((uint64_t)nq * a.ngroups >= (1ull << 31)) return fail(GTRAP_ERR_INVALID_ARG, "tls_fold: nq*nf too large");
+  const TfKernel k = tf_kernel(F, rm);
+  const size_t smem = tf_smem(nb, dmax, F);
+  GTRAP_TRY(ensure_smem((const void *)k, smem, "tls_fold"));
+  k<<<(unsigned)(nq * a.ngroups), kTfThreads, smem, stream>>>(a);
   return check_launch("tlsfold_kernel");
 }
 

@@ -337,6 +337,10 @@ int gtrap_probe_fp32_peak(float *sink, uint32_t iters, double *flops, gtrap_stre
  * (two 32-bit atomic adds to random bins) updates the launch performs. */
 int gtrap_probe_smem_atomic_peak(unsigned *sink, uint32_t iters, double *updates, gtrap_stream_t stream);
 
+/* Shared-memory load bandwidth (conflict-free 64-bit loads): *bytes receives the bytes the
+ * launch reads.  sink: at least 2 * SM-count words. */
+int gtrap_probe_smem_load_peak(unsigned long long *sink, uint32_t iters, double *bytes, gtrap_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -21,11 +21,7 @@ def _case(nq=4, n=3000, seed=3300):
     return lc, tu, off, inj
 
 
-@pytest.mark.parametrize("nb,lfrac,dmax", [(256, 0.2, 128), (512, 0.5, 256), (1024, 0.1, 400)])
-def test_tls_fold_matches_oracle(cuda, nb, lfrac, dmax):
-    lc, tu, off, inj = _case()
-    nf, fmin = 48, 1.0 / 12.0
-    df = (2.0 - fmin) / (nf - 1)
+def _check(cuda, lc, tu, off, nf, nb, fmin, df, lfrac, dmax):
     d = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
     tsr, st, du, dep = (x.cpu().numpy() for x in api.tls_fold(d(lc), d(tu), d(off), nf, nb, fmin, df, W,
                                                             lfrac=lfrac, dmax=dmax))
@@ -40,6 +36,27 @@ def test_tls_fold_matches_oracle(cuda, nb, lfrac, dmax):
         assert abs(p - opmax[q, j]) <= 1e-5 * opmax[q, j], (q, j, p, opmax[q, j])
     same = ok & (st == ost) & (du == odu)
     np.testing.assert_allclose(dep[same], odep[same], rtol=1e-3, atol=1e-7)
+
+
+# nb 256 / 512 / 1024 / 2048 / 4096 cover one to eight bins a thread; nf = 47 leaves a partial
+# group of frequencies per block
+@pytest.mark.parametrize("nb,lfrac,dmax,nf", [(256, 0.2, 128, 48), (512, 0.5, 256, 48), (1024, 0.1, 400, 48),
+                                              (2048, 0.2, 1024, 47), (4096, 0.25, 2048, 20)])
+def test_tls_fold_matches_oracle(cuda, nb, lfrac, dmax, nf):
+    lc, tu, off, inj = _case()
+    fmin = 1.0 / 12.0
+    df = (2.0 - fmin) / (nf - 1)
+    _check(cuda, lc, tu, off, nf, nb, fmin, df, lfrac, dmax)
+
+
+def test_tls_fold_dense_bins_refold(cuda):
+    """Samples crowded into a few bins (2048 or more in one bin) take the 64-bit refold."""
+    rng = np.random.default_rng(5)
+    n, nq = 6000, 2
+    tu = np.sort(rng.uniform(0.0, 0.02, (n, nq)), axis=0).astype(np.float32)
+    lc = rng.normal(0, 1e-3, (n, nq)).astype(np.float32)
+    lc[n // 3: n // 2] -= 4e-3
+    _check(cuda, lc, tu, np.zeros(nq, np.float32), 12, 256, 1.0 / 12.0, 0.05, 0.25, 128)
 
 
 def test_tls_fold_recovers_injected_period(cuda):
