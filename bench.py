@@ -806,11 +806,11 @@ def run_tlsfold(args, rank, world, local_rank):
                "ms_per_step": float(ems[0]), "api": "gtrap_gb300.api.tls_fold with pinned host buffers"}
     if rank != 0:
         return
-    # roofline: the template phase reads the moment arrays from shared memory; per template
-    # G (low words at three corners, high words at two), GS and K at three corners = 68 B,
+    # roofline: the template phase reads the moment entries from shared memory; per template
+    # three corners of 16 + 4 bytes (GS, K with the high word of G, low word of G) = 60 B,
     # plus 20 B per start bin and frequency for the start corner
     tpl = float(tlsfold_valid_templates().sum()) * nq * TF_NB
-    lds_bytes = tpl * 68.0 + float(evals) * TF_NB * 20.0
+    lds_bytes = tpl * 60.0 + float(evals) * TF_NB * 20.0
     speak = smem_load_peak(dev)
     achieved = lds_bytes / (ms / 1e3)
     nv = float(np.count_nonzero(np.isfinite(lcn) & (tun >= 0)))
@@ -830,7 +830,7 @@ def run_tlsfold(args, rank, world, local_rank):
                          "frac": achieved / speak, "traffic": traffic,
                          "kernel": "tlsfold_kernel (fold + moment arrays + templates)",
                          "kernel_ms": ms, "templates_per_step": tpl,
-                         "algorithmic_bytes": "68 B of shared-memory loads per template + 20 B per "
+                         "algorithmic_bytes": "60 B of shared-memory loads per template + 20 B per "
                                               "start bin and frequency",
                          "peak_source": "live probe: conflict-free 64-bit shared-memory loads",
                          "fold": fold_leg},

@@ -293,7 +293,7 @@ __global__ void __launch_bounds__(kTfThreads, 2) tlsfold_kernel(const TfArgs a) 
 
     // ---- templates
     const float mean = Tc > 0 ? (float)Ts / (float)Tc : 0.0f;
-    float bp = 0.0f;
+    float bp = 0.0f, thr = 0.0f;  // thr = bp less a margin that covers the rounding of the test
     unsigned long long bkey = 0ull;
     const int nd = (int)a.nd;
     // start corners of this thread's starts i = tid + 512 r, kept over the durations
@@ -303,7 +303,6 @@ __global__ void __launch_bounds__(kTfThreads, 2) tlsfold_kernel(const TfArgs a) 
     for (int r = 0; r < RM; ++r) {
       const int i = min(tid + r * kTfThreads, nb - 1);
       si[r] = GSK[i];
-      si[r].y = entry_k(si[r].y);
       gi[r] = Glo[i];
     }
     for (int d = 0; d < nd; ++d) {
@@ -321,18 +320,18 @@ __global__ void __launch_bounds__(kTfThreads, 2) tlsfold_kernel(const TfArgs a) 
         // sum C w < dmax N < 2^32: exact in 32-bit wrap-around arithmetic
         const uint32_t A2 = gi[r] - l1 - l2 + Glo[e3];
         const long long N2 = si[r].x - c1.x - c2.x + c3.x;
-        const long long B4 = entry_k(c3.y) - entry_k(c2.y) + entry_k(c1.y) - si[r].y -
-                             L4 * (entry_g(c1.y, l1) + entry_g(c2.y, l2));
+        // sum C w^2 < N dmax^2 < 2^44: exact modulo 2^48, so the packed words combine directly
+        const long long B4 = (long long)(((unsigned long long)(c3.y - c2.y + c1.y - si[r].y) -
+                                          (unsigned long long)(L4 * (entry_g(c1.y, l1) + entry_g(c2.y, l2)))) & kM48);
         const float a2 = (float)A2;
         const float num = i64_to_f32(N2) - mean * a2;
         const float den = Nf * i64_to_f32(B4) - a2 * a2;
         const float nn = num * num;
-        // cannot reach bp (the margin covers the rounding of the test): most templates stop here
-        if (!(den > 0.0f) || !(nn >= bp * den * 0.99999f)) continue;
+        if (!(nn >= thr * den) || !(den > 0.0f)) continue;  // cannot reach bp: most stop here
         const float p = nn / den;
         const unsigned long long key = ((unsigned long long)__float_as_uint(p) << 32) |
                                        (0xffffffffu - (((unsigned)d << 24) | (unsigned)i));
-        if (key > bkey) { bkey = key; bp = p; }
+        if (key > bkey) { bkey = key; bp = p; thr = p * 0.99999f; }
       }
     }
     // block argmax: larger TSR, then lower (d, i)
