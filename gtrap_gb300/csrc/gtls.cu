@@ -82,8 +82,28 @@ __device__ __forceinline__ float df_diff(float bh, float bl, float ah, float al)
   return __fadd_rn(__fsub_rn(bh, ah), __fsub_rn(bl, al));
 }
 
-__device__ __forceinline__ double df_diff_d(float bh, float bl, float ah, float al) {
-  return ((double)bh - (double)ah) + ((double)bl - (double)al);
+// sum of squares about m over a window, Q - 2 m Sx + m^2 N, in double-float arithmetic
+// (about 2^-45 relative before the final rounding; the FP64 pipe is narrow on this part).
+// Q = (bh + bl) - (ah + al) from the prefix of x^2.
+__device__ __forceinline__ float df_sumsq(float bh, float bl, float ah, float al, float m, float sx, int n) {
+  auto two_sum = [](float a, float b, float &e) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return s;
+  };
+  float e1;
+  const float q = two_sum(bh, -ah, e1);
+  const float ql = __fadd_rn(e1, __fsub_rn(bl, al));
+  const float m2 = __fmul_rn(2.0f, m);
+  const float t = __fmul_rn(m2, sx), tl = __fmaf_rn(m2, sx, -t);   // 2 m Sx exactly
+  const float mm = __fmul_rn(m, m), mml = __fmaf_rn(m, m, -mm);      // m^2 exactly
+  const float nf = (float)n;
+  const float u = __fmul_rn(mm, nf), ul = __fmaf_rn(mm, nf, -u) + mml * nf;  // m^2 N
+  float e2, e3;
+  const float s2 = two_sum(q, -t, e2);
+  const float s3 = two_sum(s2, u, e3);
+  return __fadd_rn(s3, ((e3 + e2) + (ql - tl)) + ul);
 }
 
 // kTE consecutive epochs [e0, e0 + kTE) of one curve, by the whole block.
@@ -114,7 +134,8 @@ __device__ __forceinline__ void gtls_tile(const TlsArgs &a, const int e0) {
   for (int s = tid; s < S; s += kTlsThreads) {
     const size_t idx = (size_t)(base + s) * a.stride;
     const float tr = __ldg(a.tu + idx);
-    const float tqv = __fadd_rn(-1000.0f, __double2float_rn((double)tr + 1000.0));
+    // tr + 1000 is exact in double, so one float rounding of it is the float sum
+    const float tqv = __fadd_rn(-1000.0f, __fadd_rn(tr, 1000.0f));
     const float x = __ldg(a.lc + idx);
     const bool ok = tqv >= 0.0f;
     tq[s] = ok ? tqv : -INFINITY;
@@ -263,9 +284,7 @@ __device__ __forceinline__ void gtls_tile(const TlsArgs &a, const int e0) {
     const int Nw = cnt[ubE] - cnt[lbS];
     const float m = Nw > 0 ? __fdiv_rn(df_diff(pxh[ubE], pxl[ubE], pxh[lbS], pxl[lbS]), (float)Nw) : 0.0f;
     const float SxAE = df_diff(pxh[ubE], pxl[ubE], pxh[ubS], pxl[ubS]);
-    const double SS = df_diff_d(pqh[ubE], pql[ubE], pqh[ubS], pql[ubS]) -
-                      2.0 * (double)m * (double)SxAE + (double)m * (double)m * (double)N;
-    const float SSf = (float)SS;
+    const float SSf = df_sumsq(pqh[ubE], pql[ubE], pqh[ubS], pql[ubS], m, SxAE, N);
     const double Wd = (double)W;
     const float dl = a.mode ? __double2float_rn(Wd / 4.0 / (double)nl)
                             : __double2float_rn(Wd * 0.45 / (double)nl);
@@ -277,9 +296,10 @@ __device__ __forceinline__ void gtls_tile(const TlsArgs &a, const int e0) {
     float xD = 0.f, vD = 0.f, xvD = 0.f, vvD = 0.f;
     for (int mm = 0; mm < nl; ++mm) {
       const float L = __fmul_rn((float)(a.mode ? mm + 1 : mm), dl);
-      const double Ld = (double)L;
-      const float tAB = __double2float_rn(-Wd * 0.25 - Ld * 0.5);
-      const float tBC = __double2float_rn(-Wd * 0.25 + Ld * 0.5);
+      // the reference's -W*0.25 -+ L*0.5 (double literals, float result): both terms are exact
+      // floats and their double sum is exact, so one float add rounds the same
+      const float tAB = __fsub_rn(-0.25f * W, 0.5f * L);
+      const float tBC = __fadd_rn(-0.25f * W, 0.5f * L);
       const float tCD = -tBC, tDE = -tAB;
       while (bL > lo && tt(bL - 1) > tAB) {
         --bL;
