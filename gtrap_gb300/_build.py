@@ -24,6 +24,8 @@ LIBNAME = "libgtrap_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
               "-diag-suppress", "550"]
+# the gamma sampler reproduces the reference's fast-math SourceModule build bit for bit
+FILE_FLAGS = {"gamma.cu": ["-use_fast_math"]}
 
 
 def nvcc() -> str:
@@ -80,8 +82,8 @@ def build(force: bool = False, verbose: bool = False, extra_flags=(), lib: Path 
     for src in _sources():
         obj = objdir / (src.stem + ".o")
         objs.append(obj)
-        jobs.append([cc, *ARCH, *NVCC_FLAGS, *extra_flags, "-I", str(INCLUDE), "-c", str(src),
-                     "-o", str(obj)])
+        jobs.append([cc, *ARCH, *NVCC_FLAGS, *FILE_FLAGS.get(src.name, []), *extra_flags, "-I",
+                     str(INCLUDE), "-c", str(src), "-o", str(obj)])
     workers = max(1, min(len(jobs), os.cpu_count() or 4))
     with cf.ThreadPoolExecutor(workers) as ex:
         for res in ex.map(_run, jobs):

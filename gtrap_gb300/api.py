@@ -330,3 +330,70 @@ def tls_fold(lc, tu, offset_, nf, nb, fmin, df, durations, *, lfrac=0.2, dmax=No
            w.ctypes.data_as(C.c_void_p), int(w.size), float(lfrac), int(dmax), as_ptr(ws), ws.numel(),
            stream_handle(stream))
     return tsr, st, du, dep
+
+
+# ---------------------------------------------------------------------------- mock injection
+
+TRANSIT_PARAMS = _np.dtype([(k, "<f8") for k in ("t0", "per", "rp", "a", "inc", "ecc", "w", "u1", "u2",
+                                                  "amp_sin", "amp_dcos")])
+
+
+def _transit_record(p) -> _np.ndarray:
+    rec = _np.zeros(1, TRANSIT_PARAMS)
+    for k in TRANSIT_PARAMS.names:
+        if k in p:
+            rec[k] = p[k]
+    return rec
+
+
+def transit_flux(t: torch.Tensor, params, stream=None) -> torch.Tensor:
+    """batman-style quadratic limb-darkening transit model at times ``t`` (float64 device
+    tensor) for one parameter set (a mapping with the fields of ``TRANSIT_PARAMS``):
+    gentransit's light curve (gtrap/genmock.py:9-34)."""
+    require_cuda()
+    t = t.contiguous()
+    if t.dtype != torch.float64:
+        raise TypeError("t must be float64")
+    rec = _transit_record(params)
+    out = torch.empty_like(t)
+    N.call("gtrap_transit_flux", as_ptr(out), as_ptr(t), int(t.numel()), rec.ctypes.data_as(C.c_void_p),
+           stream_handle(stream))
+    return out
+
+
+def inject_transit(lc: torch.Tensor, tu: torch.Tensor, params, *, mode=0, off=None, n=None, stride=None,
+                   stream=None) -> torch.Tensor:
+    """Inject one model per curve into ``lc`` in place (samples with tu > 0): mode 0
+    multiplies by the model (the Kepler mock driver), mode 1 by 2 - model, then adds the
+    trend terms (the TESS mock driver).  ``params`` is a ``TRANSIT_PARAMS`` array with one
+    record per curve; ``lc``/``tu`` an ``[n, nq]`` image or packed arrays with ``off``/``n``."""
+    require_cuda()
+    lc = _f32(lc, "lc")
+    tu = _f32(tu, "tu")
+    dev = lc.device
+    if off is None:
+        nt, nq = lc.shape
+        off = torch.arange(nq, dtype=torch.int64, device=dev)
+        n = torch.full((nq,), nt, dtype=torch.int32, device=dev)
+        stride = nq
+    prm = _np.ascontiguousarray(params, dtype=TRANSIT_PARAMS)
+    nc = int(off.numel())
+    if prm.size != nc:
+        raise ValueError("need one parameter record per curve (%d != %d)" % (prm.size, nc))
+    dprm = torch.from_numpy(prm.view(_np.uint8).copy()).to(dev)
+    max_n = int(n.max()) if nc else 0
+    N.call("gtrap_inject_transit", as_ptr(lc), as_ptr(tu), as_ptr(off), as_ptr(n), int(stride), nc, max_n,
+           as_ptr(dprm), int(mode), stream_handle(stream))
+    return lc
+
+
+def gamma_sample(count: int, alpha: float, beta: float, *, seed: int = 10, first_id: int = 0, device="cuda",
+                 stream=None):
+    """``count`` Gamma(alpha, rate beta) variates, variate i drawn as the reference's gammagen
+    draws id first_id + i (gtrap/ggenmock.py:18-79).  Returns (x, number of failed variates)."""
+    require_cuda()
+    x = torch.empty(count, dtype=torch.float32, device=device)
+    nfail = torch.zeros(1, dtype=torch.int32, device=device)
+    N.call("gtrap_gamma_sample", as_ptr(x), int(count), float(alpha), float(beta), int(seed), int(first_id),
+           as_ptr(nfail), stream_handle(stream))
+    return x, nfail

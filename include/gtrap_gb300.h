@@ -337,6 +337,45 @@ int gtrap_probe_fp32_peak(float *sink, uint32_t iters, double *flops, gtrap_stre
  * (two 32-bit atomic adds to random bins) updates the launch performs. */
 int gtrap_probe_smem_atomic_peak(unsigned *sink, uint32_t iters, double *updates, gtrap_stream_t stream);
 
+/* ---- mock injection (gtrap/genmock.py:9-43, gtrap/ggenmock.py:18-79) ------------------ */
+
+/* One transit model: batman's quadratic limb-darkening transit (Kreidberg 2015) with the
+ * trend terms of the TESS mock driver.  Times in days on the light curve's own axis; angles
+ * in degrees; rp and a in stellar radii.  88 bytes. */
+typedef struct gtrap_transit_params {
+  double t0;       /* time of inferior conjunction */
+  double per;      /* orbital period */
+  double rp;       /* planet radius / stellar radius */
+  double a;        /* semi-major axis / stellar radius */
+  double inc;      /* inclination (degrees) */
+  double ecc;      /* eccentricity, [0, 1) */
+  double w;        /* argument of periastron (degrees) */
+  double u1, u2;   /* quadratic limb darkening */
+  double amp_sin;  /* trend amp_sin sin(2 pi (t - t0) / per), added after the transit */
+  double amp_dcos; /* trend -amp_dcos cos(4 pi (t - t0) / per) */
+} gtrap_transit_params;
+
+/* flux[k] = model(t[k]) for one parameter record (host pointer); t and flux are device
+ * arrays of n doubles (gentransit's light curve, gtrap/genmock.py:9-34). */
+int gtrap_transit_flux(double *flux, const double *t, uint32_t n, const gtrap_transit_params *params,
+                       gtrap_stream_t stream);
+
+/* Inject params[q] (device array) into curve q: rows k < n[q] at lc[off[q] + k * stride]
+ * with tu > 0.  mode 0: lc *= F (kepler/gtls_mockkepler.py:204-205); mode 1: lc *= 2 - F
+ * (works/sp/gtls_slctess.py:40-42); then the trend terms when non-zero
+ * (works/sp/gtls_slctess.py:44-50).  A record outside the model's domain (per <= 0, a <= 0,
+ * rp < 0, ecc outside [0, 1)) leaves its curve unchanged. */
+int gtrap_inject_transit(float *lc, const float *tu, const uint64_t *off, const uint32_t *n, uint64_t stride,
+                         uint32_t ncurves, uint32_t max_n, const gtrap_transit_params *params, int32_t mode,
+                         gtrap_stream_t stream);
+
+/* count Gamma(alpha, rate beta) variates, variate i from curand_init(seed, first_id + i, 0):
+ * the reference's gammagen (seed 10, one id per block, gtrap/ggenmock.py:18-79) bit for bit.
+ * A variate that exceeds the reference's 10000 tries is 0 and counted in *nfail (device
+ * counter, optional). */
+int gtrap_gamma_sample(float *x, uint32_t count, float alpha, float beta, uint64_t seed, uint64_t first_id,
+                       uint32_t *nfail, gtrap_stream_t stream);
+
 /* Shared-memory load bandwidth (conflict-free 64-bit loads): *bytes receives the bytes the
  * launch reads.  sink: at least 2 * SM-count words. */
 int gtrap_probe_smem_load_peak(unsigned long long *sink, uint32_t iters, double *bytes, gtrap_stream_t stream);

@@ -5,7 +5,7 @@ The reference compiles its CUDA kernels at run time through PyCUDA ``SourceModul
 sources where they lie in the reference checkout -- ``include/geebls.h``,
 ``include/gtls_simple.h``, ``include/gtls_absolute.h`` and the source strings passed to
 ``SourceModule`` in ``gtrap/geebls_simple.py``, ``gtrap/gfilter.py`` and
-``gtrap/getstat.py`` -- wraps each in its own namespace with the ``#define``s of its
+``gtrap/getstat.py`` and ``gtrap/ggenmock.py`` -- wraps each in its own namespace with the ``#define``s of its
 module (``gtrap/geebls.py:14-15``, ``gtrap/gtls.py:20-22``, ``gtrap/gfilter.py:12``) and
 plain ``extern "C"`` launchers, and writes ``oracle/_ref/ref_kernels.cu`` (git-ignored,
 never committed).  ``build()`` compiles it with ``nvcc -use_fast_math`` for sm_103a into
@@ -78,6 +78,10 @@ int ref_gfilter(float *in, float *out, int i_dim, int j_dim, int r, int nbx, int
                             (cudaStream_t)stream>>>(in, out, i_dim, j_dim, r);
   return (int)cudaGetLastError();
 }
+int ref_gammagen(float *x, float ain, float bin, int nt, int nq, void *stream) {
+  ref_gamma::gammagen<<<dim3(nt, nq), dim3(1), 0, (cudaStream_t)stream>>>(x, ain, bin);
+  return (int)cudaGetLastError();
+}
 int ref_getmax(float *blsp, unsigned *p1, unsigned *p2, float *maxval, unsigned *maxidx,
                float *avesum, float *varsum, unsigned *mp1, unsigned *mp2, int nthread, int npatch,
                int nq, void *stream) {
@@ -95,10 +99,12 @@ def generate(reference: Path = DEFAULT_REFERENCE) -> Path:
     simple = _source_module_strings(reference / "gtrap" / "geebls_simple.py")[0]
     gfil = _source_module_strings(reference / "gtrap" / "gfilter.py")[0]
     gstat = _source_module_strings(reference / "gtrap" / "getstat.py")[0]
+    gamma = _source_module_strings(reference / "gtrap" / "ggenmock.py")[0]
     parts = [
         "// GENERATED by oracle/make_ref.py from the reference kernel sources.",
         "// Test harness only: never committed, never linked into the product.",
         "#include <cuda_runtime.h>",
+        "#include <curand_kernel.h>",
         "#include <stdio.h>",
         "namespace ref_full {",
         "#define MINBIN 5",
@@ -127,6 +133,9 @@ def generate(reference: Path = DEFAULT_REFERENCE) -> Path:
         "}",
         "namespace ref_getstat {",
         _strip_includes(gstat),
+        "}",
+        "namespace ref_gamma {",
+        _strip_includes(gamma),
         "}",
         LAUNCHERS,
     ]

@@ -36,7 +36,9 @@ def _load():
         lib.ref_gtls.argtypes = [i] + [vp] * 7 + [i, i, i, f, f, f, f, f, i, i, i, vp]
         lib.ref_gfilter.argtypes = [vp, vp, i, i, i, i, i, i, vp]
         lib.ref_getmax.argtypes = [vp] * 9 + [i, i, i, vp]
-        for fn in (lib.ref_geebls, lib.ref_geebls_simple, lib.ref_gtls, lib.ref_gfilter, lib.ref_getmax):
+        lib.ref_gammagen.argtypes = [vp, f, f, i, i, vp]
+        for fn in (lib.ref_geebls, lib.ref_geebls_simple, lib.ref_gtls, lib.ref_gfilter, lib.ref_getmax,
+                   lib.ref_gammagen):
             fn.restype = C.c_int
         _lib = lib
     return _lib
@@ -114,3 +116,15 @@ def gfilter(x, r, nby=1000, nbx=1):
            "gfilter")
     torch.cuda.synchronize()
     return d_out.cpu().numpy().reshape(n, nq)
+
+
+def gammagen(nt, alpha, beta, nq=1):
+    """The reference's gammagen (gtrap/ggenmock.py:18-79, grid (nt, nq), one thread a block)
+    into a zeroed array of nt floats, as its driver does (gtrap/ggenmock.py:104-112)."""
+    import torch
+    lib = _load()
+    x = torch.zeros(nt, dtype=torch.float32, device="cuda")
+    _check(lib.ref_gammagen(C.c_void_p(x.data_ptr()), float(alpha), float(beta), int(nt), int(nq), _stream()),
+           "gammagen")
+    torch.cuda.synchronize()
+    return x.cpu().numpy()
