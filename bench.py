@@ -23,7 +23,8 @@ in the reference's semantics on 4096 TESS-like curves x 18,000 epochs (8 widths 
 widths per epoch).  ``--workload tlsfold``: the folded trapezoid search (an extension) on the
 same curves: 8192 periods (0.5 .. 12 d) x 8 durations (0.5 .. 8 h) x 2048 phase bins.
 ``--workload served``: the continuous-batching server under Poisson arrivals (p50/p99
-latency per offered load).
+latency per offered load).  ``--workload mock``: mock transit injection as the TESS mock driver
+does it (one drawn planet per curve, lc *= 2 - model, plus trends) on 4096 x 18,000 samples.
 
 ``--impl reference`` times the reference's algorithm on the host CPU (the FP64 C
 restatement of geebls and gtls with scipy's median filter, all host threads) on a bounded
@@ -67,7 +68,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="ragged",
-                   choices=["ragged", "masked", "served", "plain", "tls", "tlsfold"])
+                   choices=["ragged", "masked", "served", "plain", "tls", "tlsfold", "mock"])
     p.add_argument("--nq", type=int, default=None,
                    help="curves per GPU (default: 10,000 ragged, 1024 masked)")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -872,6 +873,134 @@ def run_tlsfold_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+# ----------------------------------------------------------------------------- mock injection
+
+MOCK_UNIT = "samples/s"
+MOCK_METRIC = "mock transit injection: injected samples/sec"
+
+
+def _hbm_peak_gbs():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (copy)"
+    except Exception:
+        return 6800.0, "fallback 6.8 TB/s"
+
+
+def mock_case(nq, seed):
+    from gtrap_gb300 import mock, synth
+    lcn, tun, _ = synth.tess_like(nq=nq, n=TF_N, seed=seed)
+    lcn = (lcn + np.float32(1.0)).astype(np.float32)  # normalised flux, as the drivers inject into
+    rng = np.random.default_rng(seed + 7)
+    rs = rng.uniform(0.5, 1.5, nq)
+    rec = mock.draw_population(rng, tun, rs, rs ** 1.25, trends=True, lc=lcn)
+    return lcn, tun, rec
+
+
+def mock_cpu_sample(lcn, tun, rec, ncurves):
+    """The oracle's injection (scipy quadrature per in-transit sample), one core."""
+    import oracle.mock as om
+    t0 = time.perf_counter()
+    om.inject(lcn[:, :ncurves], tun[:, :ncurves], rec[:ncurves], mode=1)
+    dt = time.perf_counter() - t0
+    return lcn.shape[0] * ncurves / dt, dt
+
+
+def run_mock(args, rank, world, local_rank):
+    import torch
+    import torch.distributed as dist
+    from gtrap_gb300 import _build, api
+    _build.build()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    stream = torch.cuda.current_stream(dev)
+    nq = args.nq or 4096
+    lcn, tun, rec = mock_case(nq, 6000 + 100000 * rank)
+    lc = torch.from_numpy(lcn).to(dev)
+    tu = torch.from_numpy(tun).to(dev)
+    # in-place injection repeated on the same image: the same samples and transits every step
+    fn = lambda: api.inject_transit(lc, tu, rec, mode=1)
+    ms, clk = _timed(fn, args.steps, args.warmup, dev, world)
+    samples = TF_N * nq
+    e2e = None
+    if not args.no_e2e:
+        h_lc, h_tu = torch.from_numpy(lcn).pin_memory(), torch.from_numpy(tun).pin_memory()
+        h_out = torch.empty_like(h_lc).pin_memory()
+
+        def e2e_step():
+            lc.copy_(h_lc, non_blocking=True)
+            tu.copy_(h_tu, non_blocking=True)
+            fn()
+            h_out.copy_(lc, non_blocking=True)
+
+        e2e_step()
+        torch.cuda.synchronize(dev)
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        for _ in range(args.steps):
+            e2e_step()
+        e.record(stream)
+        torch.cuda.synchronize(dev)
+        ems = torch.tensor([s.elapsed_time(e) / args.steps], device=dev, dtype=torch.float64)
+        if world > 1:
+            dist.all_reduce(ems, op=dist.ReduceOp.MAX)
+        e2e = {"value": samples * world / (float(ems[0]) / 1e3), "unit": MOCK_UNIT,
+               "h2d_bytes_per_step": (h_lc.numel() + h_tu.numel()) * 4, "d2h_bytes_per_step": h_out.numel() * 4,
+               "ms_per_step": float(ems[0]), "api": "gtrap_gb300.api.inject_transit with pinned host buffers"}
+    if rank != 0:
+        return
+    peak, src = _hbm_peak_gbs()
+    nbytes = samples * 12.0  # read lc and tu, write lc
+    achieved = nbytes / (ms / 1e3) / 1e9
+    ph = ((tun - rec["t0"][None, :]) / rec["per"][None, :]) % 1.0
+    dur = np.arcsin(np.minimum(1.0, (1.0 + rec["rp"]) / rec["a"])) / (2 * np.pi)
+    intransit = float(np.mean((np.minimum(ph, 1.0 - ph) < dur[None, :]) & (tun > 0)))
+    line = {"metric": MOCK_METRIC, "value": samples * world / (ms / 1e3), "unit": MOCK_UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "mock injection as the TESS mock driver: %d TESS-like curves x %d samples, "
+                                   "one planet per curve (P ~ P^-5/3 on 3..30 d, Rp 0.2..1 R_J, b uniform), "
+                                   "lc *= 2 - model, sine and double-cosine trends" % (nq, TF_N),
+                       "curves_per_gpu": nq, "in_transit_fraction": intransit,
+                       "l2": "inputs %d MiB per GPU exceed L2" % (2 * nq * TF_N * 4 >> 20),
+                       "parallelism": "replicas x%d (curves sharded)" % world},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": None, "kernel": "inject_kernel", "kernel_ms": ms,
+                         "algorithmic_bytes": "12 B per sample (lc and tu read, lc written)", "peak_source": src},
+            "gpu_launches": args.steps, "clocks": clk}
+    if e2e:
+        line["e2e"] = e2e
+    if not args.no_cpu_baseline:
+        v, dt = mock_cpu_sample(lcn, tun, rec, 16)
+        line["cpu_baseline"] = {"value": v, "unit": MOCK_UNIT, "cores": 1, "kind": "port",
+                                "sample": "16 curves x %d samples through the oracle (scipy quadrature per "
+                                          "in-transit sample), %.1f s" % (TF_N, dt)}
+    print(json.dumps(line), flush=True)
+
+
+def run_mock_reference(args, rank, world):
+    """batman is absent: the oracle port of the injection on one host core."""
+    if rank != 0:
+        return
+    lcn, tun, rec = mock_case(64, 6000)
+    for _ in range(args.warmup):
+        mock_cpu_sample(lcn, tun, rec, 2)
+    vals, total = [], 0.0
+    for _ in range(args.steps):
+        v, dt = mock_cpu_sample(lcn, tun, rec, 8)
+        vals.append(v)
+        total += dt
+    value = float(np.median(vals))
+    line = {"impl": "reference", "metric": MOCK_METRIC, "value": value, "unit": MOCK_UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "mock injection as the TESS mock driver (oracle port; batman is absent)"},
+            "cpu_baseline": {"value": value, "unit": MOCK_UNIT, "cores": 1, "kind": "port",
+                             "sample": "per step 8 curves x %d samples" % TF_N},
+            "e2e": {"value": value, "unit": MOCK_UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
 # ----------------------------------------------------------------------------- served workload
 
 def run_served(args, rank, world, local_rank):
@@ -941,6 +1070,8 @@ def main():
             run_masked_reference(args, rank, world)
         elif args.workload == "tlsfold":
             run_tlsfold_reference(args, rank, world)
+        elif args.workload == "mock":
+            run_mock_reference(args, rank, world)
         else:
             run_ragged_reference(args, rank, world)
         return
@@ -951,7 +1082,7 @@ def main():
         dist.init_process_group("nccl")
     try:
         {"ragged": run_ragged, "masked": run_masked, "served": run_served, "plain": run_image,
-         "tls": run_image, "tlsfold": run_tlsfold}[args.workload](
+         "tls": run_image, "tlsfold": run_tlsfold, "mock": run_mock}[args.workload](
             args, rank, world, local_rank)
     finally:
         if world > 1:

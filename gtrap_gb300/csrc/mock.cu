@@ -18,8 +18,9 @@
 // Injection (per curve, samples with t > 0): mode 0 lc *= F (the Kepler driver), mode 1
 // lc *= 2 - F (the TESS driver); then, when an amplitude is non-zero, the driver's trends
 // lc += amp_sin sin(2 pi (t - t0) / P) - amp_dcos cos(4 pi (t - t0) / P)
-// (gtrap/genmock.py:37-43).  Arithmetic in double, one rounding to float per step as the
-// drivers' float32 arrays do.
+// (gtrap/genmock.py:37-43).  The model in double; the trend terms in float (1e-8 of their
+// amplitude from the double terms); one rounding to float per step as the drivers' float32
+// arrays do.
 #include "common.cuh"
 
 #include <math.h>
@@ -30,11 +31,14 @@ using gtrap::fail;
 
 constexpr int kGl = 32;  // Gauss-Legendre nodes on [-1, 1]
 
+// Nodes of the partial-circle integral in phi in [0, pi/2]: s2 = sin^2(phi) and the weight
+// times d(sin^2 phi)/d phi = sin(2 phi)
 struct GlRule {
-  double x[kGl], w[kGl];
+  double s2[kGl], wj[kGl];
 };
 
-// Legendre roots by Newton's method from the Chebyshev guesses, weights 2 / ((1 - x^2) P'^2)
+// Legendre roots by Newton's method from the Chebyshev guesses, weights 2 / ((1 - x^2) P'^2),
+// mapped to phi = pi/4 (x + 1)
 GlRule make_gl() {
   GlRule g;
   for (int i = 0; i < kGl; ++i) {
@@ -51,8 +55,9 @@ GlRule make_gl() {
       x -= dx;
       if (fabs(dx) < 1e-15) break;
     }
-    g.x[i] = x;
-    g.w[i] = 2.0 / ((1.0 - x * x) * dp * dp);
+    const double w = 2.0 / ((1.0 - x * x) * dp * dp), phi = 0.25 * M_PI * (x + 1.0);
+    g.s2[i] = sin(phi) * sin(phi);
+    g.wj[i] = 0.25 * M_PI * w * sin(2.0 * phi);
   }
   return g;
 }
@@ -92,19 +97,19 @@ __device__ double occulted(double p, double z, double u1, double u2, const GlRul
     const double D = rb - ra, z2p2 = z * z - p * p;
     double acc = 0.0;
     for (int k = 0; k < kGl; ++k) {
-      const double phi = 0.25 * M_PI * (gl.x[k] + 1.0);
-      const double s = sin(phi);
-      const double r = ra + D * s * s;
+      const double r = ra + D * gl.s2[k];
       const double c = fmin(1.0, fmax(-1.0, (r * r + z2p2) / (2.0 * r * z)));
-      acc += gl.w[k] * intensity(r, u1, u2) * 2.0 * acos(c) * r * D * sin(2.0 * phi);
+      acc += gl.wj[k] * intensity(r, u1, u2) * acos(c) * r;
     }
-    occ += 0.25 * M_PI * acc;
+    occ += 2.0 * D * acc;
   }
   return occ / total;
 }
 
 struct Orbit {
-  double n, tp, e, sw, cw, a, sini, rp, u1, u2, t0, per, as, ac;
+  double n, tp, e, sw, cw, a, sini, rp, u1, u2, t0, per;
+  float t0f, perf, win;  // circular orbits: transits only within |phase| < win of t0
+  float as, ac;          // trend amplitudes
 };
 
 __device__ Orbit make_orbit(const gtrap_transit_params &q) {
@@ -125,12 +130,26 @@ __device__ Orbit make_orbit(const gtrap_transit_params &q) {
   o.u1 = q.u1;
   o.u2 = q.u2;
   o.t0 = q.t0;
-  o.as = q.amp_sin;
-  o.ac = q.amp_dcos;
+  o.as = (float)q.amp_sin;
+  o.ac = (float)q.amp_dcos;
+  // z >= a |sin(2 pi phase)| on a circular orbit, so z < 1 + rp needs |phase| below
+  // asin((1 + rp) / a) / 2 pi (eccentric orbits: always the exact path)
+  o.t0f = (float)q.t0;
+  o.perf = (float)q.per;
+  o.win = o.e == 0.0 ? (float)(asin(fmin(1.0, (1.0 + q.rp) / q.a)) / (2.0 * M_PI)) : 1.0f;
   return o;
 }
 
 __device__ double model_flux(const Orbit &o, double t, const GlRule &gl) {
+  if (o.e == 0.0) {  // circular: sin(w + f) = cos(2 pi (t - t0) / P)
+    double ph = (t - o.t0) / o.per;
+    ph -= rint(ph);
+    const double cs = cospi(2.0 * ph);
+    if (!(cs > 0.0)) return 1.0;
+    const double z = o.a * sqrt(fmax(0.0, 1.0 - cs * cs * o.sini * o.sini));
+    if (z >= 1.0 + o.rp) return 1.0;
+    return 1.0 - occulted(o.rp, z, o.u1, o.u2, gl);
+  }
   const double M = o.n * (t - o.tp);
   double E = M;
   if (o.e > 0.0) {
@@ -161,12 +180,19 @@ __global__ void __launch_bounds__(256) inject_kernel(const MockArgs a) {
       const size_t i = base + (size_t)k * a.stride;
       const float tf = a.tu[i];
       if (!(tf > 0.0f) || !isfinite(tf)) continue;  // masked or gap (the drivers' tu > 0 test)
-      const double t = (double)tf;
-      const double F = model_flux(o, t, a.gl);
-      float v = (float)((double)a.lc[i] * (a.mode ? 2.0 - F : F));
-      if (o.as != 0.0 || o.ac != 0.0) {
-        const double ph = 2.0 * M_PI * (t - o.t0) / o.per;
-        v = (float)((double)v + o.as * sin(ph) - o.ac * cos(2.0 * ph));
+      // the phase in float: its error is below 2 (|t| + |t0|) 2^-24 / P, the margin is 8 times that
+      float ph = (tf - o.t0f) / o.perf;
+      ph -= rintf(ph);
+      const float margin = 4.0f * (fabsf(tf) + fabsf(o.t0f)) * 1.1920929e-7f / o.perf + 1e-6f;
+      const double F = fabsf(ph) < o.win + margin ? model_flux(o, (double)tf, a.gl) : 1.0;
+      float v = a.lc[i];
+      if (F != 1.0) v = (float)((double)v * (a.mode ? 2.0 - F : F));
+      if (o.as != 0.0f || o.ac != 0.0f) {
+        // trends in float from the float phase: about 1e-8 of the amplitude from the double
+        // terms, far below a float32 step of the flux; the sum of two floats rounds like the
+        // drivers' float64 sum
+        const float tr = o.as * sinpif(2.0f * ph) - o.ac * cospif(4.0f * ph);
+        v = __fadd_rn(v, tr);
       }
       a.lc[i] = v;
     }

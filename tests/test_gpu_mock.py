@@ -85,6 +85,22 @@ def test_inject_tess_mode_packed_with_trends(cuda):
     assert np.any(got > lc + 1e-3)  # mode 1 brightens
 
 
+def test_inject_late_times_short_period(cuda):
+    """Times near 3000 d and a 0.4-day period: the float phase window must not drop transits."""
+    n, nq = 4000, 2
+    t = np.linspace(2990.0, 3000.0, n)
+    tu = np.tile(t[:, None], (1, nq)).astype(np.float32)
+    lc = np.ones((n, nq), np.float32)
+    rec = np.zeros(nq, api.TRANSIT_PARAMS)
+    for q in range(nq):
+        for k, v in dict(t0=2995.123 + 0.1 * q, per=0.4, rp=0.12, a=2.5, inc=89.0, w=90.0, u1=0.3, u2=0.2).items():
+            rec[q][k] = v
+    got = api.inject_transit(torch.from_numpy(lc).to(cuda), torch.from_numpy(tu).to(cuda), rec).cpu().numpy()
+    want = om.inject(lc, tu, rec)
+    assert np.all(np.abs(got - want) <= 2 * np.spacing(np.float32(1.0)))
+    assert np.sum(got < 0.999) > 100
+
+
 def test_gamma_matches_reference_kernel(cuda):
     if not os.path.exists(GOLDEN):
         pytest.skip("ref_gamma_golden.npz not generated")
