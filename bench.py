@@ -713,18 +713,24 @@ def _timed(fn, steps, warmup, dev, world):
 
 def run_image(args, rank, world, local_rank):
     """Config 1 (plain BLS) or config 3 (GTLS, reference semantics) through the image entry
-    points, inputs resident (evaluations: (curve, frequency) or (curve, epoch))."""
+    points, inputs resident (evaluations: (curve, frequency) or (curve, epoch)); ``e2e`` with
+    pinned host buffers through the same calls."""
     import torch
+    import torch.distributed as dist
     from gtrap_gb300 import _build, api, synth
     _build.build()
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
+    stream = torch.cuda.current_stream(dev)
     d = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
     if args.workload == "plain":
         nq = args.nq or 64
         wl = synth.plain_bls(nq=nq, seed=1000 + 100000 * rank)
-        lc, tu = d(wl.lc), d(wl.tu)
-        fn = lambda: api.geebls_simple(lc, tu, wl.nf, wl.nb, wl.kma, wl.kmi, wl.kkmi, wl.fmin, wl.df)
+        lcn, tun = wl.lc, wl.tu
+        lc, tu = d(lcn), d(tun)
+        outs = [api.geebls_simple(lc, tu, wl.nf, wl.nb, wl.kma, wl.kmi, wl.kkmi, wl.fmin, wl.df)]
+        fn = lambda: outs.__setitem__(0, api.geebls_simple(lc, tu, wl.nf, wl.nb, wl.kma, wl.kmi, wl.kkmi,
+                                                           wl.fmin, wl.df))
         evals = nq * wl.nf
         cfg = {"workload": "plain BLS (geebls_simple): %d curves x 4096 samples, nf 4096, nb 1024, "
                            "qmi 0.005, qma 0.1" % nq, "curves_per_gpu": nq,
@@ -734,20 +740,84 @@ def run_image(args, rank, world, local_rank):
         lcn, tun, _ = synth.tess_like(nq=nq, n=18000, seed=3000 + 100000 * rank)
         g = synth.tls_grid()
         lc, tu = d(lcn), d(tun)
-        fn = lambda: api.gtls(lc, tu, 18000, g["nw"], g["nl"], g["nsc"], g["wmax"], g["dw"], g["deltat"])
+        outs = [api.gtls(lc, tu, 18000, g["nw"], g["nl"], g["nsc"], g["wmax"], g["dw"], g["deltat"])]
+        fn = lambda: api.gtls(lc, tu, 18000, g["nw"], g["nl"], g["nsc"], g["wmax"], g["dw"], g["deltat"],
+                              out=outs[0])
         evals = nq * 18000
         cfg = {"workload": "GTLS (reference semantics): %d TESS-like curves x 18000 epochs, nw 8 "
                            "(8 h .. 0.5 h), nl 16, nsc %d; 128 templates per (curve, epoch)"
                            % (nq, g["nsc"]), "curves_per_gpu": nq, "templates_per_eval": 128,
                "l2": "inputs %d MiB per GPU exceed L2" % (2 * nq * 18000 * 4 >> 20)}
     ms, clk = _timed(fn, args.steps, args.warmup, dev, world)
+    e2e = None
+    if not args.no_e2e:
+        h_lc, h_tu = torch.from_numpy(np.ascontiguousarray(lcn)).pin_memory(), torch.from_numpy(np.ascontiguousarray(tun)).pin_memory()
+        res = outs[0] if isinstance(outs[0], tuple) else (outs[0],)
+        h_o = [torch.empty(a.shape, dtype=a.dtype).pin_memory() for a in res]
+
+        def e2e_step():
+            lc.copy_(h_lc, non_blocking=True)
+            tu.copy_(h_tu, non_blocking=True)
+            fn()
+            r = outs[0] if isinstance(outs[0], tuple) else (outs[0],)
+            for h, a in zip(h_o, r):
+                h.copy_(a, non_blocking=True)
+
+        e2e_step()
+        torch.cuda.synchronize(dev)
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        for _ in range(args.steps):
+            e2e_step()
+        e.record(stream)
+        torch.cuda.synchronize(dev)
+        ems = torch.tensor([s.elapsed_time(e) / args.steps], device=dev, dtype=torch.float64)
+        if world > 1:
+            dist.all_reduce(ems, op=dist.ReduceOp.MAX)
+        e2e = {"value": evals * world / (float(ems[0]) / 1e3), "unit": UNIT,
+               "h2d_bytes_per_step": (h_lc.numel() + h_tu.numel()) * 4,
+               "d2h_bytes_per_step": sum(h.numel() * h.element_size() for h in h_o),
+               "ms_per_step": float(ems[0]), "api": "gtrap_gb300.api (%s) with pinned host buffers"
+               % ("geebls_simple" if args.workload == "plain" else "gtls")}
     if rank != 0:
         return
+    peak = fp32_peak_tflops(dev)
+    if args.workload == "plain":
+        flop_per_eval = 7.0 * wl.nb * (wl.kma - max(wl.kmi, 1))
+        roof = {"bound": "fp32", "kernel": "bls_fold_scan_kernel", "flop_per_eval": flop_per_eval,
+                "note": "exhaustive-scan FP32 work per (curve, frequency); pruning skips most windows"}
+    else:
+        flop_per_eval = 40.0 * 128
+        roof = {"bound": "fp32", "kernel": "gtls_kernel", "flop_per_eval": flop_per_eval,
+                "note": "40 FP32 flops of the statistic per template (H, chi^2, S/N); the kernel is "
+                        "latency bound (binary searches and walks), so this fraction is low"}
+    achieved = flop_per_eval * evals / (ms / 1e3) / 1e12
+    roof.update({"achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                 "kernel_ms": ms, "peak_source": "live FP32 FMA-chain probe on this GPU"})
     line = {"metric": METRIC, "value": evals * world / (ms / 1e3), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64" if args.workload == "plain" else "f32",
-            "data": "synthetic", "config": cfg | {"parallelism": "replicas x%d" % world},
+            "data": "synthetic", "config": cfg | {"parallelism": "replicas x%d" % world}, "roofline": roof,
             "gpu_launches": (3 if args.workload == "plain" else 1) * args.steps, "clocks": clk}
+    if e2e:
+        line["e2e"] = e2e
+    if not args.no_cpu_baseline:
+        import oracle
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        if args.workload == "plain":
+            ncs = min(nq, 64)
+            oracle.bls(np.ascontiguousarray(lcn[:, :ncs]), tun, wl.nf, wl.nb, wl.kma, wl.kmi, wl.kkmi, wl.fmin,
+                       wl.df, nthreads=threads)
+            done, sample = ncs * wl.nf, "%d curves x %d frequencies (FP64 geebls_simple restatement)" % (ncs, wl.nf)
+        else:
+            ncs = min(nq, 32)
+            oracle.gtls(np.ascontiguousarray(lcn[:, :ncs]), np.ascontiguousarray(tun[:, :ncs]), 18000, g["nw"],
+                        g["nl"], g["nsc"], g["wmax"], g["dw"], g["deltat"], nthreads=threads)
+            done, sample = ncs * 18000, "%d curves x 18000 epochs (FP64 gtls restatement)" % ncs
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": done / dt, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": sample + ", %.1f s" % dt}
     print(json.dumps(line), flush=True)
 
 
