@@ -231,9 +231,16 @@ int gtrap_gfilter_packed(const float *in, float *out, const uint64_t *off, const
   int warps = (int)(budget / per_warp);
   if (warps > 8) warps = 8;
   while (warps > 1 && per_warp * warps > 56 * 1024) --warps;
+  // rows per lane: long runs amortise each lane's initial sort (about w^2 / 4 steps) over a
+  // big batch; a few curves (a served step) get short runs so that their rows still spread
+  // over about 20,000 lanes (a run costs about its length in dependent row updates)
+  const size_t rows = (size_t)max_n * ncurves;  // upper bound of the batch's rows
+  const size_t lanes_wanted = (size_t)sm_count() * 128;
+  size_t run_fill = (rows + lanes_wanted - 1) / lanes_wanted;
   int run = (int)(8 * w);
   if (run < 64) run = 64;
   if (run > 1024) run = 1024;
+  if (run_fill < (size_t)run) run = run_fill < 16 ? 16 : (int)run_fill;
   const size_t rows_per_block = (size_t)run * 32 * warps;
   const unsigned gx = (unsigned)((max_n + rows_per_block - 1) / rows_per_block);
   const unsigned gy = ncurves < 65535 ? ncurves : 65535;

@@ -60,3 +60,24 @@ def test_get_offset_dropin(cuda):
     ref_img = resid.copy()
     ref_img[tu < 0] = 0.0
     np.testing.assert_array_equal(img, ref_img)
+
+
+@pytest.mark.parametrize("lens,r", [((10000,), 24), ((50000,), 24), ((300, 7000, 1, 65), 24), ((2000,) * 40, 12)])
+def test_gfilter_packed_bit_exact(cuda, lens, r):
+    """The packed detrend (one flat array, curve q = [off[q], off[q] + n[q])) from a lone curve
+    (short runs spread over many lanes) to a batch (long runs) equals medfilt per curve."""
+    from gtrap_gb300 import _native as N
+    from gtrap_gb300._dev import as_ptr
+    rng = np.random.default_rng(sum(lens) + r)
+    xs = [rng.normal(1.0, 1e-3, size=n).astype(np.float32) for n in lens]
+    flat = torch.from_numpy(np.concatenate(xs)).to(cuda)
+    out = torch.empty_like(flat)
+    off = torch.tensor(np.concatenate([[0], np.cumsum(lens)[:-1]]), dtype=torch.int64, device=cuda)
+    n = torch.tensor(lens, dtype=torch.int32, device=cuda)
+    N.call("gtrap_gfilter_packed", as_ptr(flat), as_ptr(out), as_ptr(off), as_ptr(n), len(lens), max(lens), r,
+           torch.cuda.current_stream().cuda_stream)
+    got = out.cpu().numpy()
+    o = 0
+    for x in xs:
+        np.testing.assert_array_equal(got[o:o + x.size], oracle.medfilt_residual(x[:, None], r)[:, 0])
+        o += x.size
