@@ -93,3 +93,59 @@ def test_packed_struct_layouts_match_the_header(tmp_path):
         assert got[(st, "size")] == dt.itemsize, st
         for f in dt.names:
             assert got[(st, f)] == dt.fields[f][1], (st, f)
+
+
+def test_new_entry_points_validate_on_the_host(lib):
+    import numpy as np
+    from gtrap_gb300 import api
+    P = C.c_void_p(16)
+    durs = np.array([0.1, 0.2], np.float32)
+    d = durs.ctypes.data_as(C.c_void_p)
+    ws = C.c_void_p(256)
+
+    def tf(nb=256, nd=2, dmax=128, lfrac=0.2, n=1000, nbytes=1 << 40, wsp=ws, lc=P):
+        return lib.gtrap_tls_fold(P, P, P, P, lc, P, P, n, 4, 8, nb, 0.1, 0.01, d, nd, lfrac, dmax, wsp, nbytes, None)
+
+    assert tf(nb=100) == _native.ERR_INVALID_ARG and b"power of two" in lib.gtrap_last_error()
+    assert tf(nd=0) == _native.ERR_INVALID_ARG
+    assert tf(nd=33) == _native.ERR_INVALID_ARG
+    assert tf(dmax=512) == _native.ERR_INVALID_ARG and b"dmax" in lib.gtrap_last_error()
+    assert tf(lfrac=0.6) == _native.ERR_INVALID_ARG
+    assert tf(n=1 << 20) == _native.ERR_INVALID_ARG
+    assert tf(lc=None) == _native.ERR_INVALID_ARG
+    assert tf(nbytes=16) == _native.ERR_WORKSPACE
+    assert tf(wsp=C.c_void_p(257)) == _native.ERR_WORKSPACE  # misaligned
+    assert lib.gtrap_tls_fold_workspace_size(1000, 4) >= 4 * 1000 * 20
+
+    rec = np.zeros(1, api.TRANSIT_PARAMS)
+    rec["per"], rec["a"], rec["rp"] = -1.0, 10.0, 0.1
+    assert lib.gtrap_transit_flux(P, P, 10, rec.ctypes.data_as(C.c_void_p), None) == _native.ERR_INVALID_ARG
+    assert lib.gtrap_transit_flux(P, P, 0, None, None) == 0  # nothing to do
+    assert lib.gtrap_inject_transit(P, P, P, P, 1, 2, 10, P, 2, None) == _native.ERR_INVALID_ARG
+    assert b"mode" in lib.gtrap_last_error()
+    assert lib.gtrap_inject_transit(P, P, P, P, 0, 2, 10, P, 0, None) == _native.ERR_INVALID_ARG
+    assert lib.gtrap_inject_transit(None, P, P, P, 1, 2, 10, P, 0, None) == _native.ERR_INVALID_ARG
+    assert lib.gtrap_gamma_sample(P, 10, 0.0, 1.0, 10, 0, None, None) == _native.ERR_INVALID_ARG
+    assert lib.gtrap_gamma_sample(None, 10, 1.0, 1.0, 10, 0, None, None) == _native.ERR_INVALID_ARG
+    assert lib.gtrap_probe_smem_load_peak(None, 10, None, None) == _native.ERR_INVALID_ARG
+
+
+def test_transit_params_record_matches_the_header(tmp_path):
+    """gtrap_transit_params: 11 doubles, 88 bytes, field order as api.TRANSIT_PARAMS."""
+    import shutil
+    import subprocess
+    from gtrap_gb300 import api
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "tp.c"
+    fields = api.TRANSIT_PARAMS.names
+    body = "".join('printf("%%zu ", offsetof(gtrap_transit_params, %s));' % f for f in fields)
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "gtrap_gb300.h"\n'
+                   'int main(void){%s printf("%%zu\\n", sizeof(gtrap_transit_params)); return 0;}\n' % body)
+    exe = tmp_path / "tp"
+    subprocess.run([cc, "-I", str(ROOT / "include"), "-I", "/usr/local/cuda/include", str(src), "-o", str(exe)],
+                   check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    assert got[:-1] == [api.TRANSIT_PARAMS.fields[f][1] for f in fields]
+    assert got[-1] == api.TRANSIT_PARAMS.itemsize == 88
