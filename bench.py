@@ -803,6 +803,19 @@ def run_image(args, rank, world, local_rank):
         line["e2e"] = e2e
     if not args.no_cpu_baseline:
         import oracle
+        if args.workload == "plain":
+            sr = outs[0].cpu().numpy()
+            ref = oracle.bls(np.ascontiguousarray(lcn[:, :4]), tun, wl.nf, wl.nb, wl.kma, wl.kmi, wl.kkmi, wl.fmin,
+                             wl.df, nthreads=os.cpu_count() or 1)[0]
+            ok = ref > 0
+            line["parity"] = {"sample": "4 curves x all %d frequencies (FP64 oracle)" % wl.nf,
+                              "sr_max_rel_err": float(np.max(np.abs(sr[:4][ok] - ref[ok]) / ref[ok]))}
+        else:
+            sn = outs[0][0].cpu().numpy()[:, :2]
+            osn = oracle.gtls(np.ascontiguousarray(lcn[:, :2]), np.ascontiguousarray(tun[:, :2]), 18000, g["nw"],
+                              g["nl"], g["nsc"], g["wmax"], g["dw"], g["deltat"], nthreads=os.cpu_count() or 1)[0]
+            line["parity"] = {"sample": "2 curves x 18000 epochs (FP64 oracle)",
+                              "sn_max_err_rel_or_abs1": float(np.max(np.abs(sn - osn) / np.maximum(np.abs(osn), 1.0)))}
         threads = os.cpu_count() or 1
         t0 = time.perf_counter()
         if args.workload == "plain":
@@ -858,6 +871,28 @@ def tlsfold_cpu_sample(lcn, tun, threads, n_freqs):
                     dmax=TF_DMAX)
     dt = time.perf_counter() - t0
     return n_freqs / dt, dt
+
+
+def tlsfold_sampled_parity(lcn, tun, outs, curves=(0, 1), nfs=16):
+    """Full-size outputs against the FP64 oracle on a sample: ``nfs`` frequencies spread
+    over the grid for each sampled curve."""
+    import oracle
+    stride = TF_NF // nfs
+    tsr = outs[0].cpu().numpy()
+    st, du = outs[1].cpu().numpy(), outs[2].cpu().numpy()
+    rel, same = 0.0, 0
+    for q in curves:
+        lc = np.ascontiguousarray(lcn[:, q:q + 1])
+        tu = np.ascontiguousarray(tun[:, q:q + 1])
+        otsr, ost, odu = oracle.tls_fold(lc, tu, np.zeros(1, np.float32), nfs, TF_NB, TF_FMIN, TF_DF * stride,
+                                         TF_DURS, lfrac=TF_LFRAC, dmax=TF_DMAX)[:3]
+        j = np.arange(nfs) * stride
+        ok = otsr[0] > 0
+        if ok.any():
+            rel = max(rel, float(np.max(np.abs(tsr[q, j][ok] - otsr[0][ok]) / otsr[0][ok])))
+        same += int(np.sum((st[q, j] == ost[0]) & (du[q, j] == odu[0])))
+    return {"sample": "%d curves x %d frequencies spread over the grid (FP64 oracle, direct sums)" % (len(curves), nfs),
+            "tsr_max_rel_err": rel, "best_template_equal_frac": same / (len(curves) * nfs)}
 
 
 def run_tlsfold(args, rank, world, local_rank):
@@ -943,6 +978,7 @@ def run_tlsfold(args, rank, world, local_rank):
     if e2e:
         line["e2e"] = e2e
     if not args.no_cpu_baseline:
+        line["parity"] = tlsfold_sampled_parity(lcn, tun, outs)
         threads = os.cpu_count() or 1
         nfs = min(TF_NF, 256 * threads)
         v, dt = tlsfold_cpu_sample(lcn, tun, threads, nfs)
@@ -1075,6 +1111,14 @@ def run_mock(args, rank, world, local_rank):
     if e2e:
         line["e2e"] = e2e
     if not args.no_cpu_baseline:
+        import oracle.mock as om
+        fresh = torch.from_numpy(lcn[:, :4].copy()).to(dev)
+        got = api.inject_transit(fresh, torch.from_numpy(np.ascontiguousarray(tun[:, :4])).to(dev), rec[:4],
+                                 mode=1).cpu().numpy()
+        want = om.inject(lcn[:, :4], tun[:, :4], rec[:4], mode=1)
+        ulp = np.spacing(np.abs(want).astype(np.float32))
+        line["parity"] = {"sample": "4 curves x %d samples injected once (quadrature oracle)" % TF_N,
+                          "max_err_in_float32_ulp": float(np.max(np.abs(got - want) / ulp))}
         v, dt = mock_cpu_sample(lcn, tun, rec, 16)
         line["cpu_baseline"] = {"value": v, "unit": MOCK_UNIT, "cores": 1, "kind": "port",
                                 "sample": "16 curves x %d samples through the oracle (scipy quadrature per "
