@@ -802,7 +802,8 @@ def run_image(args, rank, world, local_rank):
         flop_per_eval = 40.0 * 128
         roof = {"bound": "fp32", "kernel": "gtls_kernel", "flop_per_eval": flop_per_eval,
                 "note": "40 FP32 flops of the statistic per template (H, chi^2, S/N); the kernel is "
-                        "latency bound (binary searches and walks), so this fraction is low"}
+                        "issue bound (binary searches and region walks dominate its instructions), so "
+                        "this fraction is low"}
     achieved = flop_per_eval * evals / (ms / 1e3) / 1e12
     roof.update({"achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
                  "kernel_ms": ms, "peak_source": "live FP32 FMA-chain probe on this GPU"})
