@@ -143,6 +143,31 @@ class Arena:
         self.used -= need
 
 
+class _Staging:
+    """Pinned host staging for the uploads of the steps in flight: one slot per step of the
+    pipeline depth, so the slot a step fills was last used by a step that has finished (a
+    step is launched only while fewer than ``depth`` are in flight, and a step's kernels
+    wait for its uploads).  A step that needs more than a slot gets a fresh pinned buffer."""
+
+    def __init__(self, depth: int, slot_bytes: int = 32 << 20):
+        self.slot_bytes = slot_bytes
+        self.slots = [torch.empty(slot_bytes, dtype=torch.uint8, pin_memory=True) for _ in range(depth)]
+        self.cur = None
+        self.used = 0
+
+    def begin(self, step_index: int):
+        self.cur = self.slots[step_index % len(self.slots)]
+        self.used = 0
+
+    def take(self, nbytes: int) -> torch.Tensor:
+        """A pinned uint8 buffer of ``nbytes`` (256-byte aligned within the slot)."""
+        start = (self.used + 255) // 256 * 256
+        if self.cur is None or start + nbytes > self.slot_bytes:
+            return torch.empty(max(nbytes, 1), dtype=torch.uint8, pin_memory=True)
+        self.used = start + nbytes
+        return self.cur[start:start + nbytes]
+
+
 @dataclass
 class _Live:
     rid: int
@@ -212,6 +237,7 @@ class TransitServer:
         self.hbm_bytes = (self.sample_cap * SAMPLE_BYTES + self.out_cap * OUTPUT_BYTES +
                           2 * max_requests * 64)
         self.stream = torch.cuda.Stream(d)
+        self.staging = _Staging(self.depth)
         self.h2d = torch.cuda.Stream(d)
         self.d2h = torch.cuda.Stream(d)
         self.waiting: collections.deque = collections.deque()
@@ -278,8 +304,8 @@ class TransitServer:
         """Copy the new curves' samples (pinned staging, copy stream); returns the event the
         compute stream waits for."""
         total = sum(lv.req.n for lv in new)
-        th = torch.empty(total, dtype=torch.float32, pin_memory=True)
-        xh = torch.empty(total, dtype=torch.float32, pin_memory=True)
+        th = self.staging.take(4 * total).view(torch.float32)
+        xh = self.staging.take(4 * total).view(torch.float32)
         tn, xn = th.numpy(), xh.numpy()
         p = 0
         spans = []
@@ -324,7 +350,7 @@ class TransitServer:
         for a in parts:
             offs.append(p)
             p += (a.size + 255) // 256 * 256
-        host = torch.empty(max(p, 256), dtype=torch.uint8, pin_memory=True)
+        host = self.staging.take(max(p, 256))
         hn = host.numpy()
         for a, o in zip(parts, offs):
             hn[o:o + a.size] = a
@@ -335,7 +361,9 @@ class TransitServer:
         for rows, table, live, dt in ((bt, self.bls_table, nb, BLS_CURVE), (tt, self.tls_table, nt, TLS_CURVE)):
             if not len(rows):
                 continue
-            hb = torch.from_numpy(np.frombuffer(rows.tobytes(), np.uint8).copy()).pin_memory()
+            rb = np.frombuffer(rows.tobytes(), np.uint8)
+            hb = self.staging.take(rb.size)
+            hb.numpy()[:] = rb
             sz = dt.itemsize
             slots = [lv.desc for lv in live]
             if slots == list(range(slots[0], slots[0] + len(slots))):
@@ -380,6 +408,7 @@ class TransitServer:
             return done
         si = self.step_count
         self.step_count += 1
+        self.staging.begin(si)
         st = self.stream
         with torch.cuda.stream(st):
             if new:
@@ -453,11 +482,15 @@ class TransitServer:
                     srcs = (st_[lv.pk_slot * rs:(lv.pk_slot + 1) * rs], idx[lv.pk_slot], val[lv.pk_slot])
                 else:
                     srcs = [self.o[j][o:o + m] for j in range(3 if lv.req.kind == "bls" else 5)]
-                outs = []
-                for src in srcs:
-                    h = torch.empty(src.numel(), dtype=src.dtype, pin_memory=True)
+                # one pinned block for the request's outputs, one view per series
+                sizes = [(src.numel() * src.element_size() + 15) // 16 * 16 for src in srcs]
+                blk = torch.empty(sum(sizes), dtype=torch.uint8, pin_memory=True)
+                outs, o_ = [], 0
+                for src, sz in zip(srcs, sizes):
+                    h = blk[o_:o_ + src.numel() * src.element_size()].view(src.dtype)
                     h.copy_(src, non_blocking=True)
                     outs.append(h)
+                    o_ += sz
                 lv.result = tuple(outs)
                 ev = torch.cuda.Event()
                 ev.record(self.d2h)
