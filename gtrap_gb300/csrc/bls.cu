@@ -101,23 +101,32 @@ __device__ __forceinline__ bool sample_valid(const PrepArgs &a, uint32_t i, floa
   return isfinite((double)x - off);
 }
 
-// Per-curve power-of-two scale: 2^sx * max|x - offset| < xq_max.
-__global__ void __launch_bounds__(1024) bls_scale_kernel(PrepArgs a) {
-  __shared__ double part[32][33];
+// Per-curve power-of-two scale: 2^sx * max|x - offset| < xq_max.  Only the exponent of the
+// maximum matters, and rounding toward zero never crosses a power of two, so the maximum of
+// the float differences rounded toward zero has the exponent of the exact one: the kernel
+// needs no FP64.  Blocks of 32 curves x a chunk of rows fill the GPU whatever the curve
+// count; per curve they combine with atomicMax on the (non-negative) float bits, kept in sx
+// until bls_scale_final_kernel, and atomicAdd on the valid count (sx and nv start at 0).
+__global__ void __launch_bounds__(1024) bls_scale_kernel(PrepArgs a, uint32_t rows_per_chunk) {
+  __shared__ float part[32][33];
   __shared__ uint32_t pcnt[32][33];
   const int lane = threadIdx.x, row = threadIdx.y;
   const uint32_t q = blockIdx.x * 32 + lane;
-  double amax = 0.0;
+  const uint32_t r0 = blockIdx.y * rows_per_chunk;
+  const uint32_t r1 = min(a.n, r0 + rows_per_chunk);
+  float amax = 0.0f;
   uint32_t cnt = 0;
   if (q < a.nq) {
-    const double off = a.offset ? (double)a.offset[q] : 0.0;
-    for (uint32_t i = row; i < a.n; i += 32) {
-      const size_t idx = (size_t)i * a.nq + q;
-      const float x = __ldg(a.lc + idx);
-      const float t = a.full ? __ldg(a.tu + idx) : __ldg(a.tu + i);
-      if (sample_valid(a, i, t, x, off)) {
-        amax = fmax(amax, fabs((double)x - off));
-        ++cnt;
+    const float off = a.offset ? a.offset[q] : 0.0f;
+    if (isfinite(off)) {  // a non-finite offset leaves no valid sample (x - offset not finite)
+      for (uint32_t i = r0 + row; i < r1; i += 32) {
+        const size_t idx = (size_t)i * a.nq + q;
+        const float x = __ldg(a.lc + idx);
+        const float t = a.full ? __ldg(a.tu + idx) : __ldg(a.tu + i);
+        if (i < a.n_eff && isfinite(x) && isfinite(t) && (!a.full || t >= 0.0f)) {
+          amax = fmaxf(amax, fabsf(__fsub_rz(x, off)));
+          ++cnt;
+        }
       }
     }
   }
@@ -125,14 +134,36 @@ __global__ void __launch_bounds__(1024) bls_scale_kernel(PrepArgs a) {
   pcnt[row][lane] = cnt;
   __syncthreads();
   if (row == 0 && q < a.nq) {
-    double m = 0.0;
+    float m = 0.0f;
     uint32_t c = 0;
-    for (int k = 0; k < 32; ++k) { m = fmax(m, part[k][lane]); c += pcnt[k][lane]; }
-    a.nv[q] = c;
-    int s = 0;
-    if (m > 0.0) s = ilogb(a.xq_max) - ilogb(m) - 1;
-    a.sx[q] = s;
+    for (int k = 0; k < 32; ++k) { m = fmaxf(m, part[k][lane]); c += pcnt[k][lane]; }
+    if (c) atomicAdd(a.nv + q, c);
+    if (m > 0.0f) atomicMax(reinterpret_cast<unsigned *>(a.sx) + q, __float_as_uint(m));
   }
+}
+
+__global__ void __launch_bounds__(256) bls_scale_final_kernel(PrepArgs a) {
+  const uint32_t q = blockIdx.x * 256 + threadIdx.x;
+  if (q >= a.nq) return;
+  const float m = __uint_as_float((unsigned)a.sx[q]);
+  a.sx[q] = m > 0.0f ? ilogb(a.xq_max) - ilogbf(m) - 1 : 0;
+}
+
+// sx and nv to zero, the scale reduction over enough blocks for the GPU, the exponents
+int launch_scale(const PrepArgs &pa, cudaStream_t stream) {
+  cudaError_t e = cudaMemsetAsync(pa.sx, 0, (size_t)pa.nq * sizeof(int32_t), stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(pa.nv, 0, (size_t)pa.nq * sizeof(uint32_t), stream);
+  if (e != cudaSuccess) return gtrap::fail(GTRAP_ERR_CUDA, "bls prep: cudaMemsetAsync: %s", cudaGetErrorString(e));
+  const uint32_t groups = (pa.nq + 31) / 32;
+  const uint32_t want = (uint32_t)gtrap::sm_count() * 2;
+  uint32_t chunks = groups >= want ? 1 : (want + groups - 1) / groups;
+  uint32_t rows = (pa.n + chunks - 1) / chunks;
+  rows = rows < 256 ? 256 : (rows + 31) / 32 * 32;
+  chunks = (pa.n + rows - 1) / rows;
+  bls_scale_kernel<<<dim3(groups, chunks), dim3(32, 32), 0, stream>>>(pa, rows);
+  GTRAP_TRY(gtrap::check_launch("bls_scale_kernel"));
+  bls_scale_final_kernel<<<(pa.nq + 255) / 256, 256, 0, stream>>>(pa);
+  return gtrap::check_launch("bls_scale_final_kernel");
 }
 
 // Transpose a 32x32 tile of the [n, nq] image into curve-major quantised flux (and,
@@ -1065,8 +1096,7 @@ int run_bls(bool full, float *blsp, uint32_t *phase1, uint32_t *phase2, const fl
   pa.n = n; pa.nq = nq; pa.n_eff = n_eff;
   pa.fmin = fmin; pa.df = df; pa.xq_max = xq_max;
   pa.full = full ? 1 : 0; pa.exact = exact ? 1 : 0;
-  bls_scale_kernel<<<(nq + 31) / 32, dim3(32, 32), 0, stream>>>(pa);
-  GTRAP_TRY(gtrap::check_launch("bls_scale_kernel"));
+  GTRAP_TRY(launch_scale(pa, stream));
   bls_pack_kernel<<<dim3((nq + 31) / 32, (n + 31) / 32), dim3(32, 8), 0, stream>>>(pa);
   GTRAP_TRY(gtrap::check_launch("bls_pack_kernel"));
   if (!full && exact) {
@@ -1150,8 +1180,7 @@ int bls_prep_image(const float *lc, const float *tu, const float *offset, uint32
   pa.n = n; pa.nq = nq; pa.n_eff = n;
   pa.fmin = fmin; pa.df = df; pa.xq_max = xq_max;
   pa.full = 1; pa.exact = 1;
-  bls_scale_kernel<<<(nq + 31) / 32, dim3(32, 32), 0, stream>>>(pa);
-  GTRAP_TRY(check_launch("bls_scale_kernel"));
+  GTRAP_TRY(launch_scale(pa, stream));
   bls_pack_kernel<<<dim3((nq + 31) / 32, (n + 31) / 32), dim3(32, 8), 0, stream>>>(pa);
   return check_launch("bls_pack_kernel");
 }
