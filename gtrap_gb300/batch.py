@@ -5,12 +5,15 @@ float32 time and flux arrays (curve q = samples ``[off[q], off[q] + n[q])``).  O
 :meth:`RaggedBatch.launch` issues, on one stream and without host synchronisation,
 
 1. the running-median detrend of every curve (``gtrap_gfilter_packed``),
-2. the per-curve offset of the BLS curves (``gtrap_bls_offsets``; get_offset,
-   gtrap/gfilter.py:94-101),
-3. quantisation and exact phase encoding of the BLS samples (``gtrap_bls_prepare``),
+2. the per-curve offset of the BLS and folded-search curves (``gtrap_bls_offsets``;
+   get_offset, gtrap/gfilter.py:94-101),
+3. quantisation and exact phase encoding of their samples (``gtrap_bls_prepare``,
+   ``gtrap_tls_fold_prepare``),
 4. one persistent BLS launch that pops (curve, frequency tile) items from a device work
-   queue (``gtrap_bls_run``; the geebls statistic, include/geebls.h:35-165), and
-5. one persistent GTLS launch over (curve, 64-epoch tile) items (``gtrap_gtls_run``; the
+   queue (``gtrap_bls_run``; the geebls statistic, include/geebls.h:35-165),
+5. one persistent launch of the folded trapezoid search over (curve, frequency group)
+   items (``gtrap_tls_fold_run``; an extension with no counterpart in the reference), and
+6. one persistent GTLS launch over (curve, 64-epoch tile) items (``gtrap_gtls_run``; the
    gtls statistic, include/gtls_simple.h:51-404),
 
 so the whole sequence can be captured in a CUDA graph (:meth:`RaggedBatch.capture`) and
@@ -70,6 +73,24 @@ class TlsSpec:
         return N.TLS_FIX_A if self.fix_a else 0
 
 
+@dataclass(frozen=True)
+class FoldSpec:
+    """Launch-wide grid of the folded trapezoid search (``api.tls_fold``): nb phase bins,
+    durations in days, ingress fraction and longest template in bins (default nb/2)."""
+    nb: int = 2048
+    durations: tuple = tuple(float(w) for w in np.linspace(0.5, 8.0, 8, dtype=np.float32) / np.float32(24.0))
+    lfrac: float = 0.2
+    dmax: int | None = None
+
+    @property
+    def dmax_bins(self) -> int:
+        return self.nb // 2 if self.dmax is None else int(self.dmax)
+
+    @property
+    def w(self) -> np.ndarray:
+        return np.ascontiguousarray(self.durations, dtype=np.float32)
+
+
 @dataclass
 class _Bls:
     t: np.ndarray
@@ -79,6 +100,16 @@ class _Bls:
     df: float
     kkmi: int
     ntrue: int
+    offset: float
+
+
+@dataclass
+class _Fold:
+    t: np.ndarray
+    x: np.ndarray
+    nf: int
+    fmin: float
+    df: float
     offset: float
 
 
@@ -98,28 +129,31 @@ def _tiles(count: int, per: int) -> int:
 
 
 class RaggedBatch:
-    """A device-resident packed batch of BLS and GTLS requests.
+    """A device-resident packed batch of BLS, folded-trapezoid and GTLS requests.
 
-    Add curves with :meth:`add_bls` / :meth:`add_tls`, then :meth:`build` uploads them.
-    ``detrend_r`` (window 2r+1) detrends every curve before its search; with
-    ``auto_offset`` (default: when detrending) the BLS offsets are computed on the device
-    from the detrended flux, otherwise the per-curve offsets given to :meth:`add_bls` are
-    used."""
+    Add curves with :meth:`add_bls` / :meth:`add_fold` / :meth:`add_tls`, then :meth:`build`
+    uploads them.  ``detrend_r`` (window 2r+1) detrends every curve before its search; with
+    ``auto_offset`` (default: when detrending) the BLS and folded-search offsets are computed
+    on the device from the detrended flux, otherwise the per-curve offsets given to
+    :meth:`add_bls` / :meth:`add_fold` are used."""
 
     def __init__(self, bls: BlsSpec = BlsSpec(), tls: TlsSpec = TlsSpec(), detrend_r=None,
-                 auto_offset=None, device=None):
+                 auto_offset=None, device=None, fold: FoldSpec = FoldSpec()):
         self.bls_spec = bls
         self.tls_spec = tls
+        self.fold_spec = fold
         self.detrend_r = None if detrend_r is None else int(detrend_r)
         self.auto_offset = (self.detrend_r is not None) if auto_offset is None else bool(auto_offset)
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device) \
             if torch.cuda.is_available() else None
         self._bls: list[_Bls] = []
         self._tls: list[_Tls] = []
+        self._fold: list[_Fold] = []
         self.built = False
         self.F = None
         self.bls_blocks = 0
         self.tls_blocks = 0
+        self.fold_blocks = 0
 
     # -- assembling ---------------------------------------------------------------------
     def add_bls(self, t, x, nf, fmin, df, kkmi=None, qmi=0.005, ntrue=None, offset=0.0) -> int:
@@ -141,6 +175,22 @@ class RaggedBatch:
                               float(offset)))
         self.built = False
         return len(self._bls) - 1
+
+    def add_fold(self, t, x, nf, fmin, df, offset=0.0) -> int:
+        """Queue a folded trapezoid search (``api.tls_fold`` semantics on this curve alone:
+        samples with t < 0 are not folded, flux - offset, trial frequencies fmin + j*df)."""
+        t = np.ascontiguousarray(t, np.float32).reshape(-1)
+        x = np.ascontiguousarray(x, np.float32).reshape(-1)
+        n = t.size
+        if n == 0 or x.size != n:
+            raise ValueError("a folded-search curve needs n >= 1 samples of time and flux")
+        if n >= 1 << 20:
+            raise ValueError("n=%d must be below 2^20" % n)
+        if nf < 1:
+            raise ValueError("nf must be positive")
+        self._fold.append(_Fold(t, x, int(nf), float(fmin), float(df), float(offset)))
+        self.built = False
+        return len(self._fold) - 1
 
     def add_tls(self, t, x, nsc, wmax, dw, deltat, nt=None) -> int:
         """Queue a GTLS request over the first ``nt`` (default: all) samples."""
@@ -165,6 +215,10 @@ class RaggedBatch:
         return len(self._tls)
 
     @property
+    def n_fold(self) -> int:
+        return len(self._fold)
+
+    @property
     def bls_evals(self) -> int:
         """(curve, trial frequency) pairs of the BLS requests."""
         return sum(c.nf for c in self._bls)
@@ -174,21 +228,30 @@ class RaggedBatch:
         """(curve, epoch) pairs of the GTLS requests."""
         return sum(c.nt for c in self._tls)
 
+    @property
+    def fold_evals(self) -> int:
+        """(curve, trial frequency) pairs of the folded-search requests."""
+        return sum(c.nf for c in self._fold)
+
     # -- upload ---------------------------------------------------------------------------
     def build(self) -> "RaggedBatch":
-        """Pack the curves (BLS first, then GTLS) and upload them with their tables."""
+        """Pack the curves (BLS, then folded search, then GTLS) and upload them with their
+        tables."""
         require_cuda()
         dev = self.device
-        items = list(self._bls) + list(self._tls)
+        items = list(self._bls) + list(self._fold) + list(self._tls)
         if not items:
             raise ValueError("empty batch")
         lens = np.array([c.t.size for c in items], np.uint64)
         offs = np.zeros(len(items) + 1, np.uint64)
         np.cumsum(lens, out=offs[1:])
         self.total = int(offs[-1])
-        self.bls_total = int(offs[len(self._bls)])
+        nbls, nfold = len(self._bls), len(self._fold)
+        self.bls_total = int(offs[nbls])
+        self.prep_total = int(offs[nbls + nfold])  # samples of the pool (BLS and folded)
         self.max_n = int(lens.max())
-        self.max_n_bls = int(lens[:len(self._bls)].max()) if self._bls else 0
+        self.max_n_bls = int(lens[:nbls].max()) if nbls else 0
+        self.max_n_fold = int(lens[nbls:nbls + nfold].max()) if nfold else 0
         t_h = torch.empty(self.total, dtype=torch.float32, pin_memory=True)
         x_h = torch.empty(self.total, dtype=torch.float32, pin_memory=True)
         tn, xn = t_h.numpy(), x_h.numpy()
@@ -203,7 +266,6 @@ class RaggedBatch:
         self.lens = torch.from_numpy(lens.astype(np.int32)).to(dev)
         self.resid = torch.empty_like(self.x) if self.detrend_r is not None else self.x
 
-        nbls = len(self._bls)
         bt = np.zeros(nbls, BLS_CURVE)
         out = 0
         for k, c in enumerate(self._bls):
@@ -219,10 +281,23 @@ class RaggedBatch:
             out += c.nf
         self.bls_table = bt
         self.bls_out = out
+        ft = np.zeros(nfold, BLS_CURVE)
+        out = 0
+        for k, c in enumerate(self._fold):
+            ft[k]["off"] = offs[nbls + k]
+            ft[k]["out"] = out
+            ft[k]["n"] = c.t.size
+            ft[k]["nf"] = c.nf
+            ft[k]["fmin"] = c.fmin
+            ft[k]["df"] = c.df
+            ft[k]["offset"] = c.offset
+            out += c.nf
+        self.fold_table = ft
+        self.fold_out = out
         tt = np.zeros(len(self._tls), TLS_CURVE)
         out = 0
         for k, c in enumerate(self._tls):
-            tt[k]["off"] = offs[nbls + k]
+            tt[k]["off"] = offs[nbls + nfold + k]
             tt[k]["out"] = out
             tt[k]["nt"] = c.nt
             tt[k]["nsc"] = c.nsc
@@ -238,21 +313,25 @@ class RaggedBatch:
             return torch.from_numpy(np.frombuffer(arr.tobytes(), np.uint8).copy()).to(dev)
 
         self.bls_curves = up(bt) if nbls else None
+        self.fold_curves = up(ft) if nfold else None
         self.tls_curves = up(tt) if len(tt) else None
-        flags = self.bls_spec.flags
-        self.pool_bytes = int(N.fn("gtrap_bls_pool_bytes")(max(self.bls_total, 1), flags))
-        self.pool = torch.empty(self.pool_bytes, dtype=torch.uint8, device=dev) if nbls else None
+        # one pool for the BLS and folded-search samples; the folded search needs the phase pairs
+        flags = self.bls_spec.flags if not nfold else 0
+        self.pool_bytes = int(N.fn("gtrap_bls_pool_bytes")(max(self.prep_total, 1), flags))
+        self.pool = torch.empty(self.pool_bytes, dtype=torch.uint8, device=dev) if nbls + nfold else None
         self.blsp = torch.empty(max(self.bls_out, 1), dtype=torch.float32, device=dev)
         self.ph1 = torch.empty(max(self.bls_out, 1), dtype=torch.int32, device=dev)
         self.ph2 = torch.empty(max(self.bls_out, 1), dtype=torch.int32, device=dev)
         self.tls_outs = tuple(torch.empty(max(self.tls_out, 1), dtype=torch.float32, device=dev)
                               for _ in range(5))
-        self.counters = torch.zeros(2, dtype=torch.int32, device=dev)
+        self.fold_outs = tuple(torch.empty(max(self.fold_out, 1), dtype=dt, device=dev)
+                               for dt in (torch.float32, torch.int32, torch.int32, torch.float32))
+        self.counters = torch.zeros(3, dtype=torch.int32, device=dev)
         self.built = True
         if self.F is None:
-            self.set_config(default_F(self.bls_spec), 0, 0)
+            self.set_config(default_F(self.bls_spec) if nbls else 1, 0, 0)
         else:
-            self.set_config(self.F, self.bls_blocks, self.tls_blocks)
+            self.set_config(self.F, self.bls_blocks, self.tls_blocks, self.fold_blocks)
         return self
 
     def _bls_segments(self, F, curves=None):
@@ -262,6 +341,17 @@ class RaggedBatch:
         segs = np.zeros(order.size, SEGMENT)
         segs["curve"] = order
         counts = (self.bls_table["nf"][order].astype(np.int64) + F - 1) // F
+        cum = np.zeros(order.size + 1, np.uint32)
+        np.cumsum(counts, out=cum[1:])
+        return segs, cum
+
+    def _fold_segments(self, curves=None):
+        """One segment per curve, longest first; an item is a group of fold_F frequencies."""
+        idx = np.arange(self.n_fold) if curves is None else np.asarray(curves)
+        order = idx[np.argsort(-self.fold_table["n"][idx].astype(np.int64), kind="stable")]
+        segs = np.zeros(order.size, SEGMENT)
+        segs["curve"] = order
+        counts = (self.fold_table["nf"][order].astype(np.int64) + self.fold_F - 1) // self.fold_F
         cum = np.zeros(order.size + 1, np.uint32)
         np.cumsum(counts, out=cum[1:])
         return segs, cum
@@ -281,16 +371,24 @@ class RaggedBatch:
         return (torch.from_numpy(np.frombuffer(segs.tobytes(), np.uint8).copy()).to(dev),
                 torch.from_numpy(cum.view(np.int32).copy()).to(dev), int(segs.size))
 
-    def set_config(self, F: int, bls_blocks: int = 0, tls_blocks: int = 0):
+    def set_config(self, F: int, bls_blocks: int = 0, tls_blocks: int = 0, fold_blocks: int = 0):
         """Frequencies per BLS tile and persistent block counts (0: one or two per SM for
-        BLS, the occupancy limit for GTLS)."""
+        BLS, the occupancy limit for GTLS and the folded search)."""
         if not self.built:
             raise RuntimeError("build() the batch first")
         self.F = int(F)
         self.bls_blocks = int(bls_blocks)
         self.tls_blocks = int(tls_blocks)
+        self.fold_blocks = int(fold_blocks)
         self.bls_q = self._upload_segments(*self._bls_segments(self.F)) if self.n_bls else None
         self.tls_q = self._upload_segments(*self._tls_segments()) if self.n_tls else None
+        self.fold_q = None
+        if self.n_fold:
+            fs = self.fold_spec
+            self.fold_F = int(N.fn("gtrap_tls_fold_item_frequencies")(fs.nb, fs.dmax_bins))
+            if self.fold_F == 0:
+                raise ValueError("folded-search grid nb=%d, dmax=%d is out of range" % (fs.nb, fs.dmax_bins))
+            self.fold_q = self._upload_segments(*self._fold_segments())
 
     # -- launches -----------------------------------------------------------------------
     def launch_prep(self, stream=None):
@@ -298,14 +396,21 @@ class RaggedBatch:
         st = stream_handle(stream)
         if self.detrend_r is not None:
             N.call("gtrap_gfilter_packed", as_ptr(self.x), as_ptr(self.resid), as_ptr(self.offs),
-                   as_ptr(self.lens), self.n_bls + self.n_tls, self.max_n, self.detrend_r, st)
+                   as_ptr(self.lens), self.n_bls + self.n_fold + self.n_tls, self.max_n, self.detrend_r, st)
         if self.n_bls:
             if self.auto_offset:
                 N.call("gtrap_bls_offsets", as_ptr(self.bls_curves), self.n_bls, as_ptr(self.t),
                        as_ptr(self.resid), st)
             N.call("gtrap_bls_prepare", as_ptr(self.bls_curves), self.n_bls, self.max_n_bls,
-                   as_ptr(self.t), as_ptr(self.resid), self.bls_total, as_ptr(self.pool),
+                   as_ptr(self.t), as_ptr(self.resid), self.prep_total, as_ptr(self.pool),
                    self.pool_bytes, self.bls_spec.flags, st)
+        if self.n_fold:
+            if self.auto_offset:
+                N.call("gtrap_bls_offsets", as_ptr(self.fold_curves), self.n_fold, as_ptr(self.t),
+                       as_ptr(self.resid), st)
+            N.call("gtrap_tls_fold_prepare", as_ptr(self.fold_curves), self.n_fold, self.max_n_fold,
+                   as_ptr(self.t), as_ptr(self.resid), self.prep_total, as_ptr(self.pool),
+                   self.pool_bytes, st)
 
     def launch_bls(self, stream=None, queue=None, blocks=None, F=None):
         if not self.n_bls:
@@ -313,10 +418,21 @@ class RaggedBatch:
         segs, cum, nseg = self.bls_q if queue is None else queue
         s = self.bls_spec
         N.call("gtrap_bls_run", as_ptr(self.bls_curves), as_ptr(segs), as_ptr(cum), nseg,
-               as_ptr(self.t), as_ptr(self.pool), self.pool_bytes, self.bls_total, s.nb, s.kma,
+               as_ptr(self.t), as_ptr(self.pool), self.pool_bytes, self.prep_total, s.nb, s.kma,
                s.kmi, self.F if F is None else int(F), s.flags,
                self.bls_blocks if blocks is None else int(blocks), as_ptr(self.counters[0:1]),
                as_ptr(self.blsp), as_ptr(self.ph1), as_ptr(self.ph2), stream_handle(stream))
+
+    def launch_fold(self, stream=None, queue=None, blocks=None):
+        if not self.n_fold:
+            return
+        segs, cum, nseg = self.fold_q if queue is None else queue
+        fs = self.fold_spec
+        w = fs.w
+        N.call("gtrap_tls_fold_run", as_ptr(self.fold_curves), as_ptr(segs), as_ptr(cum), nseg,
+               as_ptr(self.pool), self.pool_bytes, self.prep_total, fs.nb, w.ctypes.data, int(w.size),
+               float(fs.lfrac), fs.dmax_bins, self.fold_F, self.fold_blocks if blocks is None else int(blocks),
+               as_ptr(self.counters[2:3]), *[as_ptr(a) for a in self.fold_outs], stream_handle(stream))
 
     def launch_tls(self, stream=None, queue=None, blocks=None):
         if not self.n_tls:
@@ -330,11 +446,13 @@ class RaggedBatch:
                *[as_ptr(a) for a in o], stream_handle(stream))
 
     def launch(self, stream=None):
-        """The whole pipeline on one stream: prep, then the BLS and GTLS persistent launches."""
+        """The whole pipeline on one stream: prep, then the BLS, folded-search and GTLS
+        persistent launches."""
         if not self.built:
             raise RuntimeError("build() the batch first")
         self.launch_prep(stream)
         self.launch_bls(stream)
+        self.launch_fold(stream)
         self.launch_tls(stream)
 
     def capture(self) -> torch.cuda.CUDAGraph:
@@ -353,15 +471,16 @@ class RaggedBatch:
         return g
 
     def capture_stages(self) -> dict:
-        """Capture prep, BLS and GTLS as three graphs ({"prep", "bls", "tls"}), so that events
-        recorded between their replays time each stage."""
+        """Capture prep, BLS, folded search and GTLS as four graphs ({"prep", "bls", "fold",
+        "tls"}), so that events recorded between their replays time each stage."""
         side = torch.cuda.Stream(self.device)
         side.wait_stream(torch.cuda.current_stream(self.device))
         with torch.cuda.stream(side):
             self.launch()
         torch.cuda.current_stream(self.device).wait_stream(side)
         graphs = {}
-        for name, fn in (("prep", self.launch_prep), ("bls", self.launch_bls), ("tls", self.launch_tls)):
+        for name, fn in (("prep", self.launch_prep), ("bls", self.launch_bls), ("fold", self.launch_fold),
+                         ("tls", self.launch_tls)):
             g = torch.cuda.CUDAGraph()
             with torch.cuda.graph(g, capture_error_mode="thread_local"):
                 fn()
@@ -385,6 +504,12 @@ class RaggedBatch:
         o, nf = int(self.bls_table[k]["out"]), int(self.bls_table[k]["nf"])
         return (self.blsp[o:o + nf].cpu().numpy(), self.ph1[o:o + nf].cpu().numpy(),
                 self.ph2[o:o + nf].cpu().numpy())
+
+    def fold_result(self, k: int):
+        """(tsr, start bin, duration index, depth) of folded-search request k as numpy arrays
+        (synchronises)."""
+        o, nf = int(self.fold_table[k]["out"]), int(self.fold_table[k]["nf"])
+        return tuple(a[o:o + nf].cpu().numpy() for a in self.fold_outs)
 
     def tls_result(self, k: int):
         """(sn, w, t0, l, hmax) of GTLS request k as numpy arrays (synchronises)."""
@@ -466,11 +591,12 @@ def autotune(batch: RaggedBatch, F_candidates=(2, 3, 4, 5, 6, 8, 12), bps_candid
 
 
 # -- plain baseline ---------------------------------------------------------------------------
-def run_plain(batch: RaggedBatch, stream=None, bls_curves=None, tls_curves=None):
+def run_plain(batch: RaggedBatch, stream=None, bls_curves=None, tls_curves=None, fold_curves=None):
     """The same requests through the plain per-curve entry points (one gfilter, offset and
-    geebls or gtls launch sequence per curve, as a caller of the reference does for curves
-    with different lengths or grids), writing into the batch's output arrays.  ``bls_curves``
-    and ``tls_curves`` restrict the run to those request indices."""
+    geebls, tls_fold or gtls launch sequence per curve, as a caller of the reference does for
+    curves with different lengths or grids), writing into the batch's output arrays.
+    ``bls_curves``, ``tls_curves`` and ``fold_curves`` restrict the run to those request
+    indices."""
     if not batch.built:
         batch.build()
     dev = batch.device
@@ -490,9 +616,23 @@ def run_plain(batch: RaggedBatch, stream=None, bls_curves=None, tls_curves=None)
                    float(row["fmin"]), float(row["df"]), phase=s.phase,
                    out=(batch.blsp[o:o + nf].view(1, nf), batch.ph1[o:o + nf].view(1, nf),
                         batch.ph2[o:o + nf].view(1, nf)), stream=stream)
+    fs = batch.fold_spec
+    fgiven = torch.from_numpy(batch.fold_table["offset"].astype(np.float32)).to(dev) if batch.n_fold else None
+    for k in (range(batch.n_fold) if fold_curves is None else fold_curves):
+        j = batch.n_bls + k
+        a, n = int(offs[j]), int(offs[j + 1] - offs[j])
+        x = batch.x[a:a + n].view(n, 1)
+        t = batch.t[a:a + n].view(n, 1)
+        r = api.gfilter(x, batch.detrend_r, stream=stream) if batch.detrend_r is not None else x
+        off = api.offset(r, t, stream=stream) if batch.auto_offset else fgiven[k:k + 1]
+        row = batch.fold_table[k]
+        o, nf = int(row["out"]), int(row["nf"])
+        api.tls_fold(r, t, off, nf, fs.nb, float(row["fmin"]), float(row["df"]), fs.w, lfrac=fs.lfrac,
+                     dmax=fs.dmax_bins, out=tuple(v[o:o + nf].view(1, nf) for v in batch.fold_outs),
+                     stream=stream)
     ts = batch.tls_spec
     for k in (range(batch.n_tls) if tls_curves is None else tls_curves):
-        j = batch.n_bls + k
+        j = batch.n_bls + batch.n_fold + k
         a, n = int(offs[j]), int(offs[j + 1] - offs[j])
         x = batch.x[a:a + n].view(n, 1)
         t = batch.t[a:a + n].view(n, 1)

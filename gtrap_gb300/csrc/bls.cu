@@ -223,35 +223,39 @@ __global__ void bls_common_phase_kernel(const float *__restrict__ tu, ulonglong2
 // prep of packed (ragged) batches: curve q owns samples [off, off + n) of the packed arrays
 
 // Per curve: count bits of the 64-bit fold format, power-of-two flux scale, valid samples.
+// |quantised flux| stays below min(2^(62 - CB) / n, xq_cap); as in bls_scale_kernel, the
+// maximum is taken over the float differences rounded toward zero, which have the exponents
+// of the exact ones, so a packed curve gets the scale of the same curve in an image.
 __global__ void __launch_bounds__(256) bls_ragged_scale_kernel(gtrap_bls_curve *curves,
                                                                const float *__restrict__ t,
-                                                               const float *__restrict__ x) {
-  __shared__ double pm[8];
+                                                               const float *__restrict__ x,
+                                                               double xq_cap) {
+  __shared__ float pm[8];
   __shared__ uint32_t pc[8];
   const gtrap_bls_curve c = curves[blockIdx.x];
   const double off = (double)c.offset;
-  double amax = 0.0;
+  float amax = 0.0f;
   uint32_t cnt = 0;
   for (uint32_t i = threadIdx.x; i < c.n; i += 256) {
     const float tt = __ldg(t + c.off + i), xx = __ldg(x + c.off + i);
     if (tt >= 0.0f && isfinite(tt) && isfinite(xx) && isfinite((double)xx - off)) {
-      amax = fmax(amax, fabs((double)xx - off));
+      amax = fmaxf(amax, fabsf(__fsub_rz(xx, c.offset)));
       ++cnt;
     }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+    amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
     cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
   }
   if ((threadIdx.x & 31) == 0) { pm[threadIdx.x >> 5] = amax; pc[threadIdx.x >> 5] = cnt; }
   __syncthreads();
   if (threadIdx.x == 0) {
-    for (int w = 1; w < 8; ++w) { amax = fmax(amax, pm[w]); cnt += pc[w]; }
+    for (int w = 1; w < 8; ++w) { amax = fmaxf(amax, pm[w]); cnt += pc[w]; }
     const int CB = c.n ? 32 - __clz((int)c.n) : 1;  // counts <= n < 2^CB
     double xq_max = c.n ? ldexp(1.0, 62 - CB) / (double)c.n : 1.0;
-    if (xq_max > 1073741823.0) xq_max = 1073741823.0;
-    curves[blockIdx.x].sx = amax > 0.0 ? ilogb(xq_max) - ilogb(amax) - 1 : 0;
+    if (xq_max > xq_cap) xq_max = xq_cap;
+    curves[blockIdx.x].sx = amax > 0.0f ? ilogb(xq_max) - ilogbf(amax) - 1 : 0;
     curves[blockIdx.x].nv = cnt;
     curves[blockIdx.x].cb = CB;
   }
@@ -1184,6 +1188,25 @@ int bls_prep_image(const float *lc, const float *tu, const float *offset, uint32
   bls_pack_kernel<<<dim3((nq + 31) / 32, (n + 31) / 32), dim3(32, 8), 0, stream>>>(pa);
   return check_launch("bls_pack_kernel");
 }
+
+int ragged_pool(void *pool, size_t pool_bytes, uint64_t total, uint32_t flags, int32_t **X,
+                ulonglong2 **AB) {
+  return pool_carve(pool, pool_bytes, total, flags, X, AB);
+}
+
+int ragged_prepare(gtrap_bls_curve *curves, uint32_t ncurves, uint32_t max_n, const float *t,
+                   const float *x, uint64_t total, void *pool, size_t pool_bytes, uint32_t flags,
+                   double xq_cap, cudaStream_t stream) {
+  int32_t *X;
+  ulonglong2 *AB;
+  GTRAP_TRY(pool_carve(pool, pool_bytes, total, flags, &X, &AB));
+  bls_ragged_scale_kernel<<<ncurves, 256, 0, stream>>>(curves, t, x, xq_cap);
+  GTRAP_TRY(check_launch("bls_ragged_scale_kernel"));
+  const unsigned gx = (unsigned)((max_n + 1023) / 1024 > 0 ? (max_n + 1023) / 1024 : 1);
+  const unsigned gy = ncurves < 65535 ? ncurves : 65535;
+  bls_ragged_pack_kernel<<<dim3(gx, gy), 256, 0, stream>>>(curves, ncurves, t, x, X, AB);
+  return check_launch("bls_ragged_pack_kernel");
+}
 }  // namespace gtrap
 
 extern "C" {
@@ -1206,15 +1229,8 @@ int gtrap_bls_prepare(gtrap_bls_curve *curves, uint32_t ncurves, uint32_t max_n,
   if (ncurves == 0) return GTRAP_OK;
   if (!curves || !t || !x) return fail(GTRAP_ERR_INVALID_ARG, "bls_prepare: null pointer");
   if (max_n >= (1u << 23)) return fail(GTRAP_ERR_INVALID_ARG, "bls_prepare: max_n=%u must be below 2^23", max_n);
-  int32_t *X;
-  ulonglong2 *AB;
-  GTRAP_TRY(pool_carve(pool, pool_bytes, total_samples, flags, &X, &AB));
-  bls_ragged_scale_kernel<<<ncurves, 256, 0, stream>>>(curves, t, x);
-  GTRAP_TRY(gtrap::check_launch("bls_ragged_scale_kernel"));
-  const unsigned gx = (unsigned)((max_n + 1023) / 1024 > 0 ? (max_n + 1023) / 1024 : 1);
-  const unsigned gy = ncurves < 65535 ? ncurves : 65535;
-  bls_ragged_pack_kernel<<<dim3(gx, gy), 256, 0, stream>>>(curves, ncurves, t, x, X, AB);
-  return gtrap::check_launch("bls_ragged_pack_kernel");
+  return gtrap::ragged_prepare(curves, ncurves, max_n, t, x, total_samples, pool, pool_bytes, flags,
+                               1073741823.0, stream);
 }
 
 int gtrap_bls_offsets(gtrap_bls_curve *curves, uint32_t ncurves, const float *t, const float *resid,

@@ -51,6 +51,14 @@ int bls_prep_image(const float *lc, const float *tu, const float *offset, uint32
                    float fmin, float df, double xq_max, int32_t *sx, uint32_t *nv, int32_t *X,
                    ulonglong2 *AB, cudaStream_t stream);
 
+// Packed (ragged) batches: the per-sample pool of quantised flux and exact phase pairs, and its
+// prep with a caller-chosen bound on |quantised flux| (gtrap_bls_prepare, gtrap_tls_fold_prepare).
+int ragged_pool(void *pool, size_t pool_bytes, uint64_t total, uint32_t flags, int32_t **X,
+                ulonglong2 **AB);
+int ragged_prepare(gtrap_bls_curve *curves, uint32_t ncurves, uint32_t max_n, const float *t,
+                   const float *x, uint64_t total, void *pool, size_t pool_bytes, uint32_t flags,
+                   double xq_cap, cudaStream_t stream);
+
 inline bool is_pow2(uint32_t x) { return x && !(x & (x - 1)); }
 
 inline int ilog2u(uint32_t x) {

@@ -41,18 +41,92 @@ constexpr int kTfBatch = 4;  // samples a thread loads before folding them
 constexpr int32_t kMaskedQ = INT32_MIN;
 constexpr double kTfXqMax = 1048575.0;  // |quantised flux| < 2^20
 
+// Launch-wide template grid and shared-memory layout.
+struct TfShape {
+  uint32_t nb, dmax, nd;
+  uint32_t pbytes;           // bytes of the moment arrays (16-byte multiple)
+  int lognb;
+  float lfrac;
+  float W[kTfMaxDur];        // durations (days)
+};
+
+// One [nq, n] image (gtrap_tls_fold).
 struct TfArgs {
+  TfShape sh;
   const int32_t *X;          // [nq, n] quantised flux
   const ulonglong2 *AB;      // [nq, n] exact phase pairs
   const int32_t *sx;         // [nq]
   const uint32_t *nv;        // [nq]
-  uint32_t n, nq, nf, nb, dmax, nd, ngroups;
-  uint32_t pbytes;           // bytes of the moment arrays (16-byte multiple)
-  int lognb;
-  float fmin, df, lfrac;
-  float W[kTfMaxDur];        // durations (days)
+  uint32_t n, nq, nf, ngroups;
+  float fmin, df;
   float *tsr, *depth;
   uint32_t *start, *dur;
+};
+
+// One work item: frequencies j0 .. j0 + F - 1 of one curve, as the queue kernel keeps it in
+// shared memory.
+struct TfItem {
+  const int32_t *X;          // the curve's quantised flux
+  const ulonglong2 *AB;      // the curve's exact phase pairs
+  uint64_t out;              // the curve's first output element
+  uint32_t n, nf, nv, j0;
+  int sx;
+  float fmin, df;
+  int state;                 // 0 run, 1 skip (no frequency left in the group), 2 queue empty
+};
+
+// Item accessors of tf_item.  Image items read the launch parameters (nothing held in
+// registers over the body); queue items read the descriptor in shared memory.
+struct ImgItem {
+  const TfArgs &a;
+  uint32_t q, j0_;
+  __device__ const int32_t *X() const { return a.X + (size_t)q * a.n; }
+  __device__ const ulonglong2 *AB() const { return a.AB + (size_t)q * a.n; }
+  __device__ uint32_t n() const { return a.n; }
+  __device__ uint32_t nf() const { return a.nf; }
+  __device__ uint32_t nv() const { return a.nv[q]; }
+  __device__ uint32_t j0() const { return j0_; }
+  __device__ int sx() const { return a.sx[q]; }
+  __device__ float fmin() const { return a.fmin; }
+  __device__ float df() const { return a.df; }
+  __device__ size_t out() const { return (size_t)q * a.nf; }
+  __device__ float *tsr() const { return a.tsr; }
+  __device__ float *depth() const { return a.depth; }
+  __device__ uint32_t *start() const { return a.start; }
+  __device__ uint32_t *dur() const { return a.dur; }
+};
+
+struct QueueItem {
+  const TfItem &t;           // shared memory
+  float *tsr_, *depth_;
+  uint32_t *start_, *dur_;
+  __device__ const int32_t *X() const { return t.X; }
+  __device__ const ulonglong2 *AB() const { return t.AB; }
+  __device__ uint32_t n() const { return t.n; }
+  __device__ uint32_t nf() const { return t.nf; }
+  __device__ uint32_t nv() const { return t.nv; }
+  __device__ uint32_t j0() const { return t.j0; }
+  __device__ int sx() const { return t.sx; }
+  __device__ float fmin() const { return t.fmin; }
+  __device__ float df() const { return t.df; }
+  __device__ size_t out() const { return (size_t)t.out; }
+  __device__ float *tsr() const { return tsr_; }
+  __device__ float *depth() const { return depth_; }
+  __device__ uint32_t *start() const { return start_; }
+  __device__ uint32_t *dur() const { return dur_; }
+};
+
+// Persistent launch over (curve, frequency group) items of a packed batch.
+struct TfQueue {
+  const gtrap_bls_curve *curves;
+  const gtrap_bls_segment *segs;
+  const uint32_t *cum;       // [nseg + 1] item prefix over the segments
+  uint32_t nseg;
+  const int32_t *X;          // packed quantised flux
+  const ulonglong2 *AB;      // packed phase pairs
+  float *tsr, *depth;
+  uint32_t *start, *dur;
+  uint32_t *counter;         // next item (zeroed before the launch)
 };
 
 __device__ __forceinline__ long long shfl_up_ll(long long v, int o) {
@@ -86,8 +160,8 @@ __device__ __forceinline__ long long entry_g(long long y, uint32_t lo) {
 // pbytes; histogram f (nb flux words, then nb counts) at pbytes - 8 nb + 8 nb f.  Histogram 0 lies inside the moment arrays and is read into
 // registers before they are written; later histograms lie past them.  A frequency whose bins
 // need 64-bit flux sums refolds them into the first 8 nb bytes, below histogram 0.
-template <int F, int RM>
-__global__ void __launch_bounds__(kTfThreads, 2) tlsfold_kernel(const TfArgs a) {
+template <int F, int RM, class Item>
+__device__ __forceinline__ void tf_item(const TfShape &a, const Item &c) {
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ long long wsum[4][kTfWarps];
   __shared__ uint32_t wsumc[kTfWarps];
@@ -96,23 +170,23 @@ __global__ void __launch_bounds__(kTfThreads, 2) tlsfold_kernel(const TfArgs a) 
   __shared__ int sDL[F][kTfMaxDur];  // D | L << 16, 0 when skipped
   __shared__ unsigned long long best_s[F];
   __shared__ int s_bad;
-  const uint32_t q = blockIdx.x / a.ngroups, j0 = (blockIdx.x - q * a.ngroups) * F;
+  const uint32_t j0 = c.j0();
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nb = (int)a.nb, E = nb + (int)a.dmax + 1;
   longlong2 *GSK = reinterpret_cast<longlong2 *>(smraw);
   uint32_t *Glo = reinterpret_cast<uint32_t *>(GSK + E);
   uint32_t *hist = reinterpret_cast<uint32_t *>(smraw + a.pbytes) - 2 * nb;
   unsigned long long *S64 = reinterpret_cast<unsigned long long *>(smraw);
-  const int32_t *Xq = a.X + (size_t)q * a.n;
-  const ulonglong2 *ABq = a.AB + (size_t)q * a.n;
+  const int32_t *Xq = c.X();
+  const ulonglong2 *ABq = c.AB();
   const int shift = 64 - a.lognb;
 
   for (int b = tid; b < 2 * nb * F; b += kTfThreads) hist[b] = 0u;
   if (tid < F * 32) {
     const int f = tid >> 5, d = tid & 31;
     int v = 0;
-    if (d < (int)a.nd && j0 + f < a.nf) {
-      const float f0 = __fmaf_rn(a.df, (float)(j0 + f), a.fmin);
+    if (d < (int)a.nd && j0 + f < c.nf()) {
+      const float f0 = __fmaf_rn(c.df(), (float)(j0 + f), c.fmin());
       const int D = (int)rintf(a.W[d] * f0 * (float)nb);
       int L = max(1, (int)rintf(a.lfrac * (float)D));
       if (2 * L > D) L = D / 2;
@@ -124,14 +198,14 @@ __global__ void __launch_bounds__(kTfThreads, 2) tlsfold_kernel(const TfArgs a) 
   if (tid == 0) s_bad = 0;
   __syncthreads();
   // ---- fold: F histograms from one read of each sample; kTfBatch samples' loads in flight
-  for (uint32_t k0 = tid; k0 < a.n; k0 += kTfBatch * kTfThreads) {
+  for (uint32_t k0 = tid; k0 < c.n(); k0 += kTfBatch * kTfThreads) {
     int32_t xq[kTfBatch];
     ulonglong2 ab[kTfBatch];
 #pragma unroll
     for (int u = 0; u < kTfBatch; ++u) {
       const uint32_t k = k0 + u * kTfThreads;
-      xq[u] = k < a.n ? __ldg(Xq + k) : kMaskedQ;
-      ab[u] = k < a.n ? __ldg(ABq + k) : make_ulonglong2(0ull, 0ull);
+      xq[u] = k < c.n() ? __ldg(Xq + k) : kMaskedQ;
+      ab[u] = k < c.n() ? __ldg(ABq + k) : make_ulonglong2(0ull, 0ull);
     }
 #pragma unroll
     for (int u = 0; u < kTfBatch; ++u) {
@@ -151,11 +225,11 @@ __global__ void __launch_bounds__(kTfThreads, 2) tlsfold_kernel(const TfArgs a) 
   // RM = nb / 512 bins (and starts) a thread; RM = 1 also covers nb < 512, where the threads
   // past nb hold none
   const int b0 = tid * RM;
-  const float Nf = (float)a.nv[q];
+  const float Nf = (float)c.nv();
 #pragma unroll 1
   for (int f = 0; f < F; ++f) {
     const uint32_t jf = j0 + f;
-    if (jf >= a.nf) break;
+    if (jf >= c.nf()) break;
     const uint32_t *hS = hist + 2 * nb * f, *hC = hS + nb;
     // ---- moments of this thread's RM bins: counts, flux sums, and their first moments in
     // u = 2b + 1 (second moment for the counts), scanned over the block
@@ -198,7 +272,7 @@ __global__ void __launch_bounds__(kTfThreads, 2) tlsfold_kernel(const TfArgs a) 
     if (s_bad) {  // rare: refold this frequency's flux sums in 64 bits
       for (int b = tid; b < nb; b += kTfThreads) S64[b] = 0ull;
       __syncthreads();
-      for (uint32_t k = tid; k < a.n; k += kTfThreads) {
+      for (uint32_t k = tid; k < c.n(); k += kTfThreads) {
         const int32_t xq = __ldg(Xq + k);
         if (xq == kMaskedQ) continue;
         const ulonglong2 ab = __ldg(ABq + k);
@@ -343,10 +417,10 @@ __global__ void __launch_bounds__(kTfThreads, 2) tlsfold_kernel(const TfArgs a) 
     if (lane == 0 && bkey) atomicMax(&best_s[f], bkey);
     __syncthreads();
     if (tid == 0) {  // the moment arrays stay intact until the next frequency's first barrier
-      const size_t o = (size_t)q * a.nf + jf;
+      const size_t o = c.out() + jf;
       const unsigned long long k = best_s[f];
       if (!k) {
-        a.tsr[o] = 0.0f; a.depth[o] = 0.0f; a.start[o] = 0u; a.dur[o] = 0u;
+        c.tsr()[o] = 0.0f; c.depth()[o] = 0.0f; c.start()[o] = 0u; c.dur()[o] = 0u;
       } else {
         const unsigned di = 0xffffffffu - (unsigned)(k & 0xffffffffull);
         const int d = (int)(di >> 24), i = (int)(di & 0xffffffu);
@@ -359,13 +433,56 @@ __global__ void __launch_bounds__(kTfThreads, 2) tlsfold_kernel(const TfArgs a) 
         const long long B4 = entry_k(c3.y) - entry_k(c2.y) + entry_k(c1.y) - entry_k(c0.y) - 4LL * L * (g1 + g2);
         const double num = (double)N2 - (double)mean * (double)A2;
         const double den = (double)Nf * (double)B4 - (double)A2 * (double)A2;
-        const double sc = ldexp(1.0, -a.sx[q]);
-        a.tsr[o] = (float)(sqrt((double)__uint_as_float((unsigned)(k >> 32))) * sc);
-        a.depth[o] = (float)(-num * (double)Nf * (2.0 * L) / den * sc);
-        a.start[o] = (uint32_t)i;
-        a.dur[o] = (uint32_t)d;
+        const double sc = ldexp(1.0, -c.sx());
+        c.tsr()[o] = (float)(sqrt((double)__uint_as_float((unsigned)(k >> 32))) * sc);
+        c.depth()[o] = (float)(-num * (double)Nf * (2.0 * L) / den * sc);
+        c.start()[o] = (uint32_t)i;
+        c.dur()[o] = (uint32_t)d;
       }
     }
+  }
+}
+
+template <int F, int RM>
+__global__ void __launch_bounds__(kTfThreads, 2) tlsfold_kernel(const TfArgs a) {
+  const uint32_t q = blockIdx.x / a.ngroups;
+  tf_item<F, RM>(a.sh, ImgItem{a, q, (blockIdx.x - q * a.ngroups) * F});
+}
+
+// Persistent blocks pop items from the device counter.  The barrier at the top of the loop
+// orders the previous item's last reads of the descriptor before thread 0 rewrites it.
+template <int F, int RM>
+__global__ void __launch_bounds__(kTfThreads, 2) tlsfold_queue_kernel(const TfShape sh, const TfQueue qa) {
+  __shared__ TfItem item;
+  const uint32_t total = qa.cum[qa.nseg];
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const uint32_t it = atomicAdd(qa.counter, 1u);
+      if (it >= total) {
+        item.state = 2;
+      } else {
+        uint32_t lo = 0, hi = qa.nseg;  // segment k with cum[k] <= it < cum[k + 1]
+        while (hi - lo > 1) {
+          const uint32_t mid = (lo + hi) >> 1;
+          if (qa.cum[mid] <= it) lo = mid; else hi = mid;
+        }
+        const gtrap_bls_segment sg = qa.segs[lo];
+        const gtrap_bls_curve cv = qa.curves[sg.curve];
+        item.j0 = (sg.tile0 + (it - qa.cum[lo])) * F;
+        item.state = item.j0 >= cv.nf ? 1 : 0;
+        item.X = qa.X + cv.off;
+        item.AB = qa.AB + cv.off;
+        item.out = cv.out;
+        item.n = cv.n; item.nf = cv.nf; item.nv = cv.nv; item.sx = cv.sx;
+        item.fmin = cv.fmin; item.df = cv.df;
+      }
+    }
+    __syncthreads();
+    const int state = item.state;
+    if (state == 2) break;
+    if (state == 1) continue;
+    tf_item<F, RM>(sh, QueueItem{item, qa.tsr, qa.depth, qa.start, qa.dur});
   }
 }
 
@@ -378,6 +495,11 @@ size_t tf_smem(uint32_t nb, uint32_t dmax, int F) {
 }
 
 using TfKernel = void (*)(TfArgs);
+using TfQueueKernel = void (*)(TfShape, TfQueue);
+
+int tf_slot(int rm) { return rm == 1 ? 0 : rm == 2 ? 1 : rm == 4 ? 2 : 3; }
+
+int tf_rm(uint32_t nb) { return nb >= 4096 ? 8 : nb >= 2048 ? 4 : nb >= 1024 ? 2 : 1; }
 
 // nb = 4096 (8 bins a thread) leaves no room for a second histogram at two blocks an SM
 TfKernel tf_kernel(int F, int rm) {
@@ -385,7 +507,55 @@ TfKernel tf_kernel(int F, int rm) {
       {tlsfold_kernel<1, 1>, tlsfold_kernel<1, 2>, tlsfold_kernel<1, 4>, tlsfold_kernel<1, 8>},
       {tlsfold_kernel<2, 1>, tlsfold_kernel<2, 2>, tlsfold_kernel<2, 4>, nullptr},
       {tlsfold_kernel<3, 1>, tlsfold_kernel<3, 2>, tlsfold_kernel<3, 4>, nullptr}};
-  return table[F - 1][rm == 1 ? 0 : rm == 2 ? 1 : rm == 4 ? 2 : 3];
+  return table[F - 1][tf_slot(rm)];
+}
+
+TfQueueKernel tf_queue_kernel(int F, int rm) {
+  static const TfQueueKernel table[kTfMaxF][4] = {
+      {tlsfold_queue_kernel<1, 1>, tlsfold_queue_kernel<1, 2>, tlsfold_queue_kernel<1, 4>, tlsfold_queue_kernel<1, 8>},
+      {tlsfold_queue_kernel<2, 1>, tlsfold_queue_kernel<2, 2>, tlsfold_queue_kernel<2, 4>, nullptr},
+      {tlsfold_queue_kernel<3, 1>, tlsfold_queue_kernel<3, 2>, tlsfold_queue_kernel<3, 4>, nullptr}};
+  return table[F - 1][tf_slot(rm)];
+}
+
+int check_grid(uint32_t nb, uint32_t nd, uint32_t dmax, float lfrac, const char *what) {
+  if (!gtrap::is_pow2(nb) || nb < 32 || nb > 4096)
+    return fail(GTRAP_ERR_INVALID_ARG, "%s: nb=%u must be a power of two in [32, 4096]", what, nb);
+  if (nd == 0 || nd > (uint32_t)kTfMaxDur)
+    return fail(GTRAP_ERR_INVALID_ARG, "%s: nd=%u must be in [1, %d]", what, nd, kTfMaxDur);
+  if (dmax < 2 || dmax > nb) return fail(GTRAP_ERR_INVALID_ARG, "%s: dmax=%u must be in [2, nb]", what, dmax);
+  if (!(lfrac > 0.0f) || lfrac > 0.5f) return fail(GTRAP_ERR_INVALID_ARG, "%s: lfrac must be in (0, 0.5]", what);
+  return GTRAP_OK;
+}
+
+TfShape make_shape(uint32_t nb, uint32_t dmax, const float *durations, uint32_t nd, float lfrac) {
+  TfShape sh;
+  sh.nb = nb; sh.dmax = dmax; sh.nd = nd; sh.lognb = gtrap::ilog2u(nb);
+  sh.pbytes = (uint32_t)tf_pbytes(nb, dmax);
+  sh.lfrac = lfrac;
+  for (uint32_t d = 0; d < (uint32_t)kTfMaxDur; ++d) sh.W[d] = d < nd ? durations[d] : 0.0f;  // host array
+  return sh;
+}
+
+// Frequencies per block: the most (up to 3) that still keep two blocks on an SM, else 1.
+int pick_F(uint32_t nb, uint32_t dmax) {
+  const int rm = tf_rm(nb);
+#ifdef GTRAP_TF_F
+  return rm == 8 ? 1 : GTRAP_TF_F;
+#else
+  for (int c = kTfMaxF; c >= 2; --c) {
+    const TfKernel k = tf_kernel(c, rm);
+    if (!k) continue;
+    if (gtrap::ensure_smem((const void *)k, tf_smem(nb, dmax, c), "tls_fold") != GTRAP_OK) continue;
+    int nblk = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nblk, k, kTfThreads, tf_smem(nb, dmax, c)) != cudaSuccess) {
+      cudaGetLastError();
+      continue;
+    }
+    if (nblk >= 2) return c;
+  }
+  return 1;
+#endif
 }
 
 }  // namespace
@@ -407,10 +577,7 @@ int gtrap_tls_fold(float *tsr, uint32_t *start, uint32_t *dur, float *depth, con
   if (!tsr || !start || !dur || !depth || !lc || !tu || !offset || !durations)
     return fail(GTRAP_ERR_INVALID_ARG, "tls_fold: null pointer");
   if (n == 0 || n >= (1u << 20)) return fail(GTRAP_ERR_INVALID_ARG, "tls_fold: n=%u must be in [1, 2^20)", n);
-  if (!is_pow2(nb) || nb < 32 || nb > 4096) return fail(GTRAP_ERR_INVALID_ARG, "tls_fold: nb=%u must be a power of two in [32, 4096]", nb);
-  if (nd == 0 || nd > (uint32_t)kTfMaxDur) return fail(GTRAP_ERR_INVALID_ARG, "tls_fold: nd=%u must be in [1, %d]", nd, kTfMaxDur);
-  if (dmax < 2 || dmax > nb) return fail(GTRAP_ERR_INVALID_ARG, "tls_fold: dmax=%u must be in [2, nb]", dmax);
-  if (!(lfrac > 0.0f) || lfrac > 0.5f) return fail(GTRAP_ERR_INVALID_ARG, "tls_fold: lfrac must be in (0, 0.5]");
+  GTRAP_TRY(check_grid(nb, nd, dmax, lfrac, "tls_fold"));
   if (!workspace || ((uintptr_t)workspace & 255))
     return fail(GTRAP_ERR_WORKSPACE, "tls_fold: workspace must be a 256-byte aligned device pointer");
   if (workspace_bytes < gtrap_tls_fold_workspace_size(n, nq))
@@ -423,37 +590,73 @@ int gtrap_tls_fold(float *tsr, uint32_t *start, uint32_t *dur, float *depth, con
   ulonglong2 *AB = cv.take<ulonglong2>((size_t)nq * n);
   GTRAP_TRY(bls_prep_image(lc, tu, offset, n, nq, fmin, df, kTfXqMax, sx, nv, X, AB, stream));
   TfArgs a;
+  a.sh = make_shape(nb, dmax, durations, nd, lfrac);
   a.X = X; a.AB = AB; a.sx = sx; a.nv = nv;
-  a.n = n; a.nq = nq; a.nf = nf; a.nb = nb; a.dmax = dmax; a.nd = nd; a.lognb = ilog2u(nb);
-  a.pbytes = (uint32_t)tf_pbytes(nb, dmax);
-  a.fmin = fmin; a.df = df; a.lfrac = lfrac;
-  for (uint32_t d = 0; d < (uint32_t)kTfMaxDur; ++d) a.W[d] = d < nd ? durations[d] : 0.0f;  // host array
+  a.n = n; a.nq = nq; a.nf = nf;
+  a.fmin = fmin; a.df = df;
   a.tsr = tsr; a.depth = depth; a.start = start; a.dur = dur;
-  const int rm = nb >= 4096 ? 8 : nb >= 2048 ? 4 : nb >= 1024 ? 2 : 1;
-  // frequencies per block: the most (up to 3) that still keep two blocks on an SM, else 1
-  int F = 1;
-#ifdef GTRAP_TF_F
-  F = rm == 8 ? 1 : GTRAP_TF_F;
-#else
-  for (int c = kTfMaxF; c >= 2; --c) {
-    const TfKernel k = tf_kernel(c, rm);
-    if (!k) continue;
-    if (ensure_smem((const void *)k, tf_smem(nb, dmax, c), "tls_fold") != GTRAP_OK) continue;
-    int nblk = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nblk, k, kTfThreads, tf_smem(nb, dmax, c)) != cudaSuccess) {
-      cudaGetLastError();
-      continue;
-    }
-    if (nblk >= 2) { F = c; break; }
-  }
-#endif
+  const int F = pick_F(nb, dmax);
   a.ngroups = (nf + F - 1) / F;
   if ((uint64_t)nq * a.ngroups >= (1ull << 31)) return fail(GTRAP_ERR_INVALID_ARG, "tls_fold: nq*nf too large");
-  const TfKernel k = tf_kernel(F, rm);
+  const TfKernel k = tf_kernel(F, tf_rm(nb));
   const size_t smem = tf_smem(nb, dmax, F);
   GTRAP_TRY(ensure_smem((const void *)k, smem, "tls_fold"));
   k<<<(unsigned)(nq * a.ngroups), kTfThreads, smem, stream>>>(a);
   return check_launch("tlsfold_kernel");
+}
+
+uint32_t gtrap_tls_fold_item_frequencies(uint32_t nb, uint32_t dmax) {
+  if (!gtrap::is_pow2(nb) || nb < 32 || nb > 4096 || dmax < 2 || dmax > nb) return 0;
+  return (uint32_t)pick_F(nb, dmax);
+}
+
+int gtrap_tls_fold_prepare(gtrap_bls_curve *curves, uint32_t ncurves, uint32_t max_n, const float *t,
+                           const float *x, uint64_t total_samples, void *pool, size_t pool_bytes,
+                           gtrap_stream_t stream) {
+  if (ncurves == 0) return GTRAP_OK;
+  if (!curves || !t || !x) return fail(GTRAP_ERR_INVALID_ARG, "tls_fold_prepare: null pointer");
+  if (max_n >= (1u << 20)) return fail(GTRAP_ERR_INVALID_ARG, "tls_fold_prepare: max_n=%u must be below 2^20", max_n);
+  return gtrap::ragged_prepare(curves, ncurves, max_n, t, x, total_samples, pool, pool_bytes, 0u, kTfXqMax,
+                               stream);
+}
+
+int gtrap_tls_fold_run(const gtrap_bls_curve *curves, const gtrap_bls_segment *segs, const uint32_t *cum,
+                       uint32_t nseg, const void *pool, size_t pool_bytes, uint64_t total_samples,
+                       uint32_t nb, const float *durations, uint32_t nd, float lfrac, uint32_t dmax,
+                       uint32_t F, uint32_t blocks, uint32_t *counter, float *tsr, uint32_t *start,
+                       uint32_t *dur, float *depth, gtrap_stream_t stream) {
+  using namespace gtrap;
+  if (nseg == 0) return GTRAP_OK;
+  if (!curves || !segs || !cum || !counter || !durations || !tsr || !start || !dur || !depth)
+    return fail(GTRAP_ERR_INVALID_ARG, "tls_fold_run: null pointer");
+  GTRAP_TRY(check_grid(nb, nd, dmax, lfrac, "tls_fold_run"));
+  const int rm = tf_rm(nb);
+  if (F == 0 || F > (uint32_t)kTfMaxF || !tf_queue_kernel((int)F, rm))
+    return fail(GTRAP_ERR_INVALID_ARG, "tls_fold_run: F=%u frequencies per item is not built for nb=%u", F, nb);
+  int32_t *X;
+  ulonglong2 *AB;
+  GTRAP_TRY(ragged_pool(const_cast<void *>(pool), pool_bytes, total_samples, 0u, &X, &AB));
+  TfQueue qa;
+  qa.curves = curves; qa.segs = segs; qa.cum = cum; qa.nseg = nseg;
+  qa.X = X; qa.AB = AB;
+  qa.tsr = tsr; qa.depth = depth; qa.start = start; qa.dur = dur;
+  qa.counter = counter;
+  const TfShape sh = make_shape(nb, dmax, durations, nd, lfrac);
+  const TfQueueKernel k = tf_queue_kernel((int)F, rm);
+  const size_t smem = tf_smem(nb, dmax, (int)F);
+  GTRAP_TRY(ensure_smem((const void *)k, smem, "tls_fold_run"));
+  if (blocks == 0) {  // as many as fit on the SMs at once (the queue keeps them busy)
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kTfThreads, smem) != cudaSuccess) {
+      cudaGetLastError();
+      per_sm = 1;
+    }
+    blocks = (uint32_t)(sm_count() * (per_sm > 0 ? per_sm : 1));
+  }
+  cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), stream);
+  if (e != cudaSuccess) return fail(GTRAP_ERR_CUDA, "tls_fold_run: cudaMemsetAsync: %s", cudaGetErrorString(e));
+  k<<<blocks, kTfThreads, smem, stream>>>(sh, qa);
+  return check_launch("tlsfold_queue_kernel");
 }
 
 }  // extern "C"

@@ -281,6 +281,27 @@ int gtrap_tls_fold(float *tsr, uint32_t *start, uint32_t *dur, float *depth, con
                    float lfrac, uint32_t dmax, void *workspace, size_t workspace_bytes,
                    gtrap_stream_t stream);
 
+/* Packed (ragged) folded trapezoid searches, in the layout of the packed BLS batches:
+ * curve q (gtrap_bls_curve; off, out, n, nf, fmin, df, offset used) owns samples
+ * [off, off + n) of the packed arrays and outputs [out, out + nf).  An item of a segment is a
+ * group of F frequencies (item t covers [t*F, min((t+1)*F, nf))); F must be the value
+ * gtrap_tls_fold_item_frequencies returns for the grid (0: grid out of range).  The pool has
+ * the layout of gtrap_bls_pool_bytes(total_samples, 0) and may be shared with BLS curves of
+ * other sample ranges.  Each curve's outputs are bit-identical to gtrap_tls_fold on that
+ * curve alone with offset[q] = curves[q].offset. */
+uint32_t gtrap_tls_fold_item_frequencies(uint32_t nb, uint32_t dmax);
+/* Quantise (|xq| < 2^20) and phase-encode the curves' samples; fills sx and nv. */
+int gtrap_tls_fold_prepare(gtrap_bls_curve *curves, uint32_t ncurves, uint32_t max_n, const float *t,
+                           const float *x, uint64_t total_samples, void *pool, size_t pool_bytes,
+                           gtrap_stream_t stream);
+/* Persistent blocks (0: as many as fit at once) pop items from a device counter (zeroed by
+ * the call).  durations: host array of nd values. */
+int gtrap_tls_fold_run(const gtrap_bls_curve *curves, const gtrap_bls_segment *segs, const uint32_t *cum,
+                       uint32_t nseg, const void *pool, size_t pool_bytes, uint64_t total_samples,
+                       uint32_t nb, const float *durations, uint32_t nd, float lfrac, uint32_t dmax,
+                       uint32_t F, uint32_t blocks, uint32_t *counter, float *tsr, uint32_t *start,
+                       uint32_t *dur, float *depth, gtrap_stream_t stream);
+
 /* ---------------------------------------------------------------------------
  * Candidate windows for the classifier.  Replaces pick_Wnormalized_cleaned_lc_direct
  * (gtrap/picktrap.py:27-172) for a batch of candidates: candidate c lies on curve curve[c]
