@@ -74,6 +74,9 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-plain", action="store_true")
+    p.add_argument("--tls-kind", default="gtls", choices=["gtls", "fold"],
+                   help="ragged workload: search the TLS-kind curves with GTLS (reference semantics) or "
+                        "the folded trapezoid search")
     return p.parse_args()
 
 
@@ -86,18 +89,24 @@ def masked_config(nq):
             "phase": "exact 64-bit fixed point", "l2": "inputs 512 MiB per GPU exceed L2 (no flush needed)"}
 
 
-def ragged_config(nc, bat=None):
-    cfg = {"workload": "uneven mixed BLS/GTLS batch: %d curves, n log-uniform [2000, 70000], cadence 2 or "
+def ragged_config(nc, bat=None, tls_kind="gtls"):
+    if tls_kind == "fold":
+        tls_desc = ("TLS curves through the folded trapezoid search (nb %d, 8 durations 0.5..8 h, ingress 0.2, "
+                    "longest template %d bins) on the BLS frequency rule" % (TF_NB, TF_DMAX))
+    else:
+        tls_desc = "GTLS nw=%d nl=%d (W 8 h..0.5 h), every sample an epoch" % (NW, NL)
+    cfg = {"workload": "uneven mixed BLS/%s batch: %d curves, n log-uniform [2000, 70000], cadence 2 or "
                        "29.4 min, 10%% masked, median window 49; BLS nb=%d kma=%d kmi=%d kkmi=n*%g, "
-                       "nf=clip(next_pow2(8*baseline_d), 2048, 32768) from 2/baseline to 2 /d; GTLS "
-                       "nw=%d nl=%d (W 8 h..0.5 h), every sample an epoch; one persistent launch per "
-                       "search kind, CUDA graphs, autotuned tiles" % (nc, NB, KMA, KMI, QMI, NW, NL),
+                       "nf=clip(next_pow2(8*baseline_d), 2048, 32768) from 2/baseline to 2 /d; %s; one "
+                       "persistent launch per search kind, CUDA graphs, autotuned tiles"
+                       % ("folded TLS" if tls_kind == "fold" else "GTLS", nc, NB, KMA, KMI, QMI, tls_desc),
            "curves_per_gpu": nc, "nb": NB, "kma": KMA, "kmi": KMI, "nw": NW, "nl": NL,
            "median_window": 2 * R_MEDIAN + 1, "phase": "exact 64-bit fixed point",
            "l2": "inputs of several GB per GPU exceed L2 (no flush needed)"}
     if bat is not None:
         cfg.update({"bls_curves": bat.n_bls, "tls_curves": bat.n_tls, "bls_evals": bat.bls_evals,
-                    "tls_evals": bat.tls_evals, "samples_total": bat.total,
+                    "tls_evals": bat.tls_evals, "fold_curves": bat.n_fold, "fold_evals": bat.fold_evals,
+                    "samples_total": bat.total,
                     "tile_frequencies": bat.F, "bls_blocks": bat.bls_blocks, "tls_blocks": bat.tls_blocks})
     return cfg
 
@@ -406,13 +415,27 @@ def make_mix(nc, seed):
     return synth.ragged_mix(nc, seed=seed)
 
 
-def build_batch(mix, dev_index):
+def fold_grid(c):
+    """Frequency grid of a TLS-kind curve sent to the folded search: the BLS rule,
+    nf = clip(next_pow2(8 * baseline_d), 2048, 32768) from 2/baseline to 2 per day."""
+    from gtrap_gb300 import synth
+    T = float(c["t"].max())
+    nf = int(min(32768, max(2048, synth.next_pow2(8.0 * T))))
+    fmin = 2.0 / T
+    return nf, float(np.float32(fmin)), float(np.float32((2.0 - fmin) / (nf - 1)))
+
+
+def build_batch(mix, dev_index, tls_kind="gtls"):
     from gtrap_gb300 import batch as B
     bat = B.RaggedBatch(B.BlsSpec(nb=NB, kma=KMA, kmi=KMI), B.TlsSpec(nw=NW, nl=NL),
-                        detrend_r=R_MEDIAN, device=dev_index)
+                        detrend_r=R_MEDIAN, device=dev_index,
+                        fold=B.FoldSpec(nb=TF_NB, durations=tuple(float(w) for w in TF_DURS), lfrac=TF_LFRAC,
+                                        dmax=TF_DMAX))
     for c in mix:
         if c["kind"] == "bls":
             bat.add_bls(c["t"], c["x"], c["nf"], c["fmin"], c["df"], kkmi=c["kkmi"])
+        elif tls_kind == "fold":
+            bat.add_fold(c["t"], c["x"], *fold_grid(c))
         else:
             bat.add_tls(c["t"], c["x"], c["nsc"], c["wmax"], c["dw"], c["deltat"])
     return bat.build()
@@ -519,7 +542,7 @@ def run_ragged(args, rank, world, local_rank):
     dev = torch.device("cuda", local_rank)
     nc = args.nq or NCURVES
     mix = make_mix(nc, 4000 + 100000 * rank)
-    bat = build_batch(mix, local_rank)
+    bat = build_batch(mix, local_rank, args.tls_kind)
     stream = torch.cuda.current_stream(dev)
     B.autotune(bat)
     graphs = bat.capture_stages()
@@ -540,7 +563,9 @@ def run_ragged(args, rank, world, local_rank):
         if timed:
             b.record(stream)
             marks.append((a, b))
-        graphs["tls"].replay()
+        for name in ("fold", "tls"):
+            if name in graphs:
+                graphs[name].replay()
 
     for _ in range(args.warmup):
         step()
@@ -561,11 +586,12 @@ def run_ragged(args, rank, world, local_rank):
     if world > 1:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
     ms, bls_ms = float(t[0]), float(t[1])
-    evals_rank = bat.bls_evals + bat.tls_evals
+    evals_rank = bat.bls_evals + bat.fold_evals + bat.tls_evals
     evals = evals_rank * world
     value = evals / (ms / 1e3)
     ref = [bat.bls_result(k) for k in range(0, bat.n_bls, max(1, bat.n_bls // 64))]
     ref_t = [bat.tls_result(k) for k in range(0, bat.n_tls, max(1, bat.n_tls // 64))]
+    ref_f = [bat.fold_result(k) for k in range(0, bat.n_fold, max(1, bat.n_fold // 64))]
 
     e2e = None
     if not args.no_e2e:
@@ -573,10 +599,11 @@ def run_ragged(args, rank, world, local_rank):
         # pinned host memory and its spectra back.  Two device buffer sets (a second batch with
         # the same configuration and graphs) let step k+1's upload and step k-1's download run
         # on copy streams under step k's kernels; every step's copies stay inside the region.
-        bat2 = build_batch(mix, local_rank)
+        bat2 = build_batch(mix, local_rank, args.tls_kind)
         bat2.set_config(bat.F, bat.bls_blocks, bat.tls_blocks)
         sets = [(bat, graphs), (bat2, bat2.capture_stages())]
-        outs = lambda b: (b.blsp, b.ph1, b.ph2) + tuple(b.tls_outs)
+        outs = lambda b: (b.blsp, b.ph1, b.ph2) + tuple(b.tls_outs if b.n_tls else ()) + \
+            tuple(b.fold_outs if b.n_fold else ())
         h_t = bat.t.cpu().pin_memory()
         h_x = bat.x.cpu().pin_memory()
         h_o = [[torch.empty(a.numel(), dtype=a.dtype).pin_memory() for a in outs(b)] for b, _ in sets]
@@ -599,9 +626,9 @@ def run_ragged(args, rank, world, local_rank):
                 stream.wait_event(up)
                 if done_d[i] is not None:  # set i's previous spectra are on the host
                     stream.wait_event(done_d[i])
-                gr["prep"].replay()
-                gr["bls"].replay()
-                gr["tls"].replay()
+                for name in ("prep", "bls", "fold", "tls"):
+                    if name in gr:
+                        gr[name].replay()
                 done_c[i] = torch.cuda.Event()
                 done_c[i].record(stream)
                 s_down.wait_event(done_c[i])
@@ -637,7 +664,8 @@ def run_ragged(args, rank, world, local_rank):
     plain = None
     if not args.no_plain:
         # the same requests, one plain launch sequence per curve (warm-up on a few curves)
-        B.run_plain(bat, bls_curves=range(min(8, bat.n_bls)), tls_curves=range(min(8, bat.n_tls)))
+        B.run_plain(bat, bls_curves=range(min(8, bat.n_bls)), tls_curves=range(min(8, bat.n_tls)),
+                    fold_curves=range(min(8, bat.n_fold)))
         barrier()
         s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         w0 = time.perf_counter()
@@ -653,9 +681,11 @@ def run_ragged(args, rank, world, local_rank):
                    for x, y in zip(a, bat.bls_result(k)))
         same = same and all(np.array_equal(x, y) for a, k in zip(ref_t, range(0, bat.n_tls, max(1, bat.n_tls // 64)))
                             for x, y in zip(a, bat.tls_result(k)))
+        same = same and all(np.array_equal(x, y) for a, k in zip(ref_f, range(0, bat.n_fold, max(1, bat.n_fold // 64)))
+                            for x, y in zip(a, bat.fold_result(k)))
         plain = {"value": evals / (float(pms[0]) / 1e3), "unit": UNIT, "ms_per_step": float(pms[0]),
                  "what": "same requests through the plain per-curve entry points (gfilter, get_offset, "
-                         "geebls or gtls per curve), one pass",
+                         "geebls, tls_fold or gtls per curve), one pass",
                  "bit_identical_sampled_outputs": bool(same)}
         step()  # restore the batch's own outputs
 
@@ -679,20 +709,20 @@ def run_ragged(args, rank, world, local_rank):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+i64", "data": "synthetic",
-            "config": ragged_config(nc, bat) | {"parallelism": "replicas x%d (curves sharded)" % world},
+            "config": ragged_config(nc, bat, args.tls_kind) | {"parallelism": "replicas x%d (curves sharded)" % world},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "kernel": "bls_queue_kernel (persistent BLS fold + scan)", "kernel_ms": bls_ms,
                          "kernel_share": bls_ms / ms,
                          "peak_source": "live FP32 FMA-chain probe on this GPU (MEASURED_PEAKS.json has no FP32 figure)",
                          "flop_per_eval": flop_per_eval, "fold": fold_leg},
-            "gpu_launches": 6 * args.steps,
+            "gpu_launches": (1 + 4 * (bat.n_bls > 0) + 4 * (bat.n_fold > 0) + (bat.n_tls > 0)) * args.steps,
             "clocks": clk}
     if plain:
         line["plain"] = plain
     if e2e:
         line["e2e"] = e2e
-    if not args.no_cpu_baseline:
+    if not args.no_cpu_baseline and args.tls_kind == "gtls":
         line["cpu_baseline"] = ragged_cpu_baseline(mix)
     print(json.dumps(line), flush=True)
 

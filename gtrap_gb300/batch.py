@@ -471,16 +471,19 @@ class RaggedBatch:
         return g
 
     def capture_stages(self) -> dict:
-        """Capture prep, BLS, folded search and GTLS as four graphs ({"prep", "bls", "fold",
-        "tls"}), so that events recorded between their replays time each stage."""
+        """Capture prep, BLS, folded search and GTLS as separate graphs ({"prep", "bls",
+        "fold", "tls"}; a kind without requests has none), so that events recorded between
+        their replays time each stage."""
         side = torch.cuda.Stream(self.device)
         side.wait_stream(torch.cuda.current_stream(self.device))
         with torch.cuda.stream(side):
             self.launch()
         torch.cuda.current_stream(self.device).wait_stream(side)
         graphs = {}
-        for name, fn in (("prep", self.launch_prep), ("bls", self.launch_bls), ("fold", self.launch_fold),
-                         ("tls", self.launch_tls)):
+        for name, fn, count in (("prep", self.launch_prep, 1), ("bls", self.launch_bls, self.n_bls),
+                                ("fold", self.launch_fold, self.n_fold), ("tls", self.launch_tls, self.n_tls)):
+            if not count:
+                continue
             g = torch.cuda.CUDAGraph()
             with torch.cuda.graph(g, capture_error_mode="thread_local"):
                 fn()

@@ -1,19 +1,20 @@
 """Continuous-batching transit search on one GPU.
 
-Requests (one light curve each, with a BLS frequency grid or a GTLS template grid) arrive at
-any time.  The server keeps every admitted request's samples, encoded BLS samples and outputs
+Requests (one light curve each, with a BLS frequency grid, a folded trapezoid-search frequency
+grid or a GTLS template grid) arrive at any time.  The server keeps every admitted request's samples, encoded BLS samples and outputs
 in device-resident arenas sized by an HBM budget, and runs in steps.  A step
 
 1. admits waiting requests in arrival order while their samples and outputs fit in the free
    space of the arenas (admission by HBM budget; a request waits until earlier ones free
    memory) and copies their samples to the device on a copy stream,
-2. detrends the newly admitted curves (``gtrap_gfilter_packed``), computes their BLS offsets
-   and encodes their BLS samples (``gtrap_bls_offsets``, ``gtrap_bls_prepare``),
-3. runs a bounded slice of work: up to ``bls_tiles`` (curve, frequency tile) items and
-   ``tls_tiles`` (curve, 64-epoch tile) items taken from the oldest in-flight requests, in one
-   persistent BLS launch and one persistent GTLS launch (``gtrap_bls_run``,
-   ``gtrap_gtls_run``), so tiles of many requests run side by side and a long request spans
-   several steps while newer requests join, and
+2. detrends the newly admitted curves (``gtrap_gfilter_packed``), computes the offsets of the
+   BLS and folded-search curves and encodes their samples (``gtrap_bls_offsets``,
+   ``gtrap_bls_prepare``, ``gtrap_tls_fold_prepare``),
+3. runs a bounded slice of work: up to ``bls_tiles`` (curve, frequency tile) items,
+   ``fold_tiles`` (curve, frequency group) items and ``tls_tiles`` (curve, 64-epoch tile) items
+   taken from the oldest in-flight requests, in one persistent launch per kind
+   (``gtrap_bls_run``, ``gtrap_tls_fold_run``, ``gtrap_gtls_run``), so tiles of many requests
+   run side by side and a long request spans several steps while newer requests join, and
 4. when a request's last tile has run, copies its outputs to the host on a second copy stream
    and frees its memory.  With ``tls_peaks`` a GTLS request returns only its peak statistics
    (``gtrap_peakstat``, computed on the device in the step that finishes it) instead of its
@@ -36,7 +37,7 @@ import torch
 
 from . import _native as N
 from . import api
-from .batch import BLS_CURVE, SEGMENT, TLS_CURVE, TLS_TILE, BlsSpec, TlsSpec, default_F
+from .batch import BLS_CURVE, SEGMENT, TLS_CURVE, TLS_TILE, BlsSpec, FoldSpec, TlsSpec, default_F
 from ._dev import as_ptr, require_cuda
 
 SAMPLE_BYTES = 32   # t, x, detrended x (4 B each) + quantised flux (4 B) + phase pair (16 B)
@@ -46,8 +47,9 @@ ALIGN = 32          # arena granularity (elements)
 
 @dataclass
 class Request:
-    """One light curve and its search grid.  ``kind`` is "bls" (nf, fmin, df, kkmi, ntrue)
-    or "tls" (nsc, wmax, dw, deltat; epochs = samples)."""
+    """One light curve and its search grid.  ``kind`` is "bls" (nf, fmin, df, kkmi, ntrue),
+    "fold" (the folded trapezoid search over nf, fmin, df) or "tls" (nsc, wmax, dw, deltat;
+    epochs = samples)."""
     kind: str
     t: np.ndarray
     x: np.ndarray
@@ -67,7 +69,7 @@ class Request:
 
     @property
     def outputs(self) -> int:
-        return int(self.nf) if self.kind == "bls" else self.n
+        return int(self.nf) if self.kind in ("bls", "fold") else self.n
 
     @staticmethod
     def from_curve(c: dict) -> "Request":
@@ -84,8 +86,9 @@ class Result:
     arrival: float
     admitted: float
     done: float
-    outputs: tuple   # bls: (blsp, phase1, phase2); tls: (sn, w, t0, l, hmax), or with
-    #                  tls_peaks (PEAK_STATS record, peak indices, peak heights)
+    outputs: tuple   # bls: (blsp, phase1, phase2); fold: (tsr, start, duration index, depth);
+    #                  tls: (sn, w, t0, l, hmax), or with tls_peaks (PEAK_STATS record, peak
+    #                  indices, peak heights)
     evals: int
 
     @property
@@ -194,7 +197,7 @@ class _Step:
 
 
 class TransitServer:
-    """Continuous-batching BLS/GTLS server (see the module docstring).
+    """Continuous-batching BLS, folded-search and GTLS server (see the module docstring).
 
     ``hbm_budget`` bytes are split between the sample arena (``SAMPLE_BYTES`` per sample)
     and the output arena (``OUTPUT_BYTES`` per output element) in the ratio
@@ -204,14 +207,19 @@ class TransitServer:
     def __init__(self, bls: BlsSpec = BlsSpec(), tls: TlsSpec = TlsSpec(), detrend_r: int = 24,
                  hbm_budget: float = 100e9, sample_share: float = 0.8, bls_tiles: int | None = None,
                  tls_tiles: int | None = None, F: int | None = None, max_requests: int = 1 << 16,
-                 depth: int = 2, tls_peaks: dict | None = None, device=None):
+                 depth: int = 2, tls_peaks: dict | None = None, device=None, fold: FoldSpec = FoldSpec(),
+                 fold_tiles: int | None = None):
         require_cuda()
         self.dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
-        self.bls_spec, self.tls_spec = bls, tls
+        self.bls_spec, self.tls_spec, self.fold_spec = bls, tls, fold
         self.r = int(detrend_r)
         self.F = int(F) if F else default_F(bls)
+        self.fold_F = int(N.fn("gtrap_tls_fold_item_frequencies")(fold.nb, fold.dmax_bins))
+        if self.fold_F == 0:
+            raise ValueError("folded-search grid nb=%d, dmax=%d is out of range" % (fold.nb, fold.dmax_bins))
         sms = torch.cuda.get_device_properties(self.dev).multi_processor_count
         self.bls_tiles = int(bls_tiles) if bls_tiles else sms * 2 * 8
+        self.fold_tiles = int(fold_tiles) if fold_tiles else sms * 2 * 8
         self.tls_tiles = int(tls_tiles) if tls_tiles else sms * 64
         self.depth = max(1, int(depth))
         self.tls_peaks = None if tls_peaks is None else dict(mpd=10, ntop=4, k=8) | dict(tls_peaks)
@@ -223,25 +231,29 @@ class TransitServer:
         self.samples = Arena(self.sample_cap)
         self.outs = Arena(self.out_cap)
         self.bls_desc = Arena(max_requests, align=1)
+        self.fold_desc = Arena(max_requests, align=1)
         self.tls_desc = Arena(max_requests, align=1)
         d = self.dev
         self.t = torch.zeros(self.sample_cap, dtype=torch.float32, device=d)
         self.x = torch.zeros(self.sample_cap, dtype=torch.float32, device=d)
         self.resid = torch.zeros(self.sample_cap, dtype=torch.float32, device=d)
-        self.pool_bytes = int(N.fn("gtrap_bls_pool_bytes")(self.sample_cap, bls.flags))
+        # quantised flux and phase pairs (the folded search needs the pairs in every phase mode)
+        self.pool_bytes = int(N.fn("gtrap_bls_pool_bytes")(self.sample_cap, 0))
         self.pool = torch.empty(self.pool_bytes, dtype=torch.uint8, device=d)
         self.o = [torch.zeros(self.out_cap, dtype=torch.float32, device=d) for _ in range(5)]
         self.bls_table = torch.zeros(max_requests * BLS_CURVE.itemsize, dtype=torch.uint8, device=d)
         self.tls_table = torch.zeros(max_requests * TLS_CURVE.itemsize, dtype=torch.uint8, device=d)
-        self.counters = torch.zeros(2, dtype=torch.int32, device=d)
+        self.fold_table = torch.zeros(max_requests * BLS_CURVE.itemsize, dtype=torch.uint8, device=d)
+        self.counters = torch.zeros(3, dtype=torch.int32, device=d)
         self.hbm_bytes = (self.sample_cap * SAMPLE_BYTES + self.out_cap * OUTPUT_BYTES +
-                          2 * max_requests * 64)
+                          3 * max_requests * 64)
         self.stream = torch.cuda.Stream(d)
         self.staging = _Staging(self.depth)
         self.h2d = torch.cuda.Stream(d)
         self.d2h = torch.cuda.Stream(d)
         self.waiting: collections.deque = collections.deque()
         self.live_bls: list = []
+        self.live_fold: list = []
         self.live_tls: list = []
         self.steps: collections.deque = collections.deque()
         self.draining: list = []
@@ -253,14 +265,16 @@ class TransitServer:
     # -- requests -----------------------------------------------------------------------
     def submit(self, req: Request, arrival: float | None = None) -> int:
         n = req.n
-        if req.kind not in ("bls", "tls"):
-            raise ValueError("kind must be 'bls' or 'tls'")
+        if req.kind not in ("bls", "fold", "tls"):
+            raise ValueError("kind must be 'bls', 'fold' or 'tls'")
         if n == 0 or np.asarray(req.x).size != n:
             raise ValueError("a request needs n >= 1 samples of time and flux")
         if n > self.samples.cap or req.outputs > self.outs.cap:
             raise ValueError("request of %d samples / %d outputs exceeds the HBM budget" % (n, req.outputs))
         if req.kind == "bls" and (req.nf < 1 or n >= 1 << 23):
             raise ValueError("BLS requests need nf >= 1 and n < 2^23")
+        if req.kind == "fold" and (req.nf < 1 or n >= 1 << 20):
+            raise ValueError("folded-search requests need nf >= 1 and n < 2^20")
         if req.kind == "tls" and not 1 <= req.nsc <= 65536 - 31:
             raise ValueError("GTLS requests need nsc in [1, 65505]")
         rid = self.next_rid
@@ -270,7 +284,11 @@ class TransitServer:
 
     @property
     def idle(self) -> bool:
-        return not (self.waiting or self.live_bls or self.live_tls or self.steps or self.draining)
+        return not (self.waiting or self.live_bls or self.live_fold or self.live_tls or self.steps or
+                    self.draining)
+
+    def _desc_arena(self, kind):
+        return self.bls_desc if kind == "bls" else self.fold_desc if kind == "fold" else self.tls_desc
 
     # -- one step -------------------------------------------------------------------------
     def _admit(self, now):
@@ -278,7 +296,7 @@ class TransitServer:
         while self.waiting:
             lv = self.waiting[0]
             req = lv.req
-            desc_arena = self.bls_desc if req.kind == "bls" else self.tls_desc
+            desc_arena = self._desc_arena(req.kind)
             s = self.samples.alloc(req.n)
             if s is None:
                 break
@@ -295,6 +313,8 @@ class TransitServer:
             lv.soff, lv.ooff, lv.desc, lv.admitted = s, o, dsl, now
             if req.kind == "bls":
                 lv.tiles = (req.nf + self.F - 1) // self.F
+            elif req.kind == "fold":
+                lv.tiles = (req.nf + self.fold_F - 1) // self.fold_F
             else:
                 lv.tiles = (req.n + TLS_TILE - 1) // TLS_TILE
             new.append(lv)
@@ -325,10 +345,11 @@ class TransitServer:
         ev.record(self.h2d)
         return ev
 
-    def _meta(self, new, bls_segs, tls_segs):
+    def _meta(self, new, bls_segs, tls_segs, fold_segs):
         """One pinned buffer with the step's descriptor rows, detrend list and work queues."""
         nb = [lv for lv in new if lv.req.kind == "bls"]
         nt = [lv for lv in new if lv.req.kind == "tls"]
+        nfd = [lv for lv in new if lv.req.kind == "fold"]
         parts = []
         g_off = np.array([lv.soff for lv in new], np.uint64)
         g_n = np.array([lv.req.n for lv in new], np.uint32)
@@ -342,9 +363,14 @@ class TransitServer:
         for k, lv in enumerate(nt):
             r = lv.req
             tt[k] = (lv.soff, lv.ooff, r.n, r.nsc, r.wmax, r.dw, r.deltat, 0)
+        ft = np.zeros(len(nfd), BLS_CURVE)
+        for k, lv in enumerate(nfd):
+            r = lv.req
+            ft[k] = (lv.soff, lv.ooff, r.n, r.nf, r.fmin, r.df, 0.0, 0, 0, 0, 0, 0)
         bsg, bcum = bls_segs
         tsg, tcum = tls_segs
-        for arr in (g_off, g_n, bsg, bcum, tsg, tcum):
+        fsg, fcum = fold_segs
+        for arr in (g_off, g_n, bsg, bcum, tsg, tcum, fsg, fcum):
             parts.append(np.frombuffer(arr.tobytes(), np.uint8))
         offs, p = [], 0
         for a in parts:
@@ -358,7 +384,8 @@ class TransitServer:
         base = devbuf.data_ptr()
         # descriptor rows go straight to their slots (new requests get consecutive slots
         # when the descriptor arena is not fragmented; otherwise one copy per row)
-        for rows, table, live, dt in ((bt, self.bls_table, nb, BLS_CURVE), (tt, self.tls_table, nt, TLS_CURVE)):
+        for rows, table, live, dt in ((bt, self.bls_table, nb, BLS_CURVE), (tt, self.tls_table, nt, TLS_CURVE),
+                                      (ft, self.fold_table, nfd, BLS_CURVE)):
             if not len(rows):
                 continue
             rb = np.frombuffer(rows.tobytes(), np.uint8)
@@ -371,7 +398,7 @@ class TransitServer:
             else:
                 for k, sl in enumerate(slots):
                     table[sl * sz:(sl + 1) * sz].copy_(hb[k * sz:(k + 1) * sz], non_blocking=True)
-        return devbuf, [base + o for o in offs], nb, nt
+        return devbuf, [base + o for o in offs], nb, nt, nfd
 
     def _take(self, live, budget):
         segs, counts = [], []
@@ -401,10 +428,12 @@ class TransitServer:
             return done
         new = self._admit(now)
         self.live_bls += [lv for lv in new if lv.req.kind == "bls"]
+        self.live_fold += [lv for lv in new if lv.req.kind == "fold"]
         self.live_tls += [lv for lv in new if lv.req.kind == "tls"]
         bls_segs = self._take(self.live_bls, self.bls_tiles)
+        fold_segs = self._take(self.live_fold, self.fold_tiles)
         tls_segs = self._take(self.live_tls, self.tls_tiles)
-        if not new and not len(bls_segs[0]) and not len(tls_segs[0]):
+        if not new and not len(bls_segs[0]) and not len(tls_segs[0]) and not len(fold_segs[0]):
             return done
         si = self.step_count
         self.step_count += 1
@@ -414,7 +443,8 @@ class TransitServer:
             if new:
                 ev = self._upload_samples(new)
                 st.wait_event(ev)
-            devbuf, (p_goff, p_gn, p_bsg, p_bcum, p_tsg, p_tcum), nb, nt = self._meta(new, bls_segs, tls_segs)
+            devbuf, (p_goff, p_gn, p_bsg, p_bcum, p_tsg, p_tcum, p_fsg, p_fcum), nb, nt, nfd = \
+                self._meta(new, bls_segs, tls_segs, fold_segs)
             h = st.cuda_stream
             if new:
                 N.call("gtrap_gfilter_packed", as_ptr(self.x), as_ptr(self.resid), p_goff, p_gn,
@@ -427,6 +457,12 @@ class TransitServer:
                 N.call("gtrap_bls_offsets", tbl, nbr, as_ptr(self.t), as_ptr(self.resid), h)
                 N.call("gtrap_bls_prepare", tbl, nbr, mx, as_ptr(self.t), as_ptr(self.resid),
                        self.sample_cap, as_ptr(self.pool), self.pool_bytes, self.bls_spec.flags, h)
+            for lo, hi in _runs([lv.desc for lv in nfd]):
+                tbl = as_ptr(self.fold_table) + lo * bsz
+                mx = max(lv.req.n for lv in nfd if lo <= lv.desc < hi)
+                N.call("gtrap_bls_offsets", tbl, hi - lo, as_ptr(self.t), as_ptr(self.resid), h)
+                N.call("gtrap_tls_fold_prepare", tbl, hi - lo, mx, as_ptr(self.t), as_ptr(self.resid),
+                       self.sample_cap, as_ptr(self.pool), self.pool_bytes, h)
             for lv in nt:
                 self.max_tls_nsc = max(self.max_tls_nsc, lv.req.nsc)
             s = self.bls_spec
@@ -435,6 +471,13 @@ class TransitServer:
                        as_ptr(self.t), as_ptr(self.pool), self.pool_bytes, self.sample_cap, s.nb,
                        s.kma, s.kmi, self.F, s.flags, 0, as_ptr(self.counters[0:1]),
                        as_ptr(self.o[0]), as_ptr(self.o[1]), as_ptr(self.o[2]), h)
+            fs = self.fold_spec
+            if len(fold_segs[0]):
+                w = fs.w
+                N.call("gtrap_tls_fold_run", as_ptr(self.fold_table), p_fsg, p_fcum, len(fold_segs[0]),
+                       as_ptr(self.pool), self.pool_bytes, self.sample_cap, fs.nb, w.ctypes.data, int(w.size),
+                       float(fs.lfrac), fs.dmax_bins, self.fold_F, 0, as_ptr(self.counters[2:3]),
+                       *[as_ptr(self.o[j]) for j in range(4)], h)
             ts = self.tls_spec
             if len(tls_segs[0]):
                 N.call("gtrap_gtls_run", as_ptr(self.tls_table), p_tsg, p_tcum, len(tls_segs[0]),
@@ -454,12 +497,13 @@ class TransitServer:
             ev.record(st)
         step = _Step(si, ev, peaks=pk)
         step._keep = devbuf  # staging stays alive until the step has run
-        for live in (self.live_bls, self.live_tls):
+        for live in (self.live_bls, self.live_fold, self.live_tls):
             for lv in live:
                 if lv.next_tile >= lv.tiles and lv.last_step < 0:
                     lv.last_step = si
                     step.finishing.append(lv)
         self.live_bls = [lv for lv in self.live_bls if lv.last_step < 0]
+        self.live_fold = [lv for lv in self.live_fold if lv.last_step < 0]
         self.live_tls = [lv for lv in self.live_tls if lv.last_step < 0]
         self.steps.append(step)
         self._issue_copies(step)
@@ -481,7 +525,8 @@ class TransitServer:
                     rs = api.PEAK_STATS.itemsize
                     srcs = (st_[lv.pk_slot * rs:(lv.pk_slot + 1) * rs], idx[lv.pk_slot], val[lv.pk_slot])
                 else:
-                    srcs = [self.o[j][o:o + m] for j in range(3 if lv.req.kind == "bls" else 5)]
+                    series = {"bls": 3, "fold": 4}.get(lv.req.kind, 5)
+                    srcs = [self.o[j][o:o + m] for j in range(series)]
                 # one pinned block for the request's outputs, one view per series
                 sizes = [(src.numel() * src.element_size() + 15) // 16 * 16 for src in srcs]
                 blk = torch.empty(sum(sizes), dtype=torch.uint8, pin_memory=True)
@@ -509,6 +554,9 @@ class TransitServer:
                 res = lv.result
                 if lv.req.kind == "bls":
                     res = (res[0].numpy(), res[1].numpy().view(np.int32), res[2].numpy().view(np.int32))
+                elif lv.req.kind == "fold":
+                    res = (res[0].numpy(), res[1].numpy().view(np.int32), res[2].numpy().view(np.int32),
+                           res[3].numpy())
                 elif lv.pk_slot >= 0:
                     res = (np.frombuffer(res[0].numpy().tobytes(), api.PEAK_STATS)[0], res[1].numpy(),
                            res[2].numpy())
@@ -516,7 +564,7 @@ class TransitServer:
                     res = tuple(a.numpy() for a in res)
                 self.samples.free(lv.soff, lv.req.n)
                 self.outs.free(lv.ooff, lv.req.outputs)
-                (self.bls_desc if lv.req.kind == "bls" else self.tls_desc).free(lv.desc, 1)
+                self._desc_arena(lv.req.kind).free(lv.desc, 1)
                 r = Result(lv.rid, lv.req.kind, lv.arrival, lv.admitted, now, res, lv.req.outputs)
                 self.results.append(r)
                 out.append(r)
@@ -571,14 +619,14 @@ def _runs(slots):
 
 class PlainServer:
     """Baseline: each request is processed alone, in arrival order, by the plain entry points
-    (copy in, gfilter, get_offset, geebls or gtls, copy out), as a caller of the reference's
-    per-image kernels does."""
+    (copy in, gfilter, get_offset, geebls, tls_fold or gtls, copy out), as a caller of the
+    reference's per-image kernels does."""
 
     def __init__(self, bls: BlsSpec = BlsSpec(), tls: TlsSpec = TlsSpec(), detrend_r: int = 24,
-                 device=None):
+                 device=None, fold: FoldSpec = FoldSpec()):
         require_cuda()
         self.dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
-        self.bls_spec, self.tls_spec, self.r = bls, tls, int(detrend_r)
+        self.bls_spec, self.tls_spec, self.fold_spec, self.r = bls, tls, fold, int(detrend_r)
         self.results: list = []
         self.next_rid = 0
 
@@ -597,6 +645,12 @@ class PlainServer:
             kkmi = req.kkmi if req.kkmi is not None else int(n * 0.005)
             outs = api.geebls(r, t, off, nt, req.nf, s.nb, s.kma, s.kmi, kkmi, req.fmin, req.df,
                               phase=s.phase)
+            res = tuple(o.reshape(-1).cpu().numpy() for o in outs)
+            ev = req.nf
+        elif req.kind == "fold":
+            fs = self.fold_spec
+            outs = api.tls_fold(r, t, api.offset(r, t), req.nf, fs.nb, req.fmin, req.df, fs.w, lfrac=fs.lfrac,
+                                dmax=fs.dmax_bins)
             res = tuple(o.reshape(-1).cpu().numpy() for o in outs)
             ev = req.nf
         else:

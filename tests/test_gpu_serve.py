@@ -111,3 +111,34 @@ def test_server_returns_tls_peaks(solo):
         m = min(5, want["npeaks"])
         np.testing.assert_array_equal(idx[:m], want["peaks"][:m])
         assert rec["median"] == want["median"]
+
+
+FOLD = B.FoldSpec(nb=256, durations=(0.05, 0.1, 0.2, 0.3), lfrac=0.2, dmax=128)
+
+
+def test_fold_requests_mixed_equal_plain(solo):
+    """Folded-search requests served beside BLS and GTLS requests, each spanning several steps,
+    equal the plain per-request path (gfilter, get_offset, tls_fold) bit for bit; the other
+    requests keep their solo results."""
+    reqs, ref = solo
+    curves = synth.ragged_mix(5, seed=5100, n_range=(500, 5000))
+    folds = [S.Request("fold", c["t"], c["x"], nf=40 + 9 * k, fmin=float(np.float32(0.1)),
+                       df=float(np.float32(0.015))) for k, c in enumerate(curves)]
+    plain = S.PlainServer(BLS, TLS, detrend_r=R, fold=FOLD)
+    want = [plain.process(f).outputs for f in folds]
+    srv = _server(fold=FOLD, fold_tiles=7)
+    fr, rr = [], []
+    for k in range(4):
+        fr.append(srv.submit(folds[k]))
+        rr.append(srv.submit(reqs[k]))
+    for _ in range(3):
+        srv.step()
+    fr.append(srv.submit(folds[4]))
+    srv.run_until_idle()
+    res = {r.rid: r for r in srv.results}
+    assert len(res) == 9 and srv.step_count > 4
+    for k, rid in enumerate(fr):
+        assert res[rid].kind == "fold" and res[rid].evals == folds[k].nf
+        _eq(res[rid].outputs, want[k])
+    for k, rid in enumerate(rr):
+        _eq(res[rid].outputs, ref[k])
