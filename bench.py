@@ -1199,15 +1199,21 @@ def run_served(args, rank, world, local_rank):
     with the saturation throughput and p50/p99 latency per offered load, beside the plain
     per-request server."""
     import torch
-    from gtrap_gb300 import _build, serve as S, synth
+    from gtrap_gb300 import _build, batch as B, serve as S, synth
 
     _build.build()
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
     npool = args.nq or 1500
-    pool = [S.Request.from_curve(c) for c in synth.ragged_mix(npool, seed=5000 + 100000 * rank,
-                                                                n_range=(1000, 70000))]
-    srv = S.TransitServer(detrend_r=R_MEDIAN, hbm_budget=100e9)
+    curves = synth.ragged_mix(npool, seed=5000 + 100000 * rank, n_range=(1000, 70000))
+    fold = args.tls_kind == "fold"
+    if fold:  # TLS-kind curves through the folded search on the BLS frequency rule
+        pool = [S.Request("fold", c["t"], c["x"], *fold_grid(c)) if c["kind"] == "tls" else S.Request.from_curve(c)
+                for c in curves]
+    else:
+        pool = [S.Request.from_curve(c) for c in curves]
+    fspec = B.FoldSpec(nb=TF_NB, durations=tuple(float(w) for w in TF_DURS), lfrac=TF_LFRAC, dmax=TF_DMAX)
+    srv = S.TransitServer(detrend_r=R_MEDIAN, hbm_budget=100e9, fold=fspec)
     for r in pool[:40]:
         srv.submit(r)
     srv.run_until_idle()
@@ -1216,14 +1222,14 @@ def run_served(args, rank, world, local_rank):
         srv.submit(r, t0)
     res = srv.run_until_idle()
     sat = S.latency_summary(res, time.perf_counter() - t0)
-    plain = S.PlainServer(detrend_r=R_MEDIAN)
+    plain = S.PlainServer(detrend_r=R_MEDIAN, fold=fspec)
     for r in pool[:10]:
         plain.process(r)
     t0 = time.perf_counter()
     pres = [plain.process(r, t0) for r in pool[:300]]
     psat = S.latency_summary(pres, time.perf_counter() - t0)
     sweep = []
-    for frac in (0.1, 0.2, 0.3, 0.4, 0.5, 0.6, 0.7, 0.8, 0.9, 1.0, 1.1, 1.2):
+    for frac in (0.1, 0.5, 0.9) if fold else (0.1, 0.2, 0.3, 0.4, 0.5, 0.6, 0.7, 0.8, 0.9, 1.0, 1.1, 1.2):
         rate = frac * sat["req_per_s"]
         m = min(npool, max(200, int(rate * 1.5)))
         offs = S.poisson_trace(m, rate, seed=int(frac * 1000))
@@ -1242,10 +1248,11 @@ def run_served(args, rank, world, local_rank):
             "steps": 1, "warmup": 1, "ms_per_step": 1e3 * npool / sat["req_per_s"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64",
             "data": "synthetic",
-            "config": {"workload": "served: Poisson arrivals of single-curve BLS/GTLS requests (50/50, "
-                                   "detrended), n log-uniform [1000, 70000], nf 2k-32k, HBM budget 100 GB",
+            "config": {"workload": "served: Poisson arrivals of single-curve BLS/%s requests (50/50, "
+                                   "detrended), n log-uniform [1000, 70000], nf 2k-32k, HBM budget 100 GB"
+                                   % ("folded-TLS" if fold else "GTLS"),
                        "pool": npool, "depth": srv.depth, "bls_tiles_per_step": srv.bls_tiles,
-                       "tls_tiles_per_step": srv.tls_tiles},
+                       "tls_tiles_per_step": srv.tls_tiles, "fold_tiles_per_step": srv.fold_tiles},
             "saturation": sat, "plain_saturation": psat, "sweep": sweep,
             "hbm_high_water_bytes": srv.hbm_high_water()}
     print(json.dumps(line), flush=True)
