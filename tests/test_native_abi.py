@@ -117,6 +117,30 @@ def test_new_entry_points_validate_on_the_host(lib):
     assert tf(wsp=C.c_void_p(257)) == _native.ERR_WORKSPACE  # misaligned
     assert lib.gtrap_tls_fold_workspace_size(1000, 4) >= 4 * 1000 * 20
 
+    # packed (ragged) folded searches
+    assert lib.gtrap_tls_fold_item_frequencies(100, 50) == 0
+    assert lib.gtrap_tls_fold_item_frequencies(256, 1) == 0
+    assert lib.gtrap_tls_fold_item_frequencies(256, 512) == 0
+    assert lib.gtrap_tls_fold_prepare(P, 0, 10, P, P, 10, P, 1 << 20, None) == 0  # nothing to do
+    assert lib.gtrap_tls_fold_prepare(P, 2, 1 << 20, P, P, 10, P, 1 << 20, None) == _native.ERR_INVALID_ARG
+    assert b"2^20" in lib.gtrap_last_error()
+    assert lib.gtrap_tls_fold_prepare(None, 2, 10, P, P, 10, P, 1 << 20, None) == _native.ERR_INVALID_ARG
+    assert lib.gtrap_tls_fold_prepare(P, 2, 10, P, P, 10, C.c_void_p(257), 1 << 20, None) == _native.ERR_WORKSPACE
+
+    def tr(nseg=1, nb=256, nd=2, dmax=128, F=1, pool=ws, nbytes=1 << 40, tsr=P):
+        return lib.gtrap_tls_fold_run(P, P, P, nseg, pool, nbytes, 1000, nb, d, nd, 0.2, dmax, F, 0, P, tsr, P, P, P,
+                                      None)
+
+    assert tr(nseg=0) == 0
+    assert tr(tsr=None) == _native.ERR_INVALID_ARG
+    assert tr(nb=100) == _native.ERR_INVALID_ARG
+    assert tr(nd=40) == _native.ERR_INVALID_ARG
+    assert tr(F=0) == _native.ERR_INVALID_ARG
+    assert tr(F=4) == _native.ERR_INVALID_ARG
+    assert tr(nb=4096, dmax=2048, F=2) == _native.ERR_INVALID_ARG and b"not built" in lib.gtrap_last_error()
+    assert tr(pool=C.c_void_p(257)) == _native.ERR_WORKSPACE
+    assert tr(nbytes=1000) == _native.ERR_WORKSPACE
+
     rec = np.zeros(1, api.TRANSIT_PARAMS)
     rec["per"], rec["a"], rec["rp"] = -1.0, 10.0, 0.1
     assert lib.gtrap_transit_flux(P, P, 10, rec.ctypes.data_as(C.c_void_p), None) == _native.ERR_INVALID_ARG
