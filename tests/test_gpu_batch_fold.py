@@ -150,3 +150,39 @@ def test_fold_batch_grids_given_offsets(cuda, nb, dmax):
     B.run_plain(bat)
     torch.cuda.synchronize()
     _same(got, _results(bat))
+
+
+def test_fold_only_batch_and_fp32_phase_neighbours(cuda):
+    """A batch of folded requests alone (no BLS or GTLS stage graphs), and folded requests
+    beside BLS requests in the FP32-reference phase mode (the shared pool then carries phase
+    pairs for the folded curves only): both equal the plain per-curve path."""
+    mix = synth.ragged_mix(6, seed=4500, n_range=(400, 3000))
+    alone = B.RaggedBatch(BLS, TLS, detrend_r=R, fold=FOLD)
+    for k, c in enumerate(mix):
+        alone.add_fold(c["t"], c["x"], 20 + 3 * k, 0.05, 0.02)
+    alone.build()
+    stages = alone.capture_stages()
+    assert set(stages) == {"prep", "fold"}
+    for g in stages.values():
+        g.replay()
+    torch.cuda.synchronize()
+    got = _results(alone)
+    B.run_plain(alone)
+    torch.cuda.synchronize()
+    _same(got, _results(alone))
+
+    mixed = B.RaggedBatch(B.BlsSpec(nb=256, kma=27, kmi=1, phase="fp32"), TLS, detrend_r=R, fold=FOLD)
+    for k, c in enumerate(mix):
+        if k % 2:
+            mixed.add_fold(c["t"], c["x"], 20 + 3 * k, 0.05, 0.02)
+        else:
+            mixed.add_bls(c["t"], c["x"], 50 + k, 0.05, 0.01, kkmi=3)
+    mixed.build()
+    mixed.launch()
+    torch.cuda.synchronize()
+    got = _results(mixed)
+    B.run_plain(mixed)
+    torch.cuda.synchronize()
+    _same(got, _results(mixed))
+    for k in range(mixed.n_fold):  # the same curves gave the same folded spectra alone
+        np.testing.assert_array_equal(got[1][k][0], _results(alone)[1][2 * k + 1][0])
