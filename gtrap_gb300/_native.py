@@ -55,6 +55,7 @@ _SIGNATURES = {
     "gtrap_gtls_run": (C.c_int, [vp, vp, vp, u32, vp, vp, i32, i32, i32, i32, u32, u32, vp, vp, vp,
                                  vp, vp, vp, vp]),
     "gtrap_blsstat": (C.c_int, [vp, vp, vp, u32, u32, f64, f64, u32, vp, vp, vp, vp, vp]),
+    "gtrap_blsstat_packed": (C.c_int, [vp, vp, vp, vp, vp, u32, u32, vp, vp, vp, vp, vp]),
     "gtrap_getmax": (C.c_int, [vp, vp, vp, u32, u32, u32, vp, vp, vp, vp, vp, vp, vp]),
     "gtrap_gtls": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, i32, i32, i32, i32, i32, f32, f32, f32,
                              f32, f32, i32, u32, vp]),

@@ -9,6 +9,7 @@ from __future__ import annotations
 import ctypes as C
 from dataclasses import dataclass
 
+import numpy as _np
 import torch
 
 from . import _native as N
@@ -160,6 +161,27 @@ def blsstat(blsp, phase1, phase2, df, fmin, patch=0, stream=None):
     return pest, sde, b1, b2
 
 
+BLS_STATS = _np.dtype([("pest", "<f8"), ("sde", "<f8"), ("ph1", "<i4"), ("ph2", "<i4")])
+
+
+def blsstat_packed(blsp, phase1, phase2, curves, sel=None, count=None, patch=0, stream=None):
+    """:func:`blsstat` for packed spectra (gtrap_blsstat_packed): ``curves`` is the device
+    table of ``gtrap_bls_curve`` rows (a uint8 tensor), ``sel`` an optional int32 device
+    tensor of row indices (``count`` of them; all rows without it).  Folded-search spectra
+    pass (tsr, start, duration index).  Returns (Pest, SDE, phase1 at max, phase2 at max)."""
+    dev = blsp.device
+    if count is None:
+        count = int(sel.numel()) if sel is not None else curves.numel() // 56
+    pest = torch.empty(count, dtype=torch.float64, device=dev)
+    sde = torch.empty(count, dtype=torch.float64, device=dev)
+    b1 = torch.empty(count, dtype=torch.int32, device=dev)
+    b2 = torch.empty(count, dtype=torch.int32, device=dev)
+    N.call("gtrap_blsstat_packed", as_ptr(blsp), as_ptr(phase1), as_ptr(phase2), as_ptr(curves),
+           as_ptr(sel) if sel is not None else None, int(count), int(patch), as_ptr(pest), as_ptr(sde),
+           as_ptr(b1), as_ptr(b2), stream_handle(stream))
+    return pest, sde, b1, b2
+
+
 def getmax(blsp, phase1, phase2, patch, stream=None):
     """Per-patch partial statistics with the reference getmax kernel's outputs."""
     blsp = _f32(blsp, "blsp")
@@ -228,7 +250,6 @@ def fp32_peak_probe(iters=4096, stream=None):
 
 
 # Record layout of gtrap_peak_stats (include/gtrap_gb300.h).
-import numpy as _np
 
 PEAK_STATS = _np.dtype([("maxsn", "<f4"), ("argmax", "<u4"), ("lent", "<u4"), ("npeaks", "<u4"),
                         ("median", "<f8"), ("std", "<f8"), ("far", "<f8"), ("pssn", "<f8"),

@@ -501,6 +501,22 @@ class RaggedBatch:
         n = torch.from_numpy(tt["nt"].astype(np.int32)).to(self.device)
         return api.peakstat(self.tls_outs[0], off, n, 1, int(tt["nt"].max()), mpd, ntop, k, stream)
 
+    def bls_stats(self, patch: int = 0, stream=None):
+        """get_blsstat of every BLS request's spectrum on the device (gtrap/getstat.py:64-67:
+        Pest, SDE and the window phases at the maximum); device tensors of n_bls values."""
+        if not self.n_bls:
+            raise ValueError("no BLS requests in the batch")
+        return api.blsstat_packed(self.blsp, self.ph1, self.ph2, self.bls_curves, None, self.n_bls, patch,
+                                  stream)
+
+    def fold_stats(self, patch: int = 0, stream=None):
+        """The same statistics of every folded-search spectrum: (Pest, SDE, start bin and
+        duration index at the maximum TSR)."""
+        if not self.n_fold:
+            raise ValueError("no folded-search requests in the batch")
+        o = self.fold_outs
+        return api.blsstat_packed(o[0], o[1], o[2], self.fold_curves, None, self.n_fold, patch, stream)
+
     # -- results ------------------------------------------------------------------------
     def bls_result(self, k: int):
         """(blsp, phase1, phase2) of BLS request k as numpy arrays (synchronises)."""

@@ -48,12 +48,11 @@ __device__ void block_reduce(float &m, uint32_t &mi, double &s1, double &s2) {
 
 constexpr int kStatThreads = 512;
 
-__global__ void __launch_bounds__(kStatThreads) blsstat_kernel(
-    const float *__restrict__ blsp, const uint32_t *__restrict__ phase1,
-    const uint32_t *__restrict__ phase2, uint32_t nf, uint32_t nused, double df, double fmin,
-    double *pest, double *sde, uint32_t *ph1best, uint32_t *ph2best) {
-  const uint32_t q = blockIdx.x;
-  const float *row = blsp + (size_t)q * nf;
+// Statistics of one spectrum row (nf values, the first nused entering) into output slot q.
+__device__ __forceinline__ void stat_row(const float *__restrict__ row, const uint32_t *phase1,
+                                         const uint32_t *phase2, uint32_t nf, uint32_t nused,
+                                         double df, double fmin, uint32_t q, double *pest,
+                                         double *sde, uint32_t *ph1best, uint32_t *ph2best) {
   float m = -INFINITY;
   uint32_t mi = UINT_MAX;
   double s1 = 0.0, s2 = 0.0;
@@ -70,11 +69,34 @@ __global__ void __launch_bounds__(kStatThreads) blsstat_kernel(
     const double var = s2 / (double)nf;
     const double sd = sqrt(var - ave * ave);
     pest[q] = 1.0 / ((double)mi * df + fmin);
-    sde[q] = ((double)m - ave) / sd;
-    const size_t o = (size_t)q * nf + mi;
-    if (ph1best) ph1best[q] = phase1 ? phase1[o] : 0u;
-    if (ph2best) ph2best[q] = phase2 ? phase2[o] : 0u;
+    sde[q] = nused ? ((double)m - ave) / sd : NAN;
+    if (ph1best) ph1best[q] = phase1 ? phase1[mi] : 0u;
+    if (ph2best) ph2best[q] = phase2 ? phase2[mi] : 0u;
   }
+}
+
+__global__ void __launch_bounds__(kStatThreads) blsstat_kernel(
+    const float *__restrict__ blsp, const uint32_t *__restrict__ phase1,
+    const uint32_t *__restrict__ phase2, uint32_t nf, uint32_t nused, double df, double fmin,
+    double *pest, double *sde, uint32_t *ph1best, uint32_t *ph2best) {
+  const uint32_t q = blockIdx.x;
+  const size_t o = (size_t)q * nf;
+  stat_row(blsp + o, phase1 ? phase1 + o : nullptr, phase2 ? phase2 + o : nullptr, nf, nused, df, fmin,
+           q, pest, sde, ph1best, ph2best);
+}
+
+// Packed spectra: block b takes curve sel[b] (b without sel) of the table, whose spectrum is
+// [out, out + nf) of the packed arrays; fmin and df are the table's float32 values.
+__global__ void __launch_bounds__(kStatThreads) blsstat_packed_kernel(
+    const float *__restrict__ blsp, const uint32_t *__restrict__ phase1,
+    const uint32_t *__restrict__ phase2, const gtrap_bls_curve *__restrict__ curves,
+    const uint32_t *__restrict__ sel, uint32_t patch, double *pest, double *sde, uint32_t *ph1best,
+    uint32_t *ph2best) {
+  const uint32_t b = blockIdx.x;
+  const gtrap_bls_curve c = curves[sel ? sel[b] : b];
+  const uint32_t nused = patch ? (c.nf / patch) * patch : c.nf;
+  stat_row(blsp + c.out, phase1 ? phase1 + c.out : nullptr, phase2 ? phase2 + c.out : nullptr, c.nf, nused,
+           (double)c.df, (double)c.fmin, b, pest, sde, ph1best, ph2best);
 }
 
 constexpr int kPatchThreads = 256;
@@ -125,6 +147,19 @@ int gtrap_blsstat(const float *blsp, const uint32_t *phase1, const uint32_t *pha
   blsstat_kernel<<<nq, kStatThreads, 0, stream>>>(blsp, phase1, phase2, nf, nused, df, fmin,
                                                   pest, sde, ph1best, ph2best);
   return check_launch("blsstat_kernel");
+}
+
+int gtrap_blsstat_packed(const float *blsp, const uint32_t *phase1, const uint32_t *phase2,
+                         const gtrap_bls_curve *curves, const uint32_t *sel, uint32_t count,
+                         uint32_t patch, double *pest, double *sde, uint32_t *ph1best,
+                         uint32_t *ph2best, gtrap_stream_t stream) {
+  using namespace gtrap;
+  if (count == 0) return GTRAP_OK;
+  if (!blsp || !curves || !pest || !sde) return fail(GTRAP_ERR_INVALID_ARG, "blsstat_packed: null pointer");
+  if (count > 0x7fffffffu) return fail(GTRAP_ERR_INVALID_ARG, "blsstat_packed: count too large");
+  blsstat_packed_kernel<<<count, kStatThreads, 0, stream>>>(blsp, phase1, phase2, curves, sel, patch, pest, sde,
+                                                           ph1best, ph2best);
+  return check_launch("blsstat_packed_kernel");
 }
 
 int gtrap_getmax(const float *blsp, const uint32_t *phase1, const uint32_t *phase2,

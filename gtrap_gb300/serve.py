@@ -18,7 +18,9 @@ in device-resident arenas sized by an HBM budget, and runs in steps.  A step
 4. when a request's last tile has run, copies its outputs to the host on a second copy stream
    and frees its memory.  With ``tls_peaks`` a GTLS request returns only its peak statistics
    (``gtrap_peakstat``, computed on the device in the step that finishes it) instead of its
-   five output series.
+   five output series, and with ``spectrum_stats`` a BLS or folded-search request returns only
+   get_blsstat's record (``gtrap_blsstat_packed``: Pest, SDE and the best window) instead of
+   its spectrum.
 
 The host prepares step k+1 while step k runs (at most ``depth`` steps in flight).  Each
 request's result is bit-identical to a solo run: the kernels treat every curve and tile
@@ -88,7 +90,8 @@ class Result:
     done: float
     outputs: tuple   # bls: (blsp, phase1, phase2); fold: (tsr, start, duration index, depth);
     #                  tls: (sn, w, t0, l, hmax), or with tls_peaks (PEAK_STATS record, peak
-    #                  indices, peak heights)
+    #                  indices, peak heights); bls and fold with spectrum_stats: a BLS_STATS
+    #                  record (pest, sde, ph1, ph2; for fold ph1/ph2 = start bin, duration index)
     evals: int
 
     @property
@@ -186,6 +189,7 @@ class _Live:
     result: tuple = ()
     d2h_event: object = None
     pk_slot: int = -1      # row in its finishing step's peak-statistics buffers
+    st_slot: int = -1      # row in its finishing step's spectrum-statistics buffers
 
 
 @dataclass
@@ -194,6 +198,7 @@ class _Step:
     event: object
     finishing: list = field(default_factory=list)
     peaks: tuple = ()      # (stats, idx, val) device buffers of the GTLS requests it finishes
+    bstats: dict = field(default_factory=dict)  # kind -> (pest, sde, ph1, ph2) device buffers
 
 
 class TransitServer:
@@ -208,7 +213,7 @@ class TransitServer:
                  hbm_budget: float = 100e9, sample_share: float = 0.8, bls_tiles: int | None = None,
                  tls_tiles: int | None = None, F: int | None = None, max_requests: int = 1 << 16,
                  depth: int = 2, tls_peaks: dict | None = None, device=None, fold: FoldSpec = FoldSpec(),
-                 fold_tiles: int | None = None):
+                 fold_tiles: int | None = None, spectrum_stats: bool = False):
         require_cuda()
         self.dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         self.bls_spec, self.tls_spec, self.fold_spec = bls, tls, fold
@@ -223,6 +228,7 @@ class TransitServer:
         self.tls_tiles = int(tls_tiles) if tls_tiles else sms * 64
         self.depth = max(1, int(depth))
         self.tls_peaks = None if tls_peaks is None else dict(mpd=10, ntop=4, k=8) | dict(tls_peaks)
+        self.spectrum_stats = bool(spectrum_stats)
         budget = int(hbm_budget)
         self.sample_cap = int(budget * sample_share) // SAMPLE_BYTES // ALIGN * ALIGN
         self.out_cap = int(budget * (1.0 - sample_share)) // OUTPUT_BYTES // ALIGN * ALIGN
@@ -493,9 +499,23 @@ class TransitServer:
                 c = self.tls_peaks
                 pk = api.peakstat(self.o[0], po, pn, 1, max(lv.req.n for lv in fin_tls), c["mpd"],
                                   c["ntop"], c["k"], stream=st)
+            bst, sels = {}, []
+            if self.spectrum_stats:
+                for kind, live, table in (("bls", self.live_bls, self.bls_table),
+                                          ("fold", self.live_fold, self.fold_table)):
+                    fin = [lv for lv in live if lv.next_tile >= lv.tiles and lv.last_step < 0]
+                    if not fin:
+                        continue
+                    for j, lv in enumerate(fin):
+                        lv.st_slot = j
+                    sel = torch.tensor([lv.desc for lv in fin], dtype=torch.int32).pin_memory().to(
+                        self.dev, non_blocking=True)
+                    sels.append(sel)
+                    bst[kind] = api.blsstat_packed(self.o[0], self.o[1], self.o[2], table, sel, len(fin), stream=st)
             ev = torch.cuda.Event()
             ev.record(st)
-        step = _Step(si, ev, peaks=pk)
+        step = _Step(si, ev, peaks=pk, bstats=bst)
+        step._sels = sels
         step._keep = devbuf  # staging stays alive until the step has run
         for live in (self.live_bls, self.live_fold, self.live_tls):
             for lv in live:
@@ -518,7 +538,12 @@ class TransitServer:
         with torch.cuda.stream(self.d2h):
             for lv in step.finishing:
                 m, o = lv.req.outputs, lv.ooff
-                if lv.req.kind == "tls" and lv.pk_slot >= 0:
+                if lv.st_slot >= 0 and lv.req.kind in step.bstats:
+                    bufs = step.bstats[lv.req.kind]
+                    for t_ in bufs:
+                        t_.record_stream(self.d2h)
+                    srcs = [b_[lv.st_slot:lv.st_slot + 1] for b_ in bufs]
+                elif lv.req.kind == "tls" and lv.pk_slot >= 0:
                     st_, idx, val = step.peaks
                     for t_ in step.peaks:  # keep the buffers until the copies have run
                         t_.record_stream(self.d2h)
@@ -552,7 +577,10 @@ class TransitServer:
             if lv.d2h_event.query():
                 now = time.perf_counter()
                 res = lv.result
-                if lv.req.kind == "bls":
+                if lv.st_slot >= 0:
+                    res = np.array((float(res[0].numpy()[0]), float(res[1].numpy()[0]), int(res[2].numpy()[0]),
+                                    int(res[3].numpy()[0])), dtype=api.BLS_STATS)
+                elif lv.req.kind == "bls":
                     res = (res[0].numpy(), res[1].numpy().view(np.int32), res[2].numpy().view(np.int32))
                 elif lv.req.kind == "fold":
                     res = (res[0].numpy(), res[1].numpy().view(np.int32), res[2].numpy().view(np.int32),

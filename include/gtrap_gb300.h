@@ -191,6 +191,15 @@ int gtrap_blsstat(const float *blsp, const uint32_t *phase1, const uint32_t *pha
                   uint32_t nf, uint32_t nq, double df, double fmin, uint32_t patch,
                   double *pest, double *sde, uint32_t *ph1best, uint32_t *ph2best,
                   gtrap_stream_t stream);
+/* The same statistics for packed spectra: output b is curve sel[b] (b when sel is NULL) of
+ * the device table `curves`, whose spectrum is [out, out + nf) of blsp/phase1/phase2 and
+ * whose fmin/df are the table's float32 values.  A curve with nf < patch gets sde = NaN.
+ * Folded-search spectra use it too: (tsr, start, duration index) in place of
+ * (blsp, phase1, phase2). */
+int gtrap_blsstat_packed(const float *blsp, const uint32_t *phase1, const uint32_t *phase2,
+                         const gtrap_bls_curve *curves, const uint32_t *sel, uint32_t count,
+                         uint32_t patch, double *pest, double *sde, uint32_t *ph1best,
+                         uint32_t *ph2best, gtrap_stream_t stream);
 
 /* Per-patch partials with the getmax kernel's outputs (gtrap/getstat.py:14-57): for
  * patch p of `patch` frequencies of curve q, element p + npatch*q of each output holds

@@ -186,3 +186,20 @@ def test_fold_only_batch_and_fp32_phase_neighbours(cuda):
     _same(got, _results(mixed))
     for k in range(mixed.n_fold):  # the same curves gave the same folded spectra alone
         np.testing.assert_array_equal(got[1][k][0], _results(alone)[1][2 * k + 1][0])
+
+
+def test_packed_spectrum_stats(mixed, cuda):
+    """get_blsstat of every BLS and folded spectrum of the batch (gtrap_blsstat_packed) equals
+    the image entry point on that spectrum alone, bit for bit, with and without patches."""
+    from gtrap_gb300 import api
+    mix, kinds, bat, got = mixed
+    d = lambda a: torch.from_numpy(np.ascontiguousarray(a).reshape(1, -1)).to(cuda)
+    for stats_fn, table, res in ((bat.bls_stats, bat.bls_table, got[0]), (bat.fold_stats, bat.fold_table, got[1])):
+        for patch in (0, 16):
+            pest, sde, b1, b2 = (x.cpu().numpy() for x in stats_fn(patch))
+            assert pest.size == len(table)
+            for k, row in enumerate(table):
+                spec = res[k]
+                w = [x.cpu().numpy()[0] for x in api.blsstat(d(spec[0]), d(spec[1]), d(spec[2]), float(row["df"]),
+                                                             float(row["fmin"]), patch)]
+                assert (pest[k], sde[k], b1[k], b2[k]) == tuple(w), (k, patch)

@@ -142,3 +142,26 @@ def test_fold_requests_mixed_equal_plain(solo):
         _eq(res[rid].outputs, want[k])
     for k, rid in enumerate(rr):
         _eq(res[rid].outputs, ref[k])
+
+
+def test_server_returns_spectrum_stats(solo, cuda):
+    """With spectrum_stats, a BLS request returns get_blsstat's record of its spectrum, equal to
+    the image entry point on the solo run's spectrum; other requests are unchanged."""
+    from gtrap_gb300 import api
+    reqs, ref = solo
+    srv = _server(spectrum_stats=True)
+    rids = [srv.submit(r) for r in reqs]
+    res = {r.rid: r for r in srv.run_until_idle()}
+    d = lambda a: torch.from_numpy(np.ascontiguousarray(a).reshape(1, -1)).to(cuda)
+    nbls = 0
+    for k, rid in enumerate(rids):
+        if reqs[k].kind != "bls":
+            _eq(res[rid].outputs, ref[k])
+            continue
+        nbls += 1
+        rec = res[rid].outputs
+        assert rec.dtype == api.BLS_STATS
+        w = [x.cpu().numpy()[0] for x in api.blsstat(d(ref[k][0]), d(ref[k][1]), d(ref[k][2]), reqs[k].df,
+                                                     reqs[k].fmin)]
+        assert (rec["pest"], rec["sde"], rec["ph1"], rec["ph2"]) == tuple(w), k
+    assert nbls >= 2

@@ -140,6 +140,9 @@ def test_new_entry_points_validate_on_the_host(lib):
     assert tr(nb=4096, dmax=2048, F=2) == _native.ERR_INVALID_ARG and b"not built" in lib.gtrap_last_error()
     assert tr(pool=C.c_void_p(257)) == _native.ERR_WORKSPACE
     assert tr(nbytes=1000) == _native.ERR_WORKSPACE
+    assert lib.gtrap_blsstat_packed(P, P, P, P, None, 0, 0, P, P, P, P, None) == 0  # nothing to do
+    assert lib.gtrap_blsstat_packed(None, P, P, P, None, 3, 0, P, P, P, P, None) == _native.ERR_INVALID_ARG
+    assert lib.gtrap_blsstat_packed(P, P, P, None, None, 3, 0, P, P, P, P, None) == _native.ERR_INVALID_ARG
 
     rec = np.zeros(1, api.TRANSIT_PARAMS)
     rec["per"], rec["a"], rec["rp"] = -1.0, 10.0, 0.1
