@@ -160,6 +160,8 @@ def test_fold_only_batch_and_fp32_phase_neighbours(cuda):
     alone = B.RaggedBatch(BLS, TLS, detrend_r=R, fold=FOLD)
     for k, c in enumerate(mix):
         alone.add_fold(c["t"], c["x"], 20 + 3 * k, 0.05, 0.02)
+    for nf in (1, 2):  # a single item shorter than a frequency group
+        alone.add_fold(mix[0]["t"], mix[0]["x"], nf, 0.05, 0.02)
     alone.build()
     stages = alone.capture_stages()
     assert set(stages) == {"prep", "fold"}
@@ -186,6 +188,10 @@ def test_fold_only_batch_and_fp32_phase_neighbours(cuda):
     _same(got, _results(mixed))
     for k in range(mixed.n_fold):  # the same curves gave the same folded spectra alone
         np.testing.assert_array_equal(got[1][k][0], _results(alone)[1][2 * k + 1][0])
+    short = _results(alone)[1]
+    for j, nf in ((6, 1), (7, 2)):  # and the short grids are the first frequencies of curve 0's
+        assert short[j][0].size == nf
+        np.testing.assert_array_equal(short[j][0], short[0][0][:nf])
 
 
 def test_packed_spectrum_stats(mixed, cuda):

@@ -165,3 +165,17 @@ def test_server_returns_spectrum_stats(solo, cuda):
                                                      reqs[k].fmin)]
         assert (rec["pest"], rec["sde"], rec["ph1"], rec["ph2"]) == tuple(w), k
     assert nbls >= 2
+    # folded requests: the record of (tsr, start, duration index) of the plain per-request run
+    curves = synth.ragged_mix(3, seed=5200, n_range=(500, 3000))
+    folds = [S.Request("fold", c["t"], c["x"], nf=30 + 7 * k, fmin=float(np.float32(0.1)),
+                       df=float(np.float32(0.015))) for k, c in enumerate(curves)]
+    plain = S.PlainServer(BLS, TLS, detrend_r=R, fold=FOLD)
+    srv = _server(spectrum_stats=True, fold=FOLD, fold_tiles=5)
+    rids = [srv.submit(f) for f in folds]
+    res = {r.rid: r for r in srv.run_until_idle()}
+    for k, rid in enumerate(rids):
+        full = plain.process(folds[k]).outputs
+        w = [x.cpu().numpy()[0] for x in api.blsstat(d(full[0]), d(full[1]), d(full[2]), folds[k].df,
+                                                     folds[k].fmin)]
+        rec = res[rid].outputs
+        assert (rec["pest"], rec["sde"], rec["ph1"], rec["ph2"]) == tuple(w), k
