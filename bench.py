@@ -441,13 +441,16 @@ def build_batch(mix, dev_index, tls_kind="gtls"):
     return bat.build()
 
 
-def cpu_mix_rates(mix, threads, seconds):
+def cpu_mix_rates(mix, threads, seconds, tls_kind="gtls"):
     """The reference's algorithm on the host for a bounded sample of the mix: scipy's median
-    filter, get_offset and the FP64 restatements of geebls and gtls, each kind run over
-    curves until ``seconds`` have passed.  Returns per-kind rates and a description."""
+    filter, get_offset and the FP64 restatements of geebls and gtls (or of the folded search,
+    for ``tls_kind`` "fold"), each kind run over curves until ``seconds`` have passed.
+    Returns per-kind rates and a description."""
     import oracle
+    oracle.medfilt_residual(np.zeros((64, 1), np.float32), R_MEDIAN)  # imports outside the timing
     bls = [c for c in mix if c["kind"] == "bls"]
-    tls = [c for c in mix if c["kind"] == "tls"]
+    tls = [c for c in mix if c["kind"] == "tls"] if tls_kind == "gtls" else []
+    fold = [c for c in mix if c["kind"] == "tls"] if tls_kind == "fold" else []
     t_med = n_med = 0.0
     t_b = e_b = 0.0
     t_t = e_t = 0.0
@@ -484,25 +487,56 @@ def cpu_mix_rates(mix, threads, seconds):
         nt_c += 1
         if t_t >= seconds:
             break
-    rates = {"bls": e_b / t_b, "tls": e_t / t_t, "medfilt_samples": n_med / t_med}
-    desc = ("%d BLS curves x <=%d frequencies and %d GTLS curves x <=%d epochs of the mix "
-            "(scipy medfilt + get_offset + FP64 geebls/gtls restatements), %.1f s"
-            % (nb_c, 64 * threads, nt_c, 512 * threads, t_med + t_b + t_t))
-    return rates, desc, t_med + t_b + t_t
+    t_f = e_f = 0.0
+    nf_c = 0
+    for c in fold:  # frequencies spread over the curve's grid, OpenMP over frequencies
+        t0 = time.perf_counter()
+        resid = oracle.medfilt_residual(c["x"][:, None], R_MEDIAN)
+        t1 = time.perf_counter()
+        off = oracle.offset(resid, c["t"][:, None]).astype(np.float32)
+        nf, fmin, df = fold_grid(c)
+        nfs = 2 * threads
+        oracle.tls_fold(resid, c["t"][:, None], off, nfs, TF_NB, np.float32(fmin), np.float32(df * (nf // nfs)),
+                        TF_DURS, lfrac=TF_LFRAC, dmax=TF_DMAX)
+        t2 = time.perf_counter()
+        t_med += t1 - t0
+        n_med += c["x"].size
+        t_f += t2 - t1
+        e_f += nfs
+        nf_c += 1
+        if t_f >= seconds:
+            break
+    rates = {"bls": e_b / t_b, "medfilt_samples": n_med / t_med}
+    if tls:
+        rates["tls"] = e_t / t_t
+        desc = ("%d BLS curves x <=%d frequencies and %d GTLS curves x <=%d epochs of the mix "
+                "(scipy medfilt + get_offset + FP64 geebls/gtls restatements), %.1f s"
+                % (nb_c, 64 * threads, nt_c, 512 * threads, t_med + t_b + t_t))
+    else:
+        rates["fold"] = e_f / t_f
+        desc = ("%d BLS curves x <=%d frequencies and %d folded-search curves x %d frequencies of the mix "
+                "(scipy medfilt + get_offset + FP64 geebls and folded-search restatements), %.1f s"
+                % (nb_c, 64 * threads, nf_c, 2 * threads, t_med + t_b + t_f))
+    return rates, desc, t_med + t_b + t_t + t_f
 
 
 def cpu_mix_value(mix, rates):
     """Evaluations per second of the whole mix at the sampled per-kind CPU rates."""
     bls_ev = sum(c["nf"] for c in mix if c["kind"] == "bls")
-    tls_ev = sum(c["x"].size for c in mix if c["kind"] == "tls")
+    if "fold" in rates:  # TLS-kind curves through the folded search: (curve, frequency) evals
+        tls_ev = sum(fold_grid(c)[0] for c in mix if c["kind"] == "tls")
+        r_tls = rates["fold"]
+    else:
+        tls_ev = sum(c["x"].size for c in mix if c["kind"] == "tls")
+        r_tls = rates["tls"]
     samples = sum(c["x"].size for c in mix)
-    t = bls_ev / rates["bls"] + tls_ev / rates["tls"] + samples / rates["medfilt_samples"]
+    t = bls_ev / rates["bls"] + tls_ev / r_tls + samples / rates["medfilt_samples"]
     return (bls_ev + tls_ev) / t
 
 
-def ragged_cpu_baseline(mix, seconds=6.0):
+def ragged_cpu_baseline(mix, seconds=6.0, tls_kind="gtls"):
     threads = os.cpu_count() or 1
-    rates, desc, _ = cpu_mix_rates(mix, threads, seconds)
+    rates, desc, _ = cpu_mix_rates(mix, threads, seconds, tls_kind)
     return {"value": cpu_mix_value(mix, rates), "unit": UNIT, "cores": threads, "kind": "port",
             "sample": desc, "rates": rates}
 
@@ -514,18 +548,18 @@ def run_ragged_reference(args, rank, world):
     mix = make_mix(nc, 4000)
     threads = os.cpu_count() or 1
     for _ in range(args.warmup):
-        cpu_mix_rates(mix[:40], threads, 0.2)
+        cpu_mix_rates(mix[:40], threads, 0.2, args.tls_kind)
     vals, total = [], 0.0
     desc = ""
     for k in range(args.steps):
-        rates, desc, dt = cpu_mix_rates(mix[200 * k:], threads, 1.5)
+        rates, desc, dt = cpu_mix_rates(mix[200 * k:], threads, 1.5, args.tls_kind)
         vals.append(cpu_mix_value(mix, rates))
         total += dt
     value = float(np.median(vals))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": ragged_config(nc),
+            "data": "synthetic", "config": ragged_config(nc, None, args.tls_kind),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": "per step: " + desc},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -722,8 +756,8 @@ def run_ragged(args, rank, world, local_rank):
         line["plain"] = plain
     if e2e:
         line["e2e"] = e2e
-    if not args.no_cpu_baseline and args.tls_kind == "gtls":
-        line["cpu_baseline"] = ragged_cpu_baseline(mix)
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = ragged_cpu_baseline(mix, tls_kind=args.tls_kind)
     print(json.dumps(line), flush=True)
 
 
