@@ -312,6 +312,25 @@ int gtrap_tls_fold_run(const gtrap_bls_curve *curves, const gtrap_bls_segment *s
                        uint32_t *dur, float *depth, gtrap_stream_t stream);
 
 /* ---------------------------------------------------------------------------
+ * The reference's CPU trapezoid fit (gtrap/tls.py:2-110) in FP64 on the device.  t/x: n
+ * samples sorted by t ascending, finite times only (a non-finite time is in no region).
+ * gtrap_tlsfit_grid evaluates get_chi2Hmax (gtrap/tls.py:44-79) for every template
+ * k = (iW*nL + iL)*nT + iT of the grid W[nW] x L[nL] x t0[nT] (device arrays): H[k], res[k]
+ * (chi^2 / sigma^2), npts[k] = nA + .. + nE, xsum[k] (the window mean when divx, else 0) and
+ * tlsfit's sn[k] = -H / sqrt(res / (npts - 3)).  divx = 0 gives get_Hmax's H.
+ * gtrap_nanargmax writes the first index of the largest non-NaN value of v (np.nanargmax),
+ * -1 when all are NaN.  gtrap_gen_trapezoid writes gen_trapzoid(t, H, W, L, t0) + offset
+ * (gtrap/tls.py:2-15) for any t (not sorted).
+ * ------------------------------------------------------------------------- */
+int gtrap_tlsfit_grid(const double *t, const double *x, uint32_t n, const double *W, uint32_t nW,
+                      const double *L, uint32_t nL, const double *t0, uint32_t nT, double sigma,
+                      int32_t divx, double *H, double *res, int32_t *npts, double *xsum, double *sn,
+                      gtrap_stream_t stream);
+int gtrap_nanargmax(const double *v, uint64_t count, int64_t *index, gtrap_stream_t stream);
+int gtrap_gen_trapezoid(double *out, const double *t, uint32_t n, double H, double W, double L, double t0,
+                        double offset, gtrap_stream_t stream);
+
+/* ---------------------------------------------------------------------------
  * Candidate windows for the classifier.  Replaces pick_Wnormalized_cleaned_lc_direct
  * (gtrap/picktrap.py:27-172) for a batch of candidates: candidate c lies on curve curve[c]
  * (series lc/tu[off[q] + e*stride], e < n[q]) at time T0[c] with width W[c] (days).  Writes
