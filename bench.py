@@ -25,6 +25,9 @@ same curves: 8192 periods (0.5 .. 12 d) x 8 durations (0.5 .. 8 h) x 2048 phase 
 ``--workload served``: the continuous-batching server under Poisson arrivals (p50/p99
 latency per offered load).  ``--workload mock``: mock transit injection as the TESS mock driver
 does it (one drawn planet per curve, lc *= 2 - model, plus trends) on 4096 x 18,000 samples.
+``--workload tlsfit``: the reference's CPU trapezoid fit (gtrap/tls.py tlsfit) on one TESS-like
+curve over 8 widths x 8 ingress lengths x 4320 epochs, in FP64.  ``--tls-kind fold`` sends the
+TLS half of the ragged and served mixes through the folded search instead of GTLS.
 
 ``--impl reference`` times the reference's algorithm on the host CPU (the FP64 C
 restatement of geebls and gtls with scipy's median filter, all host threads) on a bounded
@@ -68,7 +71,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="ragged",
-                   choices=["ragged", "masked", "served", "plain", "tls", "tlsfold", "mock"])
+                   choices=["ragged", "masked", "served", "plain", "tls", "tlsfold", "mock", "tlsfit"])
     p.add_argument("--nq", type=int, default=None,
                    help="curves per GPU (default: 10,000 ragged, 1024 masked)")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -763,7 +766,13 @@ def run_ragged(args, rank, world, local_rank):
 
 # ----------------------------------------------------------------------------- image workloads
 
-def _timed(fn, steps, warmup, dev, world):
+L2_FLUSH_BYTES = 256 << 20  # more than the 129 MB L2
+
+
+def _timed(fn, steps, warmup, dev, world, flush=False):
+    """Mean CUDA-event time of ``steps`` calls after ``warmup`` untimed ones.  With ``flush``
+    (inputs that fit in L2) a 256 MiB buffer is written before every timed call, outside its
+    events, so each call starts from a cold L2."""
     import torch
     import torch.distributed as dist
     stream = torch.cuda.current_stream(dev)
@@ -774,14 +783,26 @@ def _timed(fn, steps, warmup, dev, world):
     torch.cuda.synchronize(dev)
     clocks = ClockSampler(dev.index)
     clocks.start()
-    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    s.record(stream)
-    for _ in range(steps):
-        fn()
-    e.record(stream)
-    torch.cuda.synchronize(dev)
+    if flush:
+        buf = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for k in range(steps):
+            buf.fill_(k & 0xff)
+            ev[k][0].record(stream)
+            fn()
+            ev[k][1].record(stream)
+        torch.cuda.synchronize(dev)
+        ms = sum(a.elapsed_time(b) for a, b in ev)
+    else:
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        for _ in range(steps):
+            fn()
+        e.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = s.elapsed_time(e)
     clk = clocks.stop()
-    t = torch.tensor([s.elapsed_time(e) / steps], device=dev, dtype=torch.float64)
+    t = torch.tensor([ms / steps], device=dev, dtype=torch.float64)
     if world > 1:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t[0]), clk
@@ -810,7 +831,8 @@ def run_image(args, rank, world, local_rank):
         evals = nq * wl.nf
         cfg = {"workload": "plain BLS (geebls_simple): %d curves x 4096 samples, nf 4096, nb 1024, "
                            "qmi 0.005, qma 0.1" % nq, "curves_per_gpu": nq,
-               "l2": "inputs 1 MiB (fit in L2; the kernel is compute bound)"}
+               "l2": "inputs 1 MiB fit in L2: a 256 MiB buffer is written before every timed step, "
+                     "outside its CUDA events"}
     else:
         nq = args.nq or 4096
         lcn, tun, _ = synth.tess_like(nq=nq, n=18000, seed=3000 + 100000 * rank)
@@ -824,7 +846,7 @@ def run_image(args, rank, world, local_rank):
                            "(8 h .. 0.5 h), nl 16, nsc %d; 128 templates per (curve, epoch)"
                            % (nq, g["nsc"]), "curves_per_gpu": nq, "templates_per_eval": 128,
                "l2": "inputs %d MiB per GPU exceed L2" % (2 * nq * 18000 * 4 >> 20)}
-    ms, clk = _timed(fn, args.steps, args.warmup, dev, world)
+    ms, clk = _timed(fn, args.steps, args.warmup, dev, world, flush=args.workload == "plain")
     e2e = None
     if not args.no_e2e:
         h_lc, h_tu = torch.from_numpy(np.ascontiguousarray(lcn)).pin_memory(), torch.from_numpy(np.ascontiguousarray(tun)).pin_memory()
@@ -1292,6 +1314,183 @@ def run_served(args, rank, world, local_rank):
     print(json.dumps(line), flush=True)
 
 
+# ----------------------------------------------------------------------------- trapezoid grid fit
+
+FIT_UNIT = "templates/s"
+FIT_METRIC = "trapezoid grid fit (gtrap/tls.py tlsfit): (W, L, t0) templates/sec"
+FIT_W = np.linspace(0.5, 8.0, 8) / 24.0       # widths 0.5 .. 8 h (days)
+FIT_L = np.linspace(2.0, 30.0, 8) / 1440.0    # ingress 2 .. 30 min (days)
+FIT_STRIDE = 4                                # epochs: every fourth valid sample time
+FIT_FLOPS = 10.0                              # FP64 flops per (template, window sample)
+
+
+def fit_case(rank=0):
+    """One TESS-like curve of config 3's shape (18,000 samples at 2 min, a 1-day gap, a
+    trapezoid) and the epoch grid."""
+    from gtrap_gb300 import synth
+    lcn, tun, _ = synth.tess_like(nq=1, n=18000, seed=3000 + 100000 * rank, transit_frac=1.0)
+    t = tun[:, 0].astype(np.float64)
+    x = lcn[:, 0].astype(np.float64)
+    return t, x, t[t >= 0][::FIT_STRIDE]
+
+
+def fit_config(nT):
+    return {"workload": "trapezoid grid fit of gtrap/tls.py (tlsfit: get_chi2Hmax over W x L x t0, FP64): one "
+                        "TESS-like curve of 18000 samples at 2 min with a 1-day gap; W 8 values 0.5..8 h, L 8 "
+                        "values 2..30 min, t0 every fourth sample time (%d); %d templates" % (nT, 64 * nT),
+            "templates": 64 * nT, "l2": "inputs 0.3 MiB fit in L2: a 256 MiB buffer is written before every "
+                                        "timed step, outside its CUDA events"}
+
+
+def fit_window_samples(t, tl):
+    """Samples in each template's window (t - t0 in [min(-W/2, -W/4-L/2), max(W/2, W/4+L/2)])."""
+    ts = np.sort(t[np.isfinite(t)])
+    tot = 0
+    for W in FIT_W:
+        for L in FIT_L:
+            lo = tl + min(-W / 2, -W / 4 - L / 2)
+            hi = tl + max(W / 2, W / 4 + L / 2)
+            tot += int((np.searchsorted(ts, hi, "right") - np.searchsorted(ts, lo, "left")).sum())
+    return tot
+
+
+def fit_cpu_sample(t, x, tl, seconds):
+    """The reference's algorithm (oracle port of gtrap/tls.py get_chi2Hmax, NumPy, one core)
+    over templates spread through the grid until ``seconds`` pass.  Returns (templates/s, count,
+    seconds)."""
+    from oracle import tls_cpu
+    rng = np.random.default_rng(5)
+    cnt, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        W, L, T = FIT_W[rng.integers(8)], FIT_L[rng.integers(8)], tl[rng.integers(tl.size)]
+        tls_cpu.get_chi2Hmax(t, x, W, L, T)
+        cnt += 1
+    dt = time.perf_counter() - t0
+    return cnt / dt, cnt, dt
+
+
+def fit_sampled_parity(t, x, tl, H, res):
+    """Sampled grid points against the oracle: max relative error of H and chi^2."""
+    from oracle import tls_cpu
+    rng = np.random.default_rng(9)
+    nT = tl.size
+    eh = er = 0.0
+    for k in rng.choice(H.size, 48, replace=False):
+        iW, iL, iT = k // (8 * nT), (k // nT) % 8, k % nT
+        oh, ores, _, _ = tls_cpu.get_chi2Hmax(t, x, FIT_W[iW], FIT_L[iL], tl[iT])
+        if np.isfinite(oh):
+            eh = max(eh, abs(H[k] - oh) / max(abs(oh), 1e-300))
+            er = max(er, abs(res[k] - ores) / max(abs(ores), 1e-300))
+    return {"sample": "48 grid points (FP64 oracle)", "h_max_err_rel": eh, "chi2_max_err_rel": er}
+
+
+def fp64_peak_tflops(dev):
+    """FP64 FMA issue peak of this GPU, measured live (MEASURED_PEAKS.json has no FP64 figure)."""
+    import torch
+    from gtrap_gb300 import api
+    stream = torch.cuda.current_stream(dev)
+    _, flops = api.fp64_peak_probe(iters=256)
+    torch.cuda.synchronize(dev)
+    ps, pe = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ps.record(stream)
+    for _ in range(3):
+        api.fp64_peak_probe(iters=256)
+    pe.record(stream)
+    torch.cuda.synchronize(dev)
+    return flops * 3 / (ps.elapsed_time(pe) / 1e3) / 1e12
+
+
+def run_tlsfit(args, rank, world, local_rank):
+    import torch
+    from gtrap_gb300 import _build, _native as N, tls
+    from gtrap_gb300._dev import as_ptr
+    _build.build()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    t, x, tl = fit_case(rank)
+    ts, xs = tls._sorted_series(t, x, dev)
+    Wd, Ld, Td = (tls._d64(v, dev) for v in (FIT_W, FIT_L, tl))
+    k = 64 * tl.size
+    H = torch.empty(k, dtype=torch.float64, device=dev)
+    res, xsum, sn = torch.empty_like(H), torch.empty_like(H), torch.empty_like(H)
+    npts = torch.empty(k, dtype=torch.int32, device=dev)
+    idx = torch.empty(1, dtype=torch.int64, device=dev)
+    h = torch.cuda.current_stream(dev).cuda_stream
+
+    def fn():
+        N.call("gtrap_tlsfit_grid", as_ptr(ts), as_ptr(xs), ts.numel(), as_ptr(Wd), 8, as_ptr(Ld), 8, as_ptr(Td),
+               tl.size, 1.0, 1, as_ptr(H), as_ptr(res), as_ptr(npts), as_ptr(xsum), as_ptr(sn), h)
+        N.call("gtrap_nanargmax", as_ptr(sn), k, as_ptr(idx), h)
+
+    ms, clk = _timed(fn, args.steps, args.warmup, dev, world, flush=True)
+    value = k * world / (ms / 1e3)
+    e2e = None
+    if not args.no_e2e:  # the drop-in call from host arrays: upload, sort, grid, argmax, model, download
+        tls.tlsfit(t, x, FIT_W, FIT_L, tl)
+        torch.cuda.synchronize(dev)
+        w0 = time.perf_counter()
+        for _ in range(args.steps):
+            out = tls.tlsfit(t, x, FIT_W, FIT_L, tl)
+        e_ms = 1e3 * (time.perf_counter() - w0) / args.steps
+        e2e = {"value": k * world / (e_ms / 1e3), "unit": FIT_UNIT, "ms_per_step": e_ms,
+               "h2d_bytes_per_step": 16 * t.size + 8 * (16 + tl.size) + 8 * t.size,
+               "d2h_bytes_per_step": 8 * t.size + 8 * 3 + 8,
+               "api": "gtrap_gb300.tls.tlsfit on host NumPy arrays (timed on the host clock; the call "
+                      "synchronises when it returns its scalars)",
+               "best": {"W": float(out[2]), "L": float(out[3]), "T0": float(out[4]), "H": float(out[1])}}
+    if rank != 0:
+        return
+    peak = fp64_peak_tflops(dev)
+    flops = FIT_FLOPS * fit_window_samples(t, tl)
+    achieved = flops / (ms / 1e3) / 1e12
+    line = {"metric": FIT_METRIC, "value": value, "unit": FIT_UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": fit_config(tl.size) | {"parallelism": "replicas x%d" % world},
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "kernel": "tlsfit_kernel (one warp per template) + nanargmax_kernel",
+                         "algorithmic_flops": "%g FP64 flops per (template, window sample): mean, region sums "
+                                              "and residual passes" % FIT_FLOPS,
+                         "peak_source": "live FP64 FMA-chain probe on this GPU (MEASURED_PEAKS.json has no FP64 "
+                                        "figure)"},
+            "gpu_launches": 2 * args.steps, "clocks": clk}
+    line["parity"] = fit_sampled_parity(t, x, tl, H.cpu().numpy(), res.cpu().numpy())
+    if e2e:
+        line["e2e"] = e2e
+    if not args.no_cpu_baseline:
+        v, cnt, dt = fit_cpu_sample(t, x, tl, 10.0)
+        line["cpu_baseline"] = {"value": v, "unit": FIT_UNIT, "cores": 1, "kind": "port",
+                                "sample": "%d templates spread over the grid, one core, NumPy oracle port of "
+                                          "get_chi2Hmax (as the reference), %.1f s" % (cnt, dt)}
+    print(json.dumps(line), flush=True)
+
+
+def run_tlsfit_reference(args, rank, world):
+    """The reference's CPU path: the NumPy port of get_chi2Hmax on one core (tlsfit has no
+    threading), a bounded sample of templates per step."""
+    if rank != 0:
+        return
+    t, x, tl = fit_case()
+    for _ in range(args.warmup):
+        fit_cpu_sample(t, x, tl, 0.2)
+    vals, total, cnt = [], 0.0, 0
+    for _ in range(args.steps):
+        v, c, dt = fit_cpu_sample(t, x, tl, 2.0)
+        vals.append(v)
+        total += dt
+        cnt += c
+    value = float(np.median(vals))
+    line = {"impl": "reference", "metric": FIT_METRIC, "value": value, "unit": FIT_UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": fit_config(tl.size),
+            "cpu_baseline": {"value": value, "unit": FIT_UNIT, "cores": 1, "kind": "port",
+                             "sample": "per step about 2 s of templates spread over the grid (%d in all)" % cnt},
+            "e2e": {"value": value, "unit": FIT_UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -1304,6 +1503,8 @@ def main():
             run_tlsfold_reference(args, rank, world)
         elif args.workload == "mock":
             run_mock_reference(args, rank, world)
+        elif args.workload == "tlsfit":
+            run_tlsfit_reference(args, rank, world)
         else:
             run_ragged_reference(args, rank, world)
         return
@@ -1314,7 +1515,7 @@ def main():
         dist.init_process_group("nccl")
     try:
         {"ragged": run_ragged, "masked": run_masked, "served": run_served, "plain": run_image,
-         "tls": run_image, "tlsfold": run_tlsfold, "mock": run_mock}[args.workload](
+         "tls": run_image, "tlsfold": run_tlsfold, "mock": run_mock, "tlsfit": run_tlsfit}[args.workload](
             args, rank, world, local_rank)
     finally:
         if world > 1:

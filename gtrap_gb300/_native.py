@@ -76,6 +76,7 @@ _SIGNATURES = {
     "gtrap_peakstat_max_samples": (sz, []),
     "gtrap_peakstat": (C.c_int, [vp, vp, vp, u64, u32, u32, u32, u32, u32, vp, vp, vp, vp]),
     "gtrap_probe_fp32_peak": (C.c_int, [vp, u32, C.POINTER(C.c_double), vp]),
+    "gtrap_probe_fp64_peak": (C.c_int, [vp, u32, C.POINTER(C.c_double), vp]),
     "gtrap_probe_smem_atomic_peak": (C.c_int, [vp, u32, C.POINTER(C.c_double), vp]),
     "gtrap_probe_smem_load_peak": (C.c_int, [vp, u32, C.POINTER(C.c_double), vp]),
     "gtrap_transit_flux": (C.c_int, [vp, vp, u32, vp, vp]),

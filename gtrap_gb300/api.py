@@ -249,6 +249,14 @@ def fp32_peak_probe(iters=4096, stream=None):
     return sink, flops.value
 
 
+def fp64_peak_probe(iters=1024, stream=None):
+    """Launch the FP64 FMA probe; returns (sink tensor, flop count)."""
+    sink = torch.empty(1 << 20, dtype=torch.float64, device="cuda")
+    flops = C.c_double(0.0)
+    N.call("gtrap_probe_fp64_peak", as_ptr(sink), int(iters), C.byref(flops), stream_handle(stream))
+    return sink, flops.value
+
+
 # Record layout of gtrap_peak_stats (include/gtrap_gb300.h).
 
 PEAK_STATS = _np.dtype([("maxsn", "<f4"), ("argmax", "<u4"), ("lent", "<u4"), ("npeaks", "<u4"),

@@ -131,6 +131,21 @@ __global__ void __launch_bounds__(256) fp32_probe_kernel(float *sink, uint32_t i
   float s = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
   if (s == 1234.5f) sink[blockIdx.x * blockDim.x + threadIdx.x] = s;  // never true; keeps the work
 }
+// FP64 FMA-chain peak: as fp32_probe_kernel with eight independent double chains per thread.
+__global__ void __launch_bounds__(256) fp64_probe_kernel(double *sink, uint32_t iters) {
+  double a0 = threadIdx.x * 1e-9, a1 = a0 + 1e-9, a2 = a0 + 2e-9, a3 = a0 + 3e-9;
+  double a4 = a0 + 4e-9, a5 = a0 + 5e-9, a6 = a0 + 6e-9, a7 = a0 + 7e-9;
+  const double m = 0.999999999, c = 1e-9;
+  for (uint32_t it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      a0 = fma(a0, m, c); a1 = fma(a1, m, c); a2 = fma(a2, m, c); a3 = fma(a3, m, c);
+      a4 = fma(a4, m, c); a5 = fma(a5, m, c); a6 = fma(a6, m, c); a7 = fma(a7, m, c);
+    }
+  }
+  double s = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
+  if (s == 1234.5) sink[blockIdx.x * blockDim.x + threadIdx.x] = s;  // never true; keeps the work
+}
 // Shared-memory atomic issue peak for the BLS fold's pattern: per update two 32-bit atomic
 // adds to random bins of one of four 2048-bin histograms (64 KB per block, two blocks per SM).
 constexpr int kAtomBins = 2048, kAtomHist = 4;
@@ -205,6 +220,15 @@ int gtrap_probe_fp32_peak(float *sink, uint32_t iters, double *flops, gtrap_stre
   fp32_probe_kernel<<<blocks, threads, 0, stream>>>(sink, iters);
   if (flops) *flops = 2.0 * 8.0 * 16.0 * (double)iters * threads * blocks;
   return gtrap::check_launch("fp32_probe_kernel");
+}
+
+int gtrap_probe_fp64_peak(double *sink, uint32_t iters, double *flops, gtrap_stream_t stream) {
+  if (!sink || iters == 0) return gtrap::fail(GTRAP_ERR_INVALID_ARG, "probe: bad arguments");
+  const int threads = 256;
+  const int blocks = gtrap::sm_count() * 8;
+  fp64_probe_kernel<<<blocks, threads, 0, stream>>>(sink, iters);
+  if (flops) *flops = 2.0 * 8.0 * 16.0 * (double)iters * threads * blocks;
+  return gtrap::check_launch("fp64_probe_kernel");
 }
 
 }  // extern "C"

@@ -382,6 +382,9 @@ int gtrap_peakstat(const float *sn, const uint64_t *off, const uint32_t *n, uint
 /* FP32 issue peak: launches a register-resident FMA-chain kernel; *flops receives the
  * number of FP32 floating-point operations it performs (an FMA counts as 2). */
 int gtrap_probe_fp32_peak(float *sink, uint32_t iters, double *flops, gtrap_stream_t stream);
+/* The same FMA-chain probe in FP64 (eight double chains a thread); sink holds
+ * sm_count*8*256 doubles. */
+int gtrap_probe_fp64_peak(double *sink, uint32_t iters, double *flops, gtrap_stream_t stream);
 /* Shared-memory atomic peak for the BLS fold's pattern: *updates receives the number of
  * (two 32-bit atomic adds to random bins) updates the launch performs. */
 int gtrap_probe_smem_atomic_peak(unsigned *sink, uint32_t iters, double *updates, gtrap_stream_t stream);

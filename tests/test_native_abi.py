@@ -141,6 +141,13 @@ def test_new_entry_points_validate_on_the_host(lib):
     assert tr(pool=C.c_void_p(257)) == _native.ERR_WORKSPACE
     assert tr(nbytes=1000) == _native.ERR_WORKSPACE
     assert lib.gtrap_blsstat_packed(P, P, P, P, None, 0, 0, P, P, P, P, None) == 0  # nothing to do
+    assert lib.gtrap_tlsfit_grid(P, P, 10, P, 0, P, 3, P, 3, 1.0, 1, P, P, P, P, P, None) == 0  # empty grid
+    assert lib.gtrap_tlsfit_grid(None, P, 10, P, 2, P, 3, P, 3, 1.0, 1, P, P, P, P, P, None) == _native.ERR_INVALID_ARG
+    assert lib.gtrap_tlsfit_grid(P, P, 10, P, 2, P, 3, P, 3, 1.0, 1, P, P, P, P, None, None) == _native.ERR_INVALID_ARG
+    assert lib.gtrap_nanargmax(None, 3, P, None) == _native.ERR_INVALID_ARG
+    assert lib.gtrap_gen_trapezoid(P, P, 0, 1.0, 1.0, 0.1, 0.0, 0.0, None) == 0  # nothing to do
+    assert lib.gtrap_gen_trapezoid(None, P, 5, 1.0, 1.0, 0.1, 0.0, 0.0, None) == _native.ERR_INVALID_ARG
+    assert lib.gtrap_probe_fp64_peak(None, 10, None, None) == _native.ERR_INVALID_ARG
     assert lib.gtrap_blsstat_packed(None, P, P, P, None, 3, 0, P, P, P, P, None) == _native.ERR_INVALID_ARG
     assert lib.gtrap_blsstat_packed(P, P, P, None, None, 3, 0, P, P, P, P, None) == _native.ERR_INVALID_ARG
 
