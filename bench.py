@@ -1449,7 +1449,7 @@ def run_tlsfit(args, rank, world, local_rank):
             "config": fit_config(tl.size) | {"parallelism": "replicas x%d" % world},
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak, "traffic": None,
-                         "kernel": "tlsfit_kernel (one warp per template) + nanargmax_kernel",
+                         "kernel": "tlsfit_kernel (one thread per template) + nanargmax_kernel",
                          "algorithmic_flops": "%g FP64 flops per (template, window sample): mean, region sums "
                                               "and residual passes" % FIT_FLOPS,
                          "peak_source": "live FP64 FMA-chain probe on this GPU (MEASURED_PEAKS.json has no FP64 "

@@ -4,9 +4,10 @@
 //
 // The reference masks the whole series per template (about 15 passes over n samples).  Here
 // the samples are sorted by time once, so a template's samples are the index window whose
-// t - t0 lies in [-W/2, W/2] (wider when L/2 > W/4): two binary searches on the monotone
-// predicate fl(t - t0) >= a (rounding is monotone) find it, and one warp makes three passes
-// over the window: the mean
+// t - t0 lies in [-W/2, W/2] (wider when L/2 > W/4), and each region is an index range:
+// seven binary searches on the monotone predicate fl(t - t0) >= a (rounding is monotone) find
+// them, and one thread per template makes three passes over the ranges, with no comparisons of
+// times and no cross-lane reductions (both would issue on the narrow FP64 pipe): the mean
 // over |t - t0| <= W/2 (divx), the region sums, and the residual with the fitted depth.  The
 // region masks, the boundary expressions (-W/4 - L/2 evaluated as (-W/4) - L/2 ...), the
 // nansum semantics (counts over all samples, sums over finite flux) and the formulas of denA,
@@ -21,7 +22,6 @@ namespace {
 using gtrap::fail;
 
 constexpr int kFitThreads = 256;
-constexpr int kFitWarps = kFitThreads / 32;
 
 struct Bounds {  // region boundaries of a template, as the reference forms them
   double a1, a2, a3, a4, a5, a6;  // -W/2, -W/4-L/2, -W/4+L/2, W/4-L/2, W/4+L/2, W/2
@@ -44,121 +44,110 @@ __device__ __forceinline__ uint32_t first_at_least(const double *t, uint32_t n, 
   return lo;
 }
 
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = __dadd_rn(v, __shfl_xor_sync(0xffffffffu, v, o));
-  return v;
-}
-
-__device__ __forceinline__ int warp_sum_i(int v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
-// One warp per template k = (iW * nL + iL) * nT + iT.  t sorted ascending over [0, n) (finite
-// times; non-finite times belong to no region and are left out by the caller).
+// One thread per template k = (iW * nL + iL) * nT + iT: consecutive threads take consecutive
+// epochs of one (W, L), whose windows overlap, so a warp's loads stay within a few cache lines
+// and its loops have nearly equal trip counts.  t sorted ascending over [0, n) (finite times;
+// non-finite times belong to no region and are left out by the caller).
 __global__ void __launch_bounds__(kFitThreads) tlsfit_kernel(
     const double *__restrict__ t, const double *__restrict__ xx, uint32_t n,
     const double *__restrict__ Wl, uint32_t nW, const double *__restrict__ Ll, uint32_t nL,
     const double *__restrict__ tl, uint32_t nT, double sigma, int divx, double *Hout,
     double *res_out, int32_t *n_out, double *xsum_out, double *sn_out) {
-  const uint64_t k = (uint64_t)blockIdx.x * kFitWarps + (threadIdx.x >> 5);
+  const uint64_t k = (uint64_t)blockIdx.x * kFitThreads + threadIdx.x;
   const uint64_t total = (uint64_t)nW * nL * nT;
-  if (k >= total) return;  // whole warps
-  const int lane = threadIdx.x & 31;
+  if (k >= total) return;
   const uint32_t iT = (uint32_t)(k % nT), iL = (uint32_t)((k / nT) % nL), iW = (uint32_t)(k / ((uint64_t)nT * nL));
   const double W = Wl[iW], L = Ll[iL], t0 = tl[iT];
   const Bounds b = bounds_of(W, L);
-  // the window: fl(t - t0) in [min(a1, a2), max(a5, a6)] (B and D reach past -W/2 and W/2
-  // when L/2 > W/4; the mean's closed interval [a1, a6] is tested inside)
-  const uint32_t lo = first_at_least(t, n, t0, fmin(b.a1, b.a2), false);
-  const uint32_t hi = first_at_least(t, n, t0, fmax(b.a5, b.a6), true);
+  // Every region is an interval of fl(t - t0), so on the sorted series an index range:
+  // A = [i1, i2), B = [i2, i3), C = [i3, i4), D = [i4, i5), E = [i5, i6) with i(a) the first
+  // index where fl(t - t0) >= a (empty or overlapping as the boundaries fall when L/2 > W/4,
+  // like the reference's masks); the mean's closed interval [a1, a6] is [i1, j6).
+  const uint32_t i1 = first_at_least(t, n, t0, b.a1, false), i6 = first_at_least(t, n, t0, b.a6, false);
+  const uint32_t j6 = first_at_least(t, n, t0, b.a6, true);
+  const uint32_t i2 = first_at_least(t, n, t0, b.a2, false), i3 = first_at_least(t, n, t0, b.a3, false);
+  const uint32_t i4 = first_at_least(t, n, t0, b.a4, false), i5 = first_at_least(t, n, t0, b.a5, false);
+  auto cnt = [](uint32_t a, uint32_t e) { return e > a ? (int)(e - a) : 0; };
+  const int nA = cnt(i1, i2), nB = cnt(i2, i3), nC = cnt(i3, i4), nD = cnt(i4, i5), nE = cnt(i5, i6);
 
   double xsum = 0.0;
   if (divx) {  // np.nanmean(xx[(tn >= -W/2) * (tn <= W/2)])
     double s = 0.0;
     int c = 0;
-    for (uint32_t i = lo + lane; i < hi; i += 32) {
-      const double tn = __dsub_rn(t[i], t0), v = xx[i];
-      if (tn >= b.a1 && tn <= b.a6 && !isnan(v)) { s = __dadd_rn(s, v); ++c; }
+    for (uint32_t i = i1; i < j6; ++i) {
+      const double v = xx[i];
+      if (!isnan(v)) { s = __dadd_rn(s, v); ++c; }
     }
-    s = warp_sum(s);
-    c = warp_sum_i(c);
     xsum = __ddiv_rn(s, (double)c);  // 0/0 = NaN as numpy's mean of nothing
   }
-  // region sums; a NaN flux counts in nA..nE but not in the sums (np.nansum)
-  int nA = 0, nB = 0, nC = 0, nD = 0, nE = 0;
-  double sA = 0, sB = 0, sC = 0, sD = 0, sE = 0, xtB = 0, xtD = 0, tB = 0, tD = 0, t2B = 0, t2D = 0;
-  for (uint32_t i = lo + lane; i < hi; i += 32) {
-    const double tn = __dsub_rn(t[i], t0);
-    const double x = __dsub_rn(xx[i], xsum);
-    const bool ok = !isnan(x);
-    if (tn >= b.a1 && tn < b.a2) { ++nA; if (ok) sA = __dadd_rn(sA, x); }
-    if (tn >= b.a2 && tn < b.a3) {
-      ++nB;
-      tB = __dadd_rn(tB, tn);
-      t2B = __dadd_rn(t2B, __dmul_rn(tn, tn));
-      if (ok) sB = __dadd_rn(sB, x);
+  // region sums (np.nansum: NaN terms are skipped; the counts take every sample)
+  auto flux_sum = [&](uint32_t a, uint32_t e) {
+    double acc = 0.0;
+    for (uint32_t i = a; i < e; ++i) {
+      const double x = __dsub_rn(xx[i], xsum);
+      if (!isnan(x)) acc = __dadd_rn(acc, x);
+    }
+    return acc;
+  };
+  struct Ramp { double s, xt, tsum, t2; };
+  auto ramp_sums = [&](uint32_t a, uint32_t e) {
+    Ramp m{0.0, 0.0, 0.0, 0.0};
+    for (uint32_t i = a; i < e; ++i) {
+      const double tn = __dsub_rn(t[i], t0);
+      const double x = __dsub_rn(xx[i], xsum);
+      m.tsum = __dadd_rn(m.tsum, tn);
+      m.t2 = __dadd_rn(m.t2, __dmul_rn(tn, tn));
+      if (!isnan(x)) m.s = __dadd_rn(m.s, x);
       const double xt = __dmul_rn(x, tn);  // NaN for a NaN flux, or an infinite one at tn = 0
-      if (!isnan(xt)) xtB = __dadd_rn(xtB, xt);
+      if (!isnan(xt)) m.xt = __dadd_rn(m.xt, xt);
     }
-    if (tn < b.a4 && tn >= b.a3) { ++nC; if (ok) sC = __dadd_rn(sC, x); }
-    if (tn < b.a5 && tn >= b.a4) {
-      ++nD;
-      tD = __dadd_rn(tD, tn);
-      t2D = __dadd_rn(t2D, __dmul_rn(tn, tn));
-      if (ok) sD = __dadd_rn(sD, x);
-      const double xt = __dmul_rn(x, tn);
-      if (!isnan(xt)) xtD = __dadd_rn(xtD, xt);
-    }
-    if (tn < b.a6 && tn >= b.a5) { ++nE; if (ok) sE = __dadd_rn(sE, x); }
-  }
-  nA = warp_sum_i(nA); nB = warp_sum_i(nB); nC = warp_sum_i(nC); nD = warp_sum_i(nD); nE = warp_sum_i(nE);
-  sA = warp_sum(sA); sB = warp_sum(sB); sC = warp_sum(sC); sD = warp_sum(sD); sE = warp_sum(sE);
-  xtB = warp_sum(xtB); xtD = warp_sum(xtD); tB = warp_sum(tB); tD = warp_sum(tD);
-  t2B = warp_sum(t2B); t2D = warp_sum(t2D);
+    return m;
+  };
+  const double sA = flux_sum(i1, i2), sC = flux_sum(i3, i4), sE = flux_sum(i5, i6);
+  const Ramp mB = ramp_sums(i2, i3), mD = ramp_sums(i4, i5);
   const double xAEC = __dadd_rn(__dadd_rn(sA, sE), sC);
-  const double xBD = __dadd_rn(sB, sD);
-  const double t2BD = __dadd_rn(t2B, t2D);
+  const double xBD = __dadd_rn(mB.s, mD.s);
+  const double t2BD = __dadd_rn(mB.t2, mD.t2);
   // denA = 4*L*L*(nA-nC+nE) + W*W*(nB+nD) + 8*W*(tB-tD) + 16*t2BD, left to right
   const double denA = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(__dmul_rn(__dmul_rn(4.0, L), L), (double)(nA - nC + nE)),
                                                     __dmul_rn(__dmul_rn(W, W), (double)(nB + nD))),
-                                          __dmul_rn(__dmul_rn(8.0, W), __dsub_rn(tB, tD))),
+                                          __dmul_rn(__dmul_rn(8.0, W), __dsub_rn(mB.tsum, mD.tsum))),
                                 __dmul_rn(16.0, t2BD));
   // numB = 8*L*L*xAEC - 4*W*L*xBD + 16*L*(xtD-xtB)
   const double numB = __dadd_rn(__dsub_rn(__dmul_rn(__dmul_rn(__dmul_rn(8.0, L), L), xAEC),
                                           __dmul_rn(__dmul_rn(__dmul_rn(4.0, W), L), xBD)),
-                                __dmul_rn(__dmul_rn(16.0, L), __dsub_rn(xtD, xtB)));
+                                __dmul_rn(__dmul_rn(16.0, L), __dsub_rn(mD.xt, mB.xt)));
   const double H = __ddiv_rn(-numB, denA);
   const double Hh = __ddiv_rn(H, 2.0), HL = __ddiv_rn(H, L), W4 = __ddiv_rn(W, 4.0);
   // residual with the fitted depth: np.nansum of the squared differences per region, which
   // skips every NaN term (a NaN flux, or every term when the depth itself is NaN)
   auto nadd = [](double acc, double d) { const double q = __dmul_rn(d, d); return isnan(q) ? acc : __dadd_rn(acc, q); };
-  double rA = 0, rB = 0, rC = 0, rD = 0, rE = 0;
-  for (uint32_t i = lo + lane; i < hi; i += 32) {
-    const double tn = __dsub_rn(t[i], t0);
-    const double x = __dsub_rn(xx[i], xsum);
-    if (tn >= b.a1 && tn < b.a2) rA = nadd(rA, __dadd_rn(x, Hh));
-    if (tn < b.a4 && tn >= b.a3) rC = nadd(rC, __dsub_rn(x, Hh));
-    if (tn < b.a6 && tn >= b.a5) rE = nadd(rE, __dadd_rn(x, Hh));
-    if (tn >= b.a2 && tn < b.a3) rB = nadd(rB, __dsub_rn(x, __dmul_rn(HL, __dadd_rn(tn, W4))));
-    if (tn < b.a5 && tn >= b.a4) rD = nadd(rD, __dadd_rn(x, __dmul_rn(HL, __dsub_rn(tn, W4))));
+  auto flat_res = [&](uint32_t a, uint32_t e, double level) {  // sum (x - level)^2
+    double acc = 0.0;
+    for (uint32_t i = a; i < e; ++i) acc = nadd(acc, __dsub_rn(__dsub_rn(xx[i], xsum), level));
+    return acc;
+  };
+  const double rA = flat_res(i1, i2, -Hh), rC = flat_res(i3, i4, Hh), rE = flat_res(i5, i6, -Hh);
+  double rB = 0.0, rD = 0.0;
+  for (uint32_t i = i2; i < i3; ++i) {
+    const double tn = __dsub_rn(t[i], t0), x = __dsub_rn(xx[i], xsum);
+    rB = nadd(rB, __dsub_rn(x, __dmul_rn(HL, __dadd_rn(tn, W4))));
   }
-  rA = warp_sum(rA); rB = warp_sum(rB); rC = warp_sum(rC); rD = warp_sum(rD); rE = warp_sum(rE);
-  if (lane == 0) {
-    double res = __dadd_rn(__dadd_rn(rA, rC), rE);
-    res = __dadd_rn(res, rB);
-    res = __dadd_rn(res, rD);
-    res = __ddiv_rn(res, __dmul_rn(sigma, sigma));
-    const int cnt = nA + nB + nC + nD + nE;
-    Hout[k] = H;
-    res_out[k] = res;
-    n_out[k] = cnt;
-    xsum_out[k] = xsum;
-    // tlsfit: sn = -H / sqrt(res / (n - 3))
-    sn_out[k] = __ddiv_rn(-H, sqrt(__ddiv_rn(res, (double)(cnt - 3))));
+  for (uint32_t i = i4; i < i5; ++i) {
+    const double tn = __dsub_rn(t[i], t0), x = __dsub_rn(xx[i], xsum);
+    rD = nadd(rD, __dadd_rn(x, __dmul_rn(HL, __dsub_rn(tn, W4))));
   }
+  double res = __dadd_rn(__dadd_rn(rA, rC), rE);
+  res = __dadd_rn(res, rB);
+  res = __dadd_rn(res, rD);
+  res = __ddiv_rn(res, __dmul_rn(sigma, sigma));
+  const int npt = nA + nB + nC + nD + nE;
+  Hout[k] = H;
+  res_out[k] = res;
+  n_out[k] = npt;
+  xsum_out[k] = xsum;
+  // tlsfit: sn = -H / sqrt(res / (n - 3))
+  sn_out[k] = __ddiv_rn(-H, sqrt(__ddiv_rn(res, (double)(npt - 3))));
 }
 
 // First index of the largest non-NaN value (np.nanargmax); -1 when every value is NaN.
@@ -227,9 +216,9 @@ int gtrap_tlsfit_grid(const double *t, const double *x, uint32_t n, const double
   if (total == 0) return GTRAP_OK;
   if (!t || !x || !W || !L || !t0 || !H || !res || !npts || !xsum || !sn)
     return fail(GTRAP_ERR_INVALID_ARG, "tlsfit_grid: null pointer");
-  if (total > (uint64_t)0x7fffffff * kFitWarps)
+  if (total > (uint64_t)0x7fffffff * kFitThreads)
     return fail(GTRAP_ERR_INVALID_ARG, "tlsfit_grid: too many templates (%llu)", (unsigned long long)total);
-  const uint64_t blocks = (total + kFitWarps - 1) / kFitWarps;
+  const uint64_t blocks = (total + kFitThreads - 1) / kFitThreads;
   tlsfit_kernel<<<(unsigned)blocks, kFitThreads, 0, stream>>>(t, x, n, W, nW, L, nL, t0, nT, sigma, divx, H, res,
                                                               npts, xsum, sn);
   return check_launch("tlsfit_kernel");
