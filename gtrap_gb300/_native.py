@@ -68,6 +68,7 @@ _SIGNATURES = {
     "gtrap_tls_fold_prepare": (C.c_int, [vp, u32, u32, vp, vp, u64, vp, sz, vp]),
     "gtrap_tls_fold_run": (C.c_int, [vp, vp, vp, u32, vp, sz, u64, u32, vp, u32, f32, u32, u32, u32, vp, vp,
                                      vp, vp, vp, vp]),
+    "gtrap_detect_peaks": (C.c_int, [vp, u64, i32, f64, u32, f64, i32, i32, i32, vp, vp, vp, vp]),
     "gtrap_tlsfit_grid": (C.c_int, [vp, vp, u32, vp, u32, vp, u32, vp, u32, f64, i32, vp, vp, vp, vp, vp, vp]),
     "gtrap_nanargmax": (C.c_int, [vp, u64, vp, vp]),
     "gtrap_gen_trapezoid": (C.c_int, [vp, vp, u32, f64, f64, f64, f64, f64, vp]),

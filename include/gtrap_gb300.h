@@ -311,6 +311,15 @@ int gtrap_tls_fold_run(const gtrap_bls_curve *curves, const gtrap_bls_segment *s
                        uint32_t F, uint32_t blocks, uint32_t *counter, float *tsr, uint32_t *start,
                        uint32_t *dur, float *depth, gtrap_stream_t stream);
 
+/* detect_peaks (gtrap/detect_peaks.py:13-143) of one float64 series x[n] on the device, all
+ * options but the plot: mph (used when has_mph), mpd, threshold, edge (0 None, 1 rising,
+ * 2 falling, 3 both), kpsh, valley.  state: n bytes of scratch; indices: room for n values,
+ * receives the peak indices in increasing order; *count (device) their number.  Equal
+ * heights within mpd rank by index (the reference's unstable sort leaves them open). */
+int gtrap_detect_peaks(const double *x, uint64_t n, int32_t has_mph, double mph, uint32_t mpd,
+                       double threshold, int32_t edge, int32_t kpsh, int32_t valley, unsigned char *state,
+                       int64_t *indices, uint64_t *count, gtrap_stream_t stream);
+
 /* ---------------------------------------------------------------------------
  * The reference's CPU trapezoid fit (gtrap/tls.py:2-110) in FP64 on the device.  t/x: n
  * samples sorted by t ascending, finite times only (a non-finite time is in no region).

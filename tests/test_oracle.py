@@ -32,6 +32,23 @@ def test_tls_restatement_matches_reference_golden():
         np.testing.assert_allclose(np.array(got, dtype=float), g["chi2_%d" % k], rtol=1e-10, atol=1e-12)
 
 
+def test_peaks_oracle_matches_reference_option_golden():
+    """The restated detect_peaks (default options) on the option-set golden vectors made by the
+    reference's own detect_peaks."""
+    from oracle import peaks
+    g = np.load(GOLDEN / "detect_peaks_opts_golden.npz")
+    off, allind = g["ind_off"], g["ind_all"]
+    seen = 0
+    for k in range(int(g["ncases"])):
+        has_mph, mph, mpd, thr, edge, kpsh, valley = g["opts"][k]
+        if has_mph or thr > 0 or edge != 1 or kpsh or valley:
+            continue
+        x = g["series_%d" % g["series_of_case"][k]]
+        np.testing.assert_array_equal(peaks.detect_peaks(x, int(mpd)), allind[off[k]:off[k + 1]])
+        seen += 1
+    assert seen >= 10
+
+
 # ----------------------------------------------------------------------------- gfilter
 
 def test_medfilt_known_answer():
