@@ -81,6 +81,7 @@ _SIGNATURES = {
     "gtrap_probe_smem_atomic_peak": (C.c_int, [vp, u32, C.POINTER(C.c_double), vp]),
     "gtrap_probe_smem_load_peak": (C.c_int, [vp, u32, C.POINTER(C.c_double), vp]),
     "gtrap_transit_flux": (C.c_int, [vp, vp, u32, vp, vp]),
+    "gtrap_trend": (C.c_int, [vp, vp, u32, f64, f64, f64, i32, vp]),
     "gtrap_inject_transit": (C.c_int, [vp, vp, vp, vp, C.c_uint64, u32, u32, vp, C.c_int32, vp]),
     "gtrap_gamma_sample": (C.c_int, [vp, u32, C.c_float, C.c_float, C.c_uint64, C.c_uint64, vp, vp]),
 }

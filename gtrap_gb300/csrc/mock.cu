@@ -221,6 +221,24 @@ int check_params(const gtrap_transit_params &q, const char *what) {
 
 extern "C" {
 
+// gensin / gendcos (gtrap/genmock.py:37-43) in double, with NumPy's evaluation order:
+// amp * sin(2*pi*(t - t0) / P) and -amp * cos(4*pi*(t - t0) / P).
+__global__ void __launch_bounds__(256) trend_kernel(double *out, const double *t, uint32_t n, double P,
+                                                    double t0, double amp, int dcos) {
+  const uint32_t k = blockIdx.x * 256 + threadIdx.x;
+  if (k >= n) return;
+  const double d = t[k] - t0;
+  out[k] = dcos ? -amp * cos(4.0 * M_PI * d / P) : amp * sin(2.0 * M_PI * d / P);
+}
+
+int gtrap_trend(double *out, const double *t, uint32_t n, double period, double t0, double amp, int32_t dcos,
+                gtrap_stream_t stream) {
+  if (n == 0) return GTRAP_OK;
+  if (!out || !t) return fail(GTRAP_ERR_INVALID_ARG, "trend: null pointer");
+  trend_kernel<<<(n + 255) / 256, 256, 0, stream>>>(out, t, n, period, t0, amp, dcos ? 1 : 0);
+  return gtrap::check_launch("trend_kernel");
+}
+
 int gtrap_transit_flux(double *flux, const double *t, uint32_t n, const gtrap_transit_params *params,
                        gtrap_stream_t stream) {
   if (n == 0) return GTRAP_OK;

@@ -416,6 +416,10 @@ typedef struct gtrap_transit_params {
   double amp_dcos; /* trend -amp_dcos cos(4 pi (t - t0) / per) */
 } gtrap_transit_params;
 
+/* gensin (dcos = 0: amp sin(2 pi (t - t0) / period)) and gendcos (dcos = 1: -amp cos(4 pi
+ * (t - t0) / period)) of gtrap/genmock.py:37-43 in double at n times. */
+int gtrap_trend(double *out, const double *t, uint32_t n, double period, double t0, double amp, int32_t dcos,
+                gtrap_stream_t stream);
 /* flux[k] = model(t[k]) for one parameter record (host pointer); t and flux are device
  * arrays of n doubles (gentransit's light curve, gtrap/genmock.py:9-34). */
 int gtrap_transit_flux(double *flux, const double *t, uint32_t n, const gtrap_transit_params *params,

@@ -152,6 +152,8 @@ def test_new_entry_points_validate_on_the_host(lib):
     assert lib.gtrap_detect_peaks(P, 10, 0, 0.0, 1, 0.0, 7, 0, 0, P, P, P, None) == _native.ERR_INVALID_ARG
     assert b"edge" in lib.gtrap_last_error()
     assert lib.gtrap_detect_peaks(None, 10, 0, 0.0, 1, 0.0, 1, 0, 0, P, P, P, None) == _native.ERR_INVALID_ARG
+    assert lib.gtrap_trend(P, P, 0, 5.0, 0.0, 1.0, 0, None) == 0  # nothing to do
+    assert lib.gtrap_trend(None, P, 4, 5.0, 0.0, 1.0, 0, None) == _native.ERR_INVALID_ARG
     assert lib.gtrap_blsstat_packed(None, P, P, P, None, 3, 0, P, P, P, P, None) == _native.ERR_INVALID_ARG
     assert lib.gtrap_blsstat_packed(P, P, P, None, None, 3, 0, P, P, P, P, None) == _native.ERR_INVALID_ARG
 
