@@ -165,3 +165,33 @@ def test_fp32_reference_phase_batch(cuda):
     B.run_plain(bat)
     torch.cuda.synchronize()
     _same(got, _results(bat))
+
+
+def test_degenerate_curves_equal_plain(cuda):
+    """Curves of one sample, one frequency, all samples masked and fewer samples than bins,
+    mixed with ordinary ones, in every request kind: the batch equals the plain per-curve
+    path."""
+    rng = np.random.default_rng(4600)
+    bat = B.RaggedBatch(BLS, TLS, detrend_r=R, fold=B.FoldSpec(nb=256, durations=(0.05, 0.1), dmax=128))
+    ordinary_t = (np.arange(900) * 0.02).astype(np.float32)
+    ordinary_x = (1.0 + rng.normal(0, 1e-3, 900)).astype(np.float32)
+    masked_t = np.full(300, -1000.0, np.float32)
+    for t, x, nf in ((ordinary_t[:1], ordinary_x[:1], 5), (ordinary_t, ordinary_x, 1), (masked_t, ordinary_x[:300], 7),
+                     (ordinary_t[:40], ordinary_x[:40], 33), (ordinary_t, ordinary_x, 61)):
+        bat.add_bls(t, x, nf, 0.05, 0.01, kkmi=1)
+        bat.add_fold(t, x, nf, 0.05, 0.01)
+        bat.add_tls(t, x, 40, 0.3, 0.05, 0.02)
+    bat.build()
+    bat.launch()
+    torch.cuda.synchronize()
+    got = ([bat.bls_result(k) for k in range(bat.n_bls)], [bat.fold_result(k) for k in range(bat.n_fold)],
+           [bat.tls_result(k) for k in range(bat.n_tls)])
+    B.run_plain(bat)
+    torch.cuda.synchronize()
+    want = ([bat.bls_result(k) for k in range(bat.n_bls)], [bat.fold_result(k) for k in range(bat.n_fold)],
+            [bat.tls_result(k) for k in range(bat.n_tls)])
+    for g_kind, w_kind in zip(got, want):
+        for g, w in zip(g_kind, w_kind):
+            for a, b in zip(g, w):
+                np.testing.assert_array_equal(a, b)
+    assert np.all(got[0][2][0] == 0) and np.all(got[1][2][0] == 0)  # all masked: no window
