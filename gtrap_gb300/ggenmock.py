@@ -16,7 +16,7 @@ SEED = 10  # gtrap/ggenmock.py:26
 
 def _gammagen(x, ain, bin_, *, block, grid, shared, stream):
     require_cuda()
-    count = int(grid[0]) * int(grid[1])  # one variate per block, id = blockIdx.x
+    count = int(grid[0])  # one variate per block, id = blockIdx.x (further grid rows repeat the ids)
     nfail = torch.zeros(1, dtype=torch.int32, device="cuda")
     N.call("gtrap_gamma_sample", as_ptr(x), count, float(ain), float(bin_), SEED, 0, as_ptr(nfail),
            stream_handle(stream))
