@@ -77,6 +77,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-plain", action="store_true")
+    p.add_argument("--peaks-only", action="store_true",
+                   help="served workload: requests return only their statistics records (fused epilogue)")
     p.add_argument("--tls-kind", default="gtls", choices=["gtls", "fold"],
                    help="ragged workload: search the TLS-kind curves with GTLS (reference semantics) or "
                         "the folded trapezoid search")
@@ -1269,7 +1271,9 @@ def run_served(args, rank, world, local_rank):
     else:
         pool = [S.Request.from_curve(c) for c in curves]
     fspec = B.FoldSpec(nb=TF_NB, durations=tuple(float(w) for w in TF_DURS), lfrac=TF_LFRAC, dmax=TF_DMAX)
-    srv = S.TransitServer(detrend_r=R_MEDIAN, hbm_budget=100e9, fold=fspec)
+    peaks_only = args.peaks_only
+    srv = S.TransitServer(detrend_r=R_MEDIAN, hbm_budget=100e9, fold=fspec, spectrum_stats=peaks_only,
+                          tls_peaks={} if peaks_only else None)
     for r in pool[:40]:
         srv.submit(r)
     srv.run_until_idle()
@@ -1285,7 +1289,7 @@ def run_served(args, rank, world, local_rank):
     pres = [plain.process(r, t0) for r in pool[:300]]
     psat = S.latency_summary(pres, time.perf_counter() - t0)
     sweep = []
-    for frac in (0.1, 0.5, 0.9) if fold else (0.1, 0.2, 0.3, 0.4, 0.5, 0.6, 0.7, 0.8, 0.9, 1.0, 1.1, 1.2):
+    for frac in (0.1, 0.5, 0.9) if fold or peaks_only else (0.1, 0.2, 0.3, 0.4, 0.5, 0.6, 0.7, 0.8, 0.9, 1.0, 1.1, 1.2):
         rate = frac * sat["req_per_s"]
         m = min(npool, max(200, int(rate * 1.5)))
         offs = S.poisson_trace(m, rate, seed=int(frac * 1000))
@@ -1300,6 +1304,9 @@ def run_served(args, rank, world, local_rank):
                                 "p50_ms": ps["p50_ms"], "p99_ms": ps["p99_ms"]}})
     if rank != 0:
         return
+    # bytes a request returns to the host: full series, or the statistics records
+    ret = [sum(np.asarray(o).nbytes for o in r.outputs) if isinstance(r.outputs, tuple) else np.asarray(r.outputs).nbytes
+           for r in res]
     line = {"metric": METRIC, "value": sat["evals_per_s"], "unit": UNIT, "n_gpus": world,
             "steps": 1, "warmup": 1, "ms_per_step": 1e3 * npool / sat["req_per_s"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64",
@@ -1308,7 +1315,9 @@ def run_served(args, rank, world, local_rank):
                                    "detrended), n log-uniform [1000, 70000], nf 2k-32k, HBM budget 100 GB"
                                    % ("folded-TLS" if fold else "GTLS"),
                        "pool": npool, "depth": srv.depth, "bls_tiles_per_step": srv.bls_tiles,
-                       "tls_tiles_per_step": srv.tls_tiles, "fold_tiles_per_step": srv.fold_tiles},
+                       "tls_tiles_per_step": srv.tls_tiles, "fold_tiles_per_step": srv.fold_tiles,
+                       "returns": "statistics records only (get_blsstat / GTLS peak statistics)" if peaks_only
+                       else "full spectra and S/N series", "mean_bytes_returned_per_request": float(np.mean(ret))},
             "saturation": sat, "plain_saturation": psat, "sweep": sweep,
             "hbm_high_water_bytes": srv.hbm_high_water()}
     print(json.dumps(line), flush=True)

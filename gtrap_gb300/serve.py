@@ -406,6 +406,15 @@ class TransitServer:
                     table[sl * sz:(sl + 1) * sz].copy_(hb[k * sz:(k + 1) * sz], non_blocking=True)
         return devbuf, [base + o for o in offs], nb, nt, nfd
 
+    def _upload_small(self, values, dtype):
+        """A small index array through the step's pinned staging slot (no per-step pinned
+        allocation); the copy runs on the current stream."""
+        arr = np.ascontiguousarray(values, dtype=dtype)
+        hb = self.staging.take(max(arr.nbytes, 8))
+        hb.numpy()[:arr.nbytes] = arr.view(np.uint8)
+        d = hb.to(self.dev, non_blocking=True)
+        return d[:arr.nbytes].view(torch.int64 if arr.dtype == np.int64 else torch.int32)
+
     def _take(self, live, budget):
         segs, counts = [], []
         for lv in live:
@@ -494,8 +503,8 @@ class TransitServer:
             if self.tls_peaks and fin_tls:
                 for j, lv in enumerate(fin_tls):
                     lv.pk_slot = j
-                po = torch.tensor([lv.ooff for lv in fin_tls], dtype=torch.int64).pin_memory().to(self.dev, non_blocking=True)
-                pn = torch.tensor([lv.req.n for lv in fin_tls], dtype=torch.int32).pin_memory().to(self.dev, non_blocking=True)
+                po = self._upload_small([lv.ooff for lv in fin_tls], np.int64)
+                pn = self._upload_small([lv.req.n for lv in fin_tls], np.int32)
                 c = self.tls_peaks
                 pk = api.peakstat(self.o[0], po, pn, 1, max(lv.req.n for lv in fin_tls), c["mpd"],
                                   c["ntop"], c["k"], stream=st)
@@ -508,8 +517,7 @@ class TransitServer:
                         continue
                     for j, lv in enumerate(fin):
                         lv.st_slot = j
-                    sel = torch.tensor([lv.desc for lv in fin], dtype=torch.int32).pin_memory().to(
-                        self.dev, non_blocking=True)
+                    sel = self._upload_small([lv.desc for lv in fin], np.int32)
                     sels.append(sel)
                     bst[kind] = api.blsstat_packed(self.o[0], self.o[1], self.o[2], table, sel, len(fin), stream=st)
             ev = torch.cuda.Event()
