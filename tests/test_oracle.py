@@ -49,6 +49,19 @@ def test_peaks_oracle_matches_reference_option_golden():
     assert seen >= 10
 
 
+def test_tlsfit_restatement_matches_reference_golden():
+    """The restated grid fit picks the reference tlsfit's template, depth, offset and model."""
+    g = np.load(GOLDEN / "tlsfit_golden.npz")
+    for k in range(int(g["ncases"])):
+        with np.errstate(all="ignore"):
+            xpre, H, W, L, T0, off = tls_cpu.tlsfit(g["t_%d" % k], g["x_%d" % k], g["grid_%d_W" % k],
+                                                    g["grid_%d_L" % k], g["grid_%d_T" % k])
+        bH, bW, bL, bT0, boff = g["best_%d" % k]
+        assert (W, L, T0) == (bW, bL, bT0)
+        assert H == pytest.approx(bH, rel=1e-12) and off == pytest.approx(boff, rel=1e-12)
+        np.testing.assert_allclose(xpre, g["xpre_%d" % k], rtol=1e-12, atol=1e-15)
+
+
 # ----------------------------------------------------------------------------- gfilter
 
 def test_medfilt_known_answer():
