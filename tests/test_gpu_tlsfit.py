@@ -93,3 +93,16 @@ def test_tlsfit_all_nan_raises(cuda):
     x = np.full(50, np.nan)
     with pytest.raises(ValueError):
         tls.tlsfit(t, x, [1.0], [0.1], [5.0])
+
+
+def test_tlsfit_reference_golden(cuda):
+    """The device grid fit picks the reference tlsfit's template (golden vectors made by the
+    reference's own tls.py), with its depth, offset and model."""
+    g = np.load(GOLDEN / "tlsfit_golden.npz")
+    for k in range(int(g["ncases"])):
+        xpre, H, W, L, T0, off = tls.tlsfit(g["t_%d" % k], g["x_%d" % k], g["grid_%d_W" % k], g["grid_%d_L" % k],
+                                            g["grid_%d_T" % k])
+        bH, bW, bL, bT0, boff = g["best_%d" % k]
+        assert (W, L, T0) == (bW, bL, bT0), k
+        assert H == pytest.approx(bH, rel=1e-9) and off == pytest.approx(boff, rel=1e-12)
+        np.testing.assert_allclose(xpre, g["xpre_%d" % k], rtol=1e-9, atol=1e-12)
