@@ -189,3 +189,30 @@ def test_transit_params_record_matches_the_header(tmp_path):
     got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
     assert got[:-1] == [api.TRANSIT_PARAMS.fields[f][1] for f in fields]
     assert got[-1] == api.TRANSIT_PARAMS.itemsize == 88
+
+
+def test_c_host_links_and_calls(tmp_path):
+    """A C99 host (no C++, no Python) links libgtrap_gb300.so and calls it: the version, a
+    grid query and a validation error with its text (all host-side: no GPU needed)."""
+    import shutil
+    import subprocess
+    from gtrap_gb300 import _build
+    cc = shutil.which("gcc") or shutil.which("cc")
+    lib = _build.library_path()
+    if cc is None or not lib.exists():
+        pytest.skip("no C compiler or library")
+    src = tmp_path / "host.c"
+    src.write_text("\n".join([
+        '#include <stdio.h>', '#include <string.h>', '#include "gtrap_gb300.h"',
+        "int main(void) {",
+        "  if (gtrap_version() <= 0) return 1;",
+        "  if (gtrap_tls_fold_item_frequencies(100, 50) != 0) return 2;",
+        "  if (gtrap_detect_peaks(0, 10, 0, 0.0, 1, 0.0, 1, 0, 0, 0, 0, 0, 0) != GTRAP_ERR_INVALID_ARG) return 3;",
+        '  if (strstr(gtrap_last_error(), "detect_peaks") == 0) return 4;',
+        '  printf("ok %d\\n", gtrap_version());',
+        "  return 0; }"]))
+    exe = tmp_path / "host"
+    subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-I", str(ROOT / "include"), str(src), "-o", str(exe),
+                    "-L", str(lib.parent), "-lgtrap_gb300", "-Wl,-rpath," + str(lib.parent)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0 and out.stdout.startswith("ok"), (out.returncode, out.stdout, out.stderr)
