@@ -10,7 +10,7 @@ import torch
 
 from oracle import mock as OM
 from oracle import picktrap as OP
-from gtrap_gb300 import api, genmock, ggenmock, mock, picktrap
+from gtrap_gb300 import genmock, ggenmock, mock, picktrap
 
 pytestmark = pytest.mark.gpu
 

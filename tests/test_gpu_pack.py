@@ -2,7 +2,6 @@
 bit-identical images and packed arrays, valid counts, and the out-of-range status."""
 import numpy as np
 import pytest
-import torch
 
 from oracle import packer
 from gtrap_gb300 import pack
