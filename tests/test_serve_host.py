@@ -57,3 +57,16 @@ def test_runs_and_trace():
     tr = poisson_trace(20000, rate=500.0, seed=1)
     assert np.all(np.diff(tr) > 0)
     assert abs(tr[-1] / 20000 - 1 / 500.0) < 0.05 / 500.0 * 10
+
+
+def test_request_outputs_per_kind():
+    from gtrap_gb300 import serve as S, synth
+    t = np.arange(500, dtype=np.float32)
+    x = np.ones(500, np.float32)
+    assert S.Request("bls", t, x, nf=64).outputs == 64
+    assert S.Request("fold", t, x, nf=33).outputs == 33
+    assert S.Request("tls", t, x, nsc=40).outputs == 500      # one output per epoch (sample)
+    for c in synth.ragged_mix(6, seed=4000):
+        r = S.Request.from_curve(c)
+        assert r.kind == c["kind"] and r.n == c["x"].size
+        assert r.outputs == (c["nf"] if c["kind"] == "bls" else c["x"].size)
