@@ -129,50 +129,20 @@ def _profile(name):
 
 def smem_atomic_peak(dev):
     """Shared-memory atomic peak in fold updates per second (two 32-bit adds per update)."""
-    import torch
-    from gtrap_gb300 import api
-    stream = torch.cuda.current_stream(dev)
-    _, upd = api.smem_atomic_peak_probe()
-    torch.cuda.synchronize(dev)
-    ps, pe = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ps.record(stream)
-    for _ in range(3):
-        api.smem_atomic_peak_probe()
-    pe.record(stream)
-    torch.cuda.synchronize(dev)
-    return upd * 3 / (ps.elapsed_time(pe) / 1e3)
+    import bench_probes
+    return bench_probes.smem_atomic_updates(dev)
 
 
 def smem_load_peak(dev):
     """Shared-memory load bandwidth of this GPU in bytes/s (conflict-free 64-bit loads)."""
-    import torch
-    from gtrap_gb300 import api
-    stream = torch.cuda.current_stream(dev)
-    _, nbytes = api.smem_load_peak_probe()
-    torch.cuda.synchronize(dev)
-    ps, pe = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ps.record(stream)
-    for _ in range(3):
-        api.smem_load_peak_probe()
-    pe.record(stream)
-    torch.cuda.synchronize(dev)
-    return nbytes * 3 / (ps.elapsed_time(pe) / 1e3)
+    import bench_probes
+    return bench_probes.smem_load_bytes(dev)
 
 
 def fp32_peak_tflops(dev):
     """FP32 FMA issue peak of this GPU, measured live (MEASURED_PEAKS.json has no FP32 figure)."""
-    import torch
-    from gtrap_gb300 import api
-    stream = torch.cuda.current_stream(dev)
-    _, flops = api.fp32_peak_probe(iters=4096)
-    torch.cuda.synchronize(dev)
-    ps, pe = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ps.record(stream)
-    for _ in range(3):
-        api.fp32_peak_probe(iters=4096)
-    pe.record(stream)
-    torch.cuda.synchronize(dev)
-    return flops * 3 / (ps.elapsed_time(pe) / 1e3) / 1e12
+    import bench_probes
+    return bench_probes.fp32_tflops(dev)
 
 
 # ----------------------------------------------------------------------------- clocks
@@ -1395,18 +1365,8 @@ def fit_sampled_parity(t, x, tl, H, res):
 
 def fp64_peak_tflops(dev):
     """FP64 FMA issue peak of this GPU, measured live (MEASURED_PEAKS.json has no FP64 figure)."""
-    import torch
-    from gtrap_gb300 import api
-    stream = torch.cuda.current_stream(dev)
-    _, flops = api.fp64_peak_probe(iters=256)
-    torch.cuda.synchronize(dev)
-    ps, pe = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ps.record(stream)
-    for _ in range(3):
-        api.fp64_peak_probe(iters=256)
-    pe.record(stream)
-    torch.cuda.synchronize(dev)
-    return flops * 3 / (ps.elapsed_time(pe) / 1e3) / 1e12
+    import bench_probes
+    return bench_probes.fp64_tflops(dev)
 
 
 def run_tlsfit(args, rank, world, local_rank):

@@ -64,16 +64,12 @@ def _run(cmd):
     return res
 
 
-def build(force: bool = False, verbose: bool = False, extra_flags=(), lib: Path | None = None) -> Path:
-    """Compile (if needed) and return the path of the shared library.
-
-    ``extra_flags`` (e.g. ``-DGTRAP_BLS_MINB=1``) and ``lib`` build a variant library
-    elsewhere, for tuning experiments; the default build has neither."""
-    variant = lib is not None
-    lib = Path(lib) if variant else library_path()
+def build(force: bool = False, verbose: bool = False) -> Path:
+    """Compile (if needed) and return the path of the shared library."""
+    lib = library_path()
     if not force and _up_to_date(lib):
         return lib
-    objdir = BUILD / ("variant_" + lib.stem if variant else "default")
+    objdir = BUILD / "default"
     objdir.mkdir(parents=True, exist_ok=True)
     lib.parent.mkdir(parents=True, exist_ok=True)
     cc = nvcc()
@@ -82,7 +78,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags=(), lib: Path 
     for src in _sources():
         obj = objdir / (src.stem + ".o")
         objs.append(obj)
-        jobs.append([cc, *ARCH, *NVCC_FLAGS, *FILE_FLAGS.get(src.name, []), *extra_flags, "-I",
+        jobs.append([cc, *ARCH, *NVCC_FLAGS, *FILE_FLAGS.get(src.name, []), "-I",
                      str(INCLUDE), "-c", str(src), "-o", str(obj)])
     workers = max(1, min(len(jobs), os.cpu_count() or 4))
     with cf.ThreadPoolExecutor(workers) as ex:

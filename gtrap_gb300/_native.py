@@ -6,9 +6,7 @@ library is missing or cannot be loaded, every call raises ``GtrapError``.
 from __future__ import annotations
 
 import ctypes as C
-import os
 import threading
-from pathlib import Path
 
 from . import _build
 
@@ -76,10 +74,6 @@ _SIGNATURES = {
                                  vp, vp, vp]),
     "gtrap_peakstat_max_samples": (sz, []),
     "gtrap_peakstat": (C.c_int, [vp, vp, vp, u64, u32, u32, u32, u32, u32, vp, vp, vp, vp]),
-    "gtrap_probe_fp32_peak": (C.c_int, [vp, u32, C.POINTER(C.c_double), vp]),
-    "gtrap_probe_fp64_peak": (C.c_int, [vp, u32, C.POINTER(C.c_double), vp]),
-    "gtrap_probe_smem_atomic_peak": (C.c_int, [vp, u32, C.POINTER(C.c_double), vp]),
-    "gtrap_probe_smem_load_peak": (C.c_int, [vp, u32, C.POINTER(C.c_double), vp]),
     "gtrap_transit_flux": (C.c_int, [vp, vp, u32, vp, vp]),
     "gtrap_trend": (C.c_int, [vp, vp, u32, f64, f64, f64, i32, vp]),
     "gtrap_inject_transit": (C.c_int, [vp, vp, vp, vp, C.c_uint64, u32, u32, vp, C.c_int32, vp]),
@@ -107,8 +101,7 @@ def load(build_if_missing: bool = False):
     with _lock:
         if _lib is not None:
             return _lib
-        override = os.environ.get("GTRAP_GB300_LIB")  # a tuning variant built by _build.build
-        path = Path(override) if override else _build.library_path()
+        path = _build.library_path()
         if not path.exists():
             if build_if_missing:
                 _build.build()

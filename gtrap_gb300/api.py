@@ -225,38 +225,6 @@ def gtls(lc, tu, nt, nw, nl, nsc, wmax, dw, deltat, *, mode=0, t0min=0.0, dt=0.0
     return out
 
 
-def smem_atomic_peak_probe(iters=2048, stream=None):
-    """Launch the shared-memory atomic probe; returns (sink tensor, update count)."""
-    sink = torch.empty(1 << 16, dtype=torch.int32, device="cuda")
-    upd = C.c_double(0.0)
-    N.call("gtrap_probe_smem_atomic_peak", as_ptr(sink), int(iters), C.byref(upd), stream_handle(stream))
-    return sink, upd.value
-
-
-def smem_load_peak_probe(iters=4096, stream=None):
-    """Launch the shared-memory load probe; returns (sink tensor, bytes read)."""
-    sink = torch.empty(1 << 16, dtype=torch.int64, device="cuda")
-    nbytes = C.c_double(0.0)
-    N.call("gtrap_probe_smem_load_peak", as_ptr(sink), int(iters), C.byref(nbytes), stream_handle(stream))
-    return sink, nbytes.value
-
-
-def fp32_peak_probe(iters=4096, stream=None):
-    """Launch the FP32 FMA probe; returns (sink tensor, flop count)."""
-    sink = torch.empty(1 << 20, dtype=torch.float32, device="cuda")
-    flops = C.c_double(0.0)
-    N.call("gtrap_probe_fp32_peak", as_ptr(sink), int(iters), C.byref(flops), stream_handle(stream))
-    return sink, flops.value
-
-
-def fp64_peak_probe(iters=1024, stream=None):
-    """Launch the FP64 FMA probe; returns (sink tensor, flop count)."""
-    sink = torch.empty(1 << 20, dtype=torch.float64, device="cuda")
-    flops = C.c_double(0.0)
-    N.call("gtrap_probe_fp64_peak", as_ptr(sink), int(iters), C.byref(flops), stream_handle(stream))
-    return sink, flops.value
-
-
 # Record layout of gtrap_peak_stats (include/gtrap_gb300.h).
 
 PEAK_STATS = _np.dtype([("maxsn", "<f4"), ("argmax", "<u4"), ("lent", "<u4"), ("npeaks", "<u4"),

@@ -29,12 +29,11 @@
 #include "common.cuh"
 
 #include <climits>
-#include <mutex>
 
 // Fixed scratch for gtrap_geebls_noalloc.  A file-scope device array: every GPU that
 // loads this library holds it until the process exits.  Host code must not use the
 // symbol's name as an address (it names a host-side stand-in); the device address is
-// looked up per device with cudaGetSymbolAddress.
+// looked up with cudaGetSymbolAddress in the calling thread's current context.
 constexpr size_t kNoallocScratchBytes = size_t(64) << 20;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
 
@@ -43,9 +42,7 @@ namespace {
 using gtrap::fail;
 
 constexpr int kThreads = 512;
-#ifndef GTRAP_BLS_MINB
-#define GTRAP_BLS_MINB 2  // resident blocks per SM the R = 8 scan is compiled for
-#endif
+constexpr int kMinBlocks = 2;  // resident blocks per SM the R = 8 scan is compiled for
 constexpr int kMaxNb = 8192;
 constexpr int32_t kMasked = INT32_MIN;
 // Largest bin count for which the 32-bit fold format is exact (see the fold).
@@ -892,7 +889,7 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
 
 // Plain launch: one block per (curve, tile) of an [n, nq] image batch.
 template <int R, int MODE>
-__global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1)
+__global__ void __launch_bounds__(kThreads, R == 8 ? kMinBlocks : 1)
 bls_fold_scan_kernel(const BlsShape sh, const BlsArgs a) {
   // the tile descriptor lives in shared memory: read where used, not held in registers
   __shared__ BlsTile t;
@@ -937,7 +934,7 @@ struct BlsQueue {
 };
 
 template <int R, int MODE>
-__global__ void __launch_bounds__(kThreads, R == 8 ? GTRAP_BLS_MINB : 1)
+__global__ void __launch_bounds__(kThreads, R == 8 ? kMinBlocks : 1)
 bls_queue_kernel(const BlsShape sh, const BlsQueue qa) {
   __shared__ uint32_t item_s;
   __shared__ BlsTile t;  // descriptor of the current tile (see bls_fold_scan_kernel)
@@ -1013,8 +1010,6 @@ int make_plan(uint32_t nb, uint32_t kma, uint32_t nf, uint32_t F_req, Plan *p) {
   if (F > 64) F = 64;
   F = F / G * G;
   if (F == 0) F = G;
-  const char *env = getenv("GTRAP_BLS_F");
-  if (env && atoi(env) > 0) F = (uint32_t)atoi(env);
   if (F_req) F = F_req;
   if (F > 64) return fail(GTRAP_ERR_INVALID_ARG, "geebls: at most 64 frequencies per block (F=%u)", F);
   if (nf && F > nf) F = nf;
@@ -1140,26 +1135,16 @@ int run_bls(bool full, float *blsp, uint32_t *phase1, uint32_t *phase2, const fl
   return gtrap::check_launch("bls_fold_scan_kernel");
 }
 
-constexpr int kMaxDevices = 64;
-std::mutex g_noalloc_mutex;
-void *g_noalloc_ptr[kMaxDevices];  // device address of g_noalloc_scratch, per device
-
-// Device address of the fixed scratch on the current device.  The first call on a device
-// looks it up (cudaGetSymbolAddress with that device current) and caches it.
+// Device address of the fixed scratch in the calling thread's current context.  It is looked
+// up on every call (cheap once the module is loaded) rather than cached: a device reset or a
+// non-primary driver context loads the module again, possibly at another address, and a
+// cached address would then point at nothing of this library's.
 int noalloc_scratch(void **out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return fail(GTRAP_ERR_CUDA, "geebls_noalloc: cudaGetDevice: %s", cudaGetErrorString(e));
-  if (dev < 0 || dev >= kMaxDevices) return fail(GTRAP_ERR_UNSUPPORTED, "geebls_noalloc: device %d out of range", dev);
-  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (!g_noalloc_ptr[dev]) {
-    void *p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p)
-      return fail(GTRAP_ERR_CUDA, "geebls_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
-    g_noalloc_ptr[dev] = p;
-  }
-  *out = g_noalloc_ptr[dev];
+  void *p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p)
+    return fail(GTRAP_ERR_CUDA, "geebls_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+  *out = p;
   return GTRAP_OK;
 }
 

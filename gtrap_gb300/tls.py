@@ -7,9 +7,9 @@ Same names, arguments and return values as the reference's NumPy functions:
 * :func:`get_chi2Hmax` (``:44-79``): depth, chi^2, sample count and window mean,
 * :func:`tlsfit` (``:82-110``): the brute-force grid fit over widths x ingress x epochs,
 
-computed in FP64 by ``gtrap_tlsfit_grid`` / ``gtrap_gen_trapezoid`` (one warp per template over
-the template's window of the time-sorted series, instead of ~15 full-series mask passes per
-template).  :func:`chi2_grid` returns the whole grid as device tensors.  The reference's
+computed in FP64 by ``gtrap_tlsfit_grid`` / ``gtrap_gen_trapezoid`` (one thread per template,
+summing index ranges of the time-sorted series found by binary search, instead of ~15
+full-series mask passes per template).  :func:`chi2_grid` returns the whole grid as device tensors.  The reference's
 ``tlsfit`` prints the winning index; this one does not.
 """
 from __future__ import annotations

@@ -99,10 +99,13 @@ int gtrap_geebls(float *blsp, uint32_t *phase1, uint32_t *phase2, const float *l
  * gtrap_geebls_noalloc_max_scratch() bytes (64 MiB) compiled into the library, which every
  * GPU that loads the library holds until exit.  Batches needing more scratch than that
  * (gtrap_geebls_workspace_size(n, nq, flags) bytes) are rejected with
- * GTRAP_ERR_INVALID_ARG.  The first call on a device looks up the array's device address
- * and should come before any stream capture.  All calls share the one array and every call
- * rewrites what it reads, so calls that overlap on the GPU (different streams, threads or
- * processes sharing the context) race and must be serialised by the caller. */
+ * GTRAP_ERR_INVALID_ARG.  Every call looks up the array's device address
+ * (cudaGetSymbolAddress) in the calling thread's current context, so an address is only
+ * used in the context that looked it up (a device reset or another driver context gets its
+ * own copy of the array); the first call on a device loads the module there and should come
+ * before any stream capture.  All calls share the one array and every call rewrites what it
+ * reads, so calls that overlap on the GPU (different streams, threads or processes sharing
+ * the context) race and must be serialised by the caller. */
 size_t gtrap_geebls_noalloc_max_scratch(void);
 int gtrap_geebls_noalloc(float *blsp, uint32_t *phase1, uint32_t *phase2, const float *lc,
                          const float *tu, const float *offset, const uint32_t *ntrue, uint32_t n,
@@ -385,19 +388,6 @@ int gtrap_peakstat(const float *sn, const uint64_t *off, const uint32_t *n, uint
                    gtrap_peak_stats *stats, uint32_t *peak_idx, float *peak_val,
                    gtrap_stream_t stream);
 
-/* ---------------------------------------------------------------------------
- * Measurement helpers (used by the benchmark to report roofline fractions).
- * ------------------------------------------------------------------------- */
-/* FP32 issue peak: launches a register-resident FMA-chain kernel; *flops receives the
- * number of FP32 floating-point operations it performs (an FMA counts as 2). */
-int gtrap_probe_fp32_peak(float *sink, uint32_t iters, double *flops, gtrap_stream_t stream);
-/* The same FMA-chain probe in FP64 (eight double chains a thread); sink holds
- * sm_count*8*256 doubles. */
-int gtrap_probe_fp64_peak(double *sink, uint32_t iters, double *flops, gtrap_stream_t stream);
-/* Shared-memory atomic peak for the BLS fold's pattern: *updates receives the number of
- * (two 32-bit atomic adds to random bins) updates the launch performs. */
-int gtrap_probe_smem_atomic_peak(unsigned *sink, uint32_t iters, double *updates, gtrap_stream_t stream);
-
 /* ---- mock injection (gtrap/genmock.py:9-43, gtrap/ggenmock.py:18-79) ------------------ */
 
 /* One transit model: batman's quadratic limb-darkening transit (Kreidberg 2015) with the
@@ -440,10 +430,6 @@ int gtrap_inject_transit(float *lc, const float *tu, const uint64_t *off, const 
  * counter, optional). */
 int gtrap_gamma_sample(float *x, uint32_t count, float alpha, float beta, uint64_t seed, uint64_t first_id,
                        uint32_t *nfail, gtrap_stream_t stream);
-
-/* Shared-memory load bandwidth (conflict-free 64-bit loads): *bytes receives the bytes the
- * launch reads.  sink: at least 2 * SM-count words. */
-int gtrap_probe_smem_load_peak(unsigned long long *sink, uint32_t iters, double *bytes, gtrap_stream_t stream);
 
 #ifdef __cplusplus
 }

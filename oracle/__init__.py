@@ -12,7 +12,8 @@ path (``gtrap_gb300``) never imports this package.
 * gtrap/tls.py (the reference's own CPU TLS math): NumPy restatement in ``tls_cpu.py``.
 
 Pinning: the restatements are checked against the golden vectors committed under
-``tests/golden/`` (see ``tests/golden/README.md`` for their provenance).
+``tests/golden/``; each fixture's provenance is the docstring of the ``make_*_golden.py``
+script beside it that generated it.
 """
 from __future__ import annotations
 

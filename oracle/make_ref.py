@@ -12,7 +12,7 @@ never committed).  ``build()`` compiles it with ``nvcc -use_fast_math`` for sm_1
 ``oracle/_ref/libgtrap_ref.so`` wherever nvcc exists (the generated source travels to a
 GPU host; the reference checkout does not need to).
 
-Usage: ``python -m oracle.make_ref [--reference PATH]``.
+Usage: ``python -m oracle.make_ref [--reference PATH]`` (or ``GTRAP_REFERENCE=PATH``).
 """
 from __future__ import annotations
 
@@ -27,7 +27,16 @@ HERE = Path(__file__).resolve().parent
 REF_DIR = HERE / "_ref"
 GEN = REF_DIR / "ref_kernels.cu"
 LIB = REF_DIR / "libgtrap_ref.so"
+# where this recipe looks for the reference checkout unless told otherwise
 DEFAULT_REFERENCE = Path("/root/reference")
+
+
+def reference_dir(path=None):
+    """The reference checkout: ``path`` if given, else ``$GTRAP_REFERENCE``, else this recipe's
+    default location.  Returns None when the directory does not exist (a GPU host has only the
+    generated source)."""
+    cand = Path(path or os.environ.get("GTRAP_REFERENCE") or DEFAULT_REFERENCE)
+    return cand if cand.is_dir() else None
 
 
 def _source_module_strings(pyfile: Path):
@@ -93,8 +102,10 @@ int ref_getmax(float *blsp, unsigned *p1, unsigned *p2, float *maxval, unsigned 
 '''
 
 
-def generate(reference: Path = DEFAULT_REFERENCE) -> Path:
-    reference = Path(reference)
+def generate(reference=None) -> Path:
+    reference = reference_dir(reference)
+    if reference is None:
+        raise FileNotFoundError("reference checkout not found (give a path or set GTRAP_REFERENCE)")
     inc = reference / "include"
     simple = _source_module_strings(reference / "gtrap" / "geebls_simple.py")[0]
     gfil = _source_module_strings(reference / "gtrap" / "gfilter.py")[0]
@@ -164,7 +175,7 @@ def build(force: bool = False) -> Path | None:
 
 
 if __name__ == "__main__":
-    ref = DEFAULT_REFERENCE
+    ref = None
     if "--reference" in sys.argv:
         ref = Path(sys.argv[sys.argv.index("--reference") + 1])
     print(generate(ref))

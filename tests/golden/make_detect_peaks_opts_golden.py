@@ -5,7 +5,7 @@ values, plateaus, NaNs and infinities.  Cases whose result depends on the order 
 heights (mpd > 1 without kpsh and two equal candidate heights within mpd: the reference's
 unstable argsort decides them) are left out.
 
-    python tests/golden/make_detect_peaks_opts_golden.py /root/reference
+    python tests/golden/make_detect_peaks_opts_golden.py /path/to/reference
 """
 import importlib.util
 import itertools
@@ -13,6 +13,8 @@ import sys
 from pathlib import Path
 
 import numpy as np
+
+from _refpath import reference_dir
 
 EDGES = {None: 0, "rising": 1, "falling": 2, "both": 3}
 
@@ -85,4 +87,4 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    main(reference_dir())

@@ -2,7 +2,7 @@
 (gtrap/read_keplerlc.py:123-146), taken from the reference checkout by parsing the file and
 compiling only that function (the module itself imports astropy, absent here), followed by
 the zig-zag fill and ntrue of load_keplc (:36-47) on seeded synthetic cadence series.
-Run from the repository root:  python tests/golden/make_packer_golden.py
+Run from the repository root:  python tests/golden/make_packer_golden.py /path/to/reference
 """
 import ast
 import sys
@@ -10,7 +10,9 @@ from pathlib import Path
 
 import numpy as np
 
-REF = Path("/root/reference/gtrap/read_keplerlc.py")
+from _refpath import reference_dir
+
+REF = reference_dir() / "gtrap" / "read_keplerlc.py"
 OUT = Path(__file__).resolve().parent / "packer_golden.npz"
 
 

@@ -2,7 +2,7 @@
 
 Loads gtrap/detect_peaks.py (pure NumPy) from the reference checkout by path and runs it,
 and the statistics of gtrap/gtls.py:245-273 written with the same NumPy calls, on seeded
-series.  Run from the repository root:  python tests/golden/make_peaks_golden.py
+series.  Run from the repository root:  python tests/golden/make_peaks_golden.py /path/to/reference
 """
 import importlib.util
 import sys
@@ -10,7 +10,9 @@ from pathlib import Path
 
 import numpy as np
 
-REF = Path("/root/reference/gtrap/detect_peaks.py")
+from _refpath import reference_dir
+
+REF = reference_dir() / "gtrap" / "detect_peaks.py"
 OUT = Path(__file__).resolve().parent / "detect_peaks_golden.npz"
 
 

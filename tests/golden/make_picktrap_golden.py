@@ -2,7 +2,7 @@
 (gtrap/picktrap.py:27-172), taken from the reference checkout by parsing the file and
 compiling only that function (the module imports astropy and matplotlib, absent here), on
 seeded light curves with gaps and candidates near gaps and edges.
-Run from the repository root:  python tests/golden/make_picktrap_golden.py
+Run from the repository root:  python tests/golden/make_picktrap_golden.py /path/to/reference
 """
 import ast
 import os
@@ -10,9 +10,11 @@ import sys
 from pathlib import Path
 
 import numpy as np
+
+from _refpath import reference_dir
 from scipy import interpolate
 
-REF = Path("/root/reference/gtrap/picktrap.py")
+REF = reference_dir() / "gtrap" / "picktrap.py"
 OUT = Path(__file__).resolve().parent / "picktrap_golden.npz"
 
 

@@ -5,7 +5,7 @@ gen_trapzoid, get_Hmax and get_chi2Hmax on seeded cases, including the module's 
 self-check (gtrap/tls.py:113-122: noiseless trapezoid, H=-3, W=30, L=5, t0=50 on
 t = linspace(0, 100, 132)).
 
-Usage: python tests/golden/make_tls_golden.py [/path/to/reference]
+Usage: python tests/golden/make_tls_golden.py /path/to/reference (or GTRAP_REFERENCE=...)
 """
 import importlib.util
 import sys
@@ -13,7 +13,9 @@ from pathlib import Path
 
 import numpy as np
 
-ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+from _refpath import reference_dir
+
+ref = reference_dir()
 spec = importlib.util.spec_from_file_location("ref_tls", ref / "gtrap" / "tls.py")
 tls = importlib.util.module_from_spec(spec)
 spec.loader.exec_module(tls)

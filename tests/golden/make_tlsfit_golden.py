@@ -2,7 +2,7 @@
 (gtrap/tls.py:82-110, pure NumPy): seeded noisy trapezoids, some with NaN flux, over small
 (W, L, t0) grids; records the winning template, its depth and offset, and the model.
 
-Usage: python tests/golden/make_tlsfit_golden.py [/path/to/reference]
+Usage: python tests/golden/make_tlsfit_golden.py /path/to/reference (or GTRAP_REFERENCE=...)
 """
 import contextlib
 import importlib.util
@@ -12,7 +12,9 @@ from pathlib import Path
 
 import numpy as np
 
-ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+from _refpath import reference_dir
+
+ref = reference_dir()
 spec = importlib.util.spec_from_file_location("ref_tls", ref / "gtrap" / "tls.py")
 tls = importlib.util.module_from_spec(spec)
 spec.loader.exec_module(tls)

@@ -52,3 +52,15 @@ def test_parse_defaults(monkeypatch):
     a = bench.parse()
     assert (a.gpus, a.workload, a.impl, a.tls_kind, a.peaks_only) == (1, "ragged", "ours", "gtls", False)
     assert a.warmup >= 3
+
+
+def test_probe_library_is_separate_and_validates_on_the_host():
+    """The roofline probes live in the benchmark's own library, not in the product ABI."""
+    import ctypes as C
+    import bench_probes
+    from gtrap_gb300 import _native
+    lib = bench_probes.load()
+    for name in ("bench_probe_fp32", "bench_probe_fp64", "bench_probe_smem_atomic", "bench_probe_smem_load"):
+        assert getattr(lib, name)(None, 10, None, None) == -1
+        assert not any("probe" in s for s in _native.exported_symbols())
+    assert lib.bench_probe_fp32(C.c_void_p(0), 0, None, None) == -1

@@ -1,5 +1,8 @@
 """The C-ABI library loads and exports every entry point declared in include/*.h.
-Only argument-validation paths run here (they return before any CUDA call)."""
+Only argument-validation paths run here (they return before any CUDA call).  Tests that
+pass made-up device addresses to reach a check behind the null-pointer checks run only
+where no CUDA device is visible, so a regression in the order of the checks can never
+launch a kernel on such an address."""
 import ctypes as C
 import re
 from pathlib import Path
@@ -17,6 +20,13 @@ def _declared():
         src = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
         names |= set(re.findall(r"\b(gtrap_[a-z0-9_]+)\s*\(", src))
     return names
+
+
+@pytest.fixture
+def no_device():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("passes made-up device addresses: host-only test")
 
 
 @pytest.fixture(scope="module")
@@ -39,7 +49,7 @@ def test_version_and_error_text(lib):
     assert isinstance(lib.gtrap_last_error(), bytes)
 
 
-def test_validation_errors_need_no_gpu(lib):
+def test_validation_errors_need_no_gpu(lib, no_device):
     st = lib.gtrap_gfilter(None, None, 10, 10, 2, None)
     assert st == _native.ERR_INVALID_ARG
     assert b"null" in lib.gtrap_last_error()
@@ -59,7 +69,7 @@ def test_workspace_sizes_are_host_side(lib):
     assert lib.gtrap_geebls_simple_workspace_size(4096, 64, 0) >= 64 * 4096 * 4 + 4096 * 16
 
 
-def test_missing_workspace_is_an_error(lib):
+def test_missing_workspace_is_an_error(lib, no_device):
     st = lib.gtrap_geebls_simple(C.c_void_p(256), None, None, C.c_void_p(256), C.c_void_p(256), 100, 2,
                                  10, 64, 10, 1, 5, 0.1, 0.01, 0, 0, None, 0, None)
     assert st == _native.ERR_WORKSPACE
@@ -95,7 +105,7 @@ def test_packed_struct_layouts_match_the_header(tmp_path):
             assert got[(st, f)] == dt.fields[f][1], (st, f)
 
 
-def test_new_entry_points_validate_on_the_host(lib):
+def test_new_entry_points_validate_on_the_host(lib, no_device):
     import numpy as np
     from gtrap_gb300 import api
     P = C.c_void_p(16)
@@ -147,7 +157,6 @@ def test_new_entry_points_validate_on_the_host(lib):
     assert lib.gtrap_nanargmax(None, 3, P, None) == _native.ERR_INVALID_ARG
     assert lib.gtrap_gen_trapezoid(P, P, 0, 1.0, 1.0, 0.1, 0.0, 0.0, None) == 0  # nothing to do
     assert lib.gtrap_gen_trapezoid(None, P, 5, 1.0, 1.0, 0.1, 0.0, 0.0, None) == _native.ERR_INVALID_ARG
-    assert lib.gtrap_probe_fp64_peak(None, 10, None, None) == _native.ERR_INVALID_ARG
     assert lib.gtrap_detect_peaks(P, 10, 0, 0.0, 1, 0.0, 1, 0, 0, P, P, None, None) == _native.ERR_INVALID_ARG
     assert lib.gtrap_detect_peaks(P, 10, 0, 0.0, 1, 0.0, 7, 0, 0, P, P, P, None) == _native.ERR_INVALID_ARG
     assert b"edge" in lib.gtrap_last_error()
@@ -167,7 +176,6 @@ def test_new_entry_points_validate_on_the_host(lib):
     assert lib.gtrap_inject_transit(None, P, P, P, 1, 2, 10, P, 0, None) == _native.ERR_INVALID_ARG
     assert lib.gtrap_gamma_sample(P, 10, 0.0, 1.0, 10, 0, None, None) == _native.ERR_INVALID_ARG
     assert lib.gtrap_gamma_sample(None, 10, 1.0, 1.0, 10, 0, None, None) == _native.ERR_INVALID_ARG
-    assert lib.gtrap_probe_smem_load_peak(None, 10, None, None) == _native.ERR_INVALID_ARG
 
 
 def test_transit_params_record_matches_the_header(tmp_path):
