@@ -71,12 +71,14 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="ragged",
-                   choices=["ragged", "masked", "served", "plain", "tls", "tlsfold", "mock", "tlsfit"])
+                   choices=["ragged", "masked", "served", "plain", "tls", "tlsfold", "mock", "tlsfit", "epilogue"])
     p.add_argument("--nq", type=int, default=None,
                    help="curves per GPU (default: 10,000 ragged, 1024 masked)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-plain", action="store_true")
+    p.add_argument("--no-parity", action="store_true", help="ragged workload: skip the oracle sample")
+    p.add_argument("--no-served", action="store_true", help="ragged workload: skip the served block")
     p.add_argument("--peaks-only", action="store_true",
                    help="served workload: requests return only their statistics records (fused epilogue)")
     p.add_argument("--tls-kind", default="gtls", choices=["gtls", "fold"],
@@ -541,6 +543,143 @@ def run_ragged_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def per_kind(bat, stage_ms, ms):
+    """Evaluations per second of each search kind over its own stage of the step (CUDA events
+    between the stage replays), and the prep stage's share."""
+    out = {"prep_ms": stage_ms.get("prep"), "step_ms": ms}
+    if bat.n_bls:
+        out["bls"] = {"unit": "(curve, frequency) evals/s", "evals": bat.bls_evals, "stage_ms": stage_ms["bls"],
+                      "value": bat.bls_evals / (stage_ms["bls"] / 1e3)}
+    if bat.n_fold:
+        out["fold"] = {"unit": "(curve, frequency) evals/s", "evals": bat.fold_evals, "stage_ms": stage_ms["fold"],
+                       "value": bat.fold_evals / (stage_ms["fold"] / 1e3)}
+    if bat.n_tls:
+        out["gtls"] = {"unit": "(curve, epoch) evals/s", "evals": bat.tls_evals, "stage_ms": stage_ms["tls"],
+                       "value": bat.tls_evals / (stage_ms["tls"] / 1e3)}
+    return out
+
+
+def ragged_parity(mix, bat, n_curves=16, fstride=8):
+    """The headline run's outputs against the FP64 oracle on a sample of its full-length
+    curves: ``n_curves`` BLS requests spread over the batch at every ``fstride``-th frequency
+    and ``n_curves`` GTLS requests at every epoch (each from the raw curve through scipy's
+    median filter; the BLS offset is the device's get_offset, itself checked against FP64).
+    Tolerances: SR relative error <= 1e-4; best bins identical or tie-equivalent (the
+    oracle's power of the GPU's window within 1e-5 of the maximum); GTLS S/N within 1e-4
+    (relative, absolute below 1)."""
+    import oracle
+    from gtrap_gb300 import batch as B
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    bls_curves = [c for c in mix if c["kind"] == "bls"]
+    tls_curves = [c for c in mix if c["kind"] == "tls"]
+    dev_table = np.frombuffer(bat.bls_curves.cpu().numpy().tobytes(), B.BLS_CURVE)
+    out = {"tolerance": "SR rel err <= 1e-4 vs FP64, best bins identical or tie-equivalent (FP64 power "
+                        "within 1e-5 of the maximum); GTLS S/N rel err <= 1e-4 (absolute below 1)"}
+    if bat.n_bls:
+        ks = sorted(set(np.linspace(0, bat.n_bls - 1, min(n_curves, bat.n_bls)).astype(int).tolist()))
+        err = off_err = 0.0
+        evals = same = ties = bad = best_same = best_tie = best_bad = 0
+        for k in ks:
+            c, row = bls_curves[k], bat.bls_table[k]
+            x, t = c["x"].astype(np.float32), c["t"].astype(np.float32)
+            resid = oracle.medfilt_residual(x[:, None], R_MEDIAN)
+            off64 = oracle.offset(resid, t[:, None])[0]
+            off = np.array([dev_table[k]["offset"]], np.float32)
+            off_err = max(off_err, abs(float(off[0]) - off64) / max(1e-3, abs(off64)))
+            nt = np.array([row["ntrue"]], np.uint32)
+            fmin, df8 = float(row["fmin"]), float(np.float32(row["df"]) * np.float32(fstride))
+            nf8 = (int(row["nf"]) + fstride - 1) // fstride
+            osr, op1, op2, opmax = oracle.bls(resid, t[:, None], nf8, NB, KMA, KMI, int(row["kkmi"]), fmin, df8,
+                                              offset=off, ntrue=nt, nthreads=threads)
+            sr, p1, p2 = (a[::fstride] for a in bat.bls_result(k))
+            fin = np.isfinite(osr[0])
+            err = max(err, float(np.max(np.abs(sr[fin] - osr[0][fin]) / np.maximum(osr[0][fin], 1e-30))))
+            evals += nf8
+            diff = ((p1 != op1[0]) | (p2 != op2[0])) & fin
+            same += int(fin.sum() - diff.sum())
+
+            def tie(j):
+                pw = oracle.bls_window_power(resid, t[:, None], 0, j, int(p1[j]), int(p2[j]), NB, fmin, df8,
+                                             offset=off, ntrue=nt)
+                return abs(pw - opmax[0, j]) <= 1e-5 * opmax[0, j]
+            for j in np.flatnonzero(diff):
+                if tie(j):
+                    ties += 1
+                else:
+                    bad += 1
+            # the curve's best period: argmax over the sampled frequencies, then its bins
+            jg, jo = int(np.argmax(sr)), int(np.argmax(osr[0]))
+            if jg == jo and p1[jg] == op1[0, jg] and p2[jg] == op2[0, jg]:
+                best_same += 1
+            elif osr[0, jg] >= osr[0, jo] * (1 - 1e-5) and tie(jg):
+                best_tie += 1
+            else:
+                best_bad += 1
+        out["bls"] = {"curves": len(ks), "evals": evals, "frequency_stride": fstride,
+                      "sr_max_rel_err": err, "bins_identical": same, "bins_tie_equivalent": ties,
+                      "bins_mismatched": bad, "best_period_bins_identical": best_same,
+                      "best_period_bins_tie_equivalent": best_tie, "best_period_bins_mismatched": best_bad,
+                      "offset_max_rel_err": off_err}
+    if bat.n_tls:
+        ks = sorted(set(np.linspace(0, bat.n_tls - 1, min(n_curves, bat.n_tls)).astype(int).tolist()))
+        err = 0.0
+        evals = wsame = 0
+        for k in ks:
+            c = tls_curves[k]
+            x, t = c["x"].astype(np.float32), c["t"].astype(np.float32)
+            resid = oracle.medfilt_residual(x[:, None], R_MEDIAN)
+            n = x.size
+            ref = oracle.gtls(resid, t[:, None], n, NW, NL, c["nsc"], c["wmax"], c["dw"], c["deltat"],
+                              nthreads=threads)
+            got = bat.tls_result(k)
+            err = max(err, float(np.max(np.abs(got[0] - ref[0][:, 0]) / np.maximum(np.abs(ref[0][:, 0]), 1.0))))
+            evals += n
+            wsame += int(np.sum(got[1] == ref[1][:, 0]))
+        out["gtls"] = {"curves": len(ks), "evals": evals, "sn_max_err": err, "w_identical": wsame}
+    out["oracle_seconds"] = time.perf_counter() - t0
+    return out
+
+
+def served_block(dev, rank, npool=600, fracs=(0.1, 0.5, 0.9)):
+    """The continuous-batching server on a Poisson pool of single-curve requests (BLS or GTLS
+    50/50, detrended; n log-uniform [1000, 70000]): saturation throughput and p50/p99 latency
+    at ``fracs`` of saturation, beside the plain per-request path at the same offered rates."""
+    from gtrap_gb300 import serve as S, synth
+    curves = synth.ragged_mix(npool, seed=5000 + 100000 * rank, n_range=(1000, 70000))
+    pool = [S.Request.from_curve(c) for c in curves]
+    srv = S.TransitServer(detrend_r=R_MEDIAN, hbm_budget=100e9)
+    for r in pool[:40]:
+        srv.submit(r)
+    srv.run_until_idle()
+    t0 = time.perf_counter()
+    for r in pool:
+        srv.submit(r, t0)
+    sat = S.latency_summary(srv.run_until_idle(), time.perf_counter() - t0)
+    plain = S.PlainServer(detrend_r=R_MEDIAN)
+    for r in pool[:10]:
+        plain.process(r)
+    t0 = time.perf_counter()
+    psat = S.latency_summary([plain.process(r, t0) for r in pool[:200]], time.perf_counter() - t0)
+    sweep = []
+    for frac in fracs:
+        rate = frac * sat["req_per_s"]
+        m = min(npool, max(200, int(rate * 1.0)))
+        s = S.latency_summary(S.serve_trace(srv, pool[:m], S.poisson_trace(m, rate, seed=int(frac * 1000))))
+        pm = min(200, max(60, int(rate * 0.3)))
+        ps = S.latency_summary(S.serve_trace(plain, pool[:pm], S.poisson_trace(pm, rate, seed=int(frac * 1000))))
+        sweep.append({"offered_frac": frac, "offered_req_per_s": rate, "requests": m,
+                      "served_req_per_s": s["req_per_s"], "p50_ms": s["p50_ms"], "p99_ms": s["p99_ms"],
+                      "evals_per_s": s["evals_per_s"],
+                      "plain": {"requests": pm, "served_req_per_s": ps["req_per_s"], "p50_ms": ps["p50_ms"],
+                                "p99_ms": ps["p99_ms"]}})
+    return {"what": "continuous-batching server (gtrap_gb300.serve.TransitServer), Poisson arrivals of "
+                    "single-curve BLS/GTLS requests (50/50, detrended), n log-uniform [1000, 70000], nf 2k-32k, "
+                    "HBM budget 100 GB; latency = result on the host minus arrival",
+            "pool": npool, "saturation": sat, "plain_saturation": psat, "sweep": sweep,
+            "hbm_high_water_bytes": srv.hbm_high_water()}
+
+
 def run_ragged(args, rank, world, local_rank):
     import torch
     import torch.distributed as dist
@@ -561,20 +700,19 @@ def run_ragged(args, rank, world, local_rank):
             dist.barrier()
         torch.cuda.synchronize(dev)
 
-    marks = []
+    stages = [name for name in ("prep", "bls", "fold", "tls") if name in graphs]
+    marks = {name: [] for name in stages}
 
     def step(timed=False):
-        graphs["prep"].replay()
-        if timed:
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-        graphs["bls"].replay()
-        if timed:
-            b.record(stream)
-            marks.append((a, b))
-        for name in ("fold", "tls"):
-            if name in graphs:
-                graphs[name].replay()
+        # events between the stage replays time each stage on the launching stream
+        for name in stages:
+            if timed:
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+            graphs[name].replay()
+            if timed:
+                b.record(stream)
+                marks[name].append((a, b))
 
     for _ in range(args.warmup):
         step()
@@ -590,11 +728,13 @@ def run_ragged(args, rank, world, local_rank):
     barrier()
     clk = clocks.stop()
     ms = start.elapsed_time(end) / args.steps
-    bls_ms = float(np.mean([a.elapsed_time(b) for a, b in marks]))
-    t = torch.tensor([ms, bls_ms], device=dev, dtype=torch.float64)
+    stage_ms = {name: float(np.mean([a.elapsed_time(b) for a, b in marks[name]])) for name in stages}
+    t = torch.tensor([ms] + [stage_ms[name] for name in stages], device=dev, dtype=torch.float64)
     if world > 1:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms, bls_ms = float(t[0]), float(t[1])
+    ms = float(t[0])
+    stage_ms = {name: float(v) for name, v in zip(stages, t[1:].tolist())}
+    bls_ms = stage_ms.get("bls", 0.0)
     evals_rank = bat.bls_evals + bat.fold_evals + bat.tls_evals
     evals = evals_rank * world
     value = evals / (ms / 1e3)
@@ -698,16 +838,53 @@ def run_ragged(args, rank, world, local_rank):
                  "bit_identical_sampled_outputs": bool(same)}
         step()  # restore the batch's own outputs
 
+    plain_images = None
+    if not args.no_plain:
+        # the reference drivers' form: one padded [n, nq] image launch sequence per 256 curves
+        imgs = B.ImageBatches(bat, per_image=256)
+        imgs.run()  # warm-up pass (kernel attributes, allocator)
+        barrier()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        w0 = time.perf_counter()
+        s.record(stream)
+        imgs.run()
+        e.record(stream)
+        barrier()
+        pw = time.perf_counter() - w0
+        pms = torch.tensor([max(s.elapsed_time(e), 1e3 * pw)], device=dev, dtype=torch.float64)
+        if world > 1:
+            dist.all_reduce(pms, op=dist.ReduceOp.MAX)
+        plain_images = {"value": evals / (float(pms[0]) / 1e3), "unit": UNIT, "ms_per_step": float(pms[0]),
+                        "what": "the reference drivers' per-batch form: curves in arrival order, 256 per [n, nq] "
+                                "image padded to its longest curve, one gfilter + get_offset + geebls (common "
+                                "grid: lowest fmin and finest df of the image's curves; kkmi of its shortest) or "
+                                "gfilter + gtls (images of one cadence) launch sequence per image; value counts "
+                                "the requested evaluations only",
+                        "images": len(imgs.bls_images) + len(imgs.tls_images),
+                        "evaluated_pairs": imgs.bls_pairs + imgs.tls_pairs, "requested_pairs": evals_rank}
+        del imgs
+        step()
+
     if rank != 0:
         return
     peak = fp32_peak_tflops(dev)
-    flop_per_eval = 7.0 * NB * (KMA - max(KMI, 1))   # s, kk, N-kk, den, s^2 and an FMA compare
+    # the exhaustive scan's work per evaluation: nb * kma candidate windows at ~5 FP32
+    # operations each (two prefix differences, the square, the denominator, the compare)
+    flop_per_eval = 5.0 * NB * KMA
     achieved = flop_per_eval * bat.bls_evals / (bls_ms / 1e3) / 1e12
-    traffic = None
+    traffic = issue = None
     prof = _profile("bls_queue_ragged_traffic.json")
     if prof and prof.get("dram_bytes_per_sample_frequency"):
         unit_work = float(sum(int(r["n"]) * int(r["nf"]) for r in bat.bls_table))
         traffic = prof["dram_bytes_per_sample_frequency"] * unit_work
+    if prof and prof.get("warp_inst_per_eval") and clk.get("sm_mhz"):
+        # executed instructions (ncu count per evaluation of the same mix) per second of the
+        # live kernel time, against the issue limit of 4 warp instructions per clock per SM
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        ipeak = 4.0 * sms * clk["sm_mhz"] * 1e6
+        irate = prof["warp_inst_per_eval"] * bat.bls_evals / (bls_ms / 1e3)
+        issue = {"achieved": irate, "peak": ipeak, "unit": "warp instructions/s", "frac": irate / ipeak,
+                 "inst_per_eval": prof["warp_inst_per_eval"], "source": prof.get("source")}
     # second roofline leg: the fold's sample updates against the shared-atomic peak
     dev_table = np.frombuffer(bat.bls_curves.cpu().numpy().tobytes(), B.BLS_CURVE)
     updates = float((dev_table["nv"].astype(np.float64) * dev_table["nf"]).sum())
@@ -724,11 +901,21 @@ def run_ragged(args, rank, world, local_rank):
                          "kernel": "bls_queue_kernel (persistent BLS fold + scan)", "kernel_ms": bls_ms,
                          "kernel_share": bls_ms / ms,
                          "peak_source": "live FP32 FMA-chain probe on this GPU (MEASURED_PEAKS.json has no FP32 figure)",
-                         "flop_per_eval": flop_per_eval, "fold": fold_leg},
+                         "flop_per_eval": flop_per_eval,
+                         "work": "exhaustive-scan equivalent: nb*kma windows x 5 FP32 ops per evaluation; the "
+                                 "pruned scan evaluates a few per cent of them, see issue",
+                         "issue": issue, "fold": fold_leg},
+            "per_kind": per_kind(bat, stage_ms, ms),
             "gpu_launches": (1 + 4 * (bat.n_bls > 0) + 4 * (bat.n_fold > 0) + (bat.n_tls > 0)) * args.steps,
             "clocks": clk}
     if plain:
         line["plain"] = plain
+    if plain_images:
+        line["plain_images"] = plain_images
+    if not args.no_parity:
+        line["parity"] = ragged_parity(mix, bat)
+    if not args.no_served and args.tls_kind == "gtls":
+        line["served"] = served_block(dev, rank)
     if e2e:
         line["e2e"] = e2e
     if not args.no_cpu_baseline:
@@ -1293,6 +1480,67 @@ def run_served(args, rank, world, local_rank):
     print(json.dumps(line), flush=True)
 
 
+# ----------------------------------------------------------------------------- epilogue
+
+EPI_METRIC = "BLS/TLS epilogue: curves/sec of the fused statistics, the best-peak refinement and detect_peaks"
+
+
+def run_epilogue(args, rank, world, local_rank):
+    """The steps after the searches, on the outputs of the uneven mix (``--nq`` curves, default
+    2000): get_blsstat of every BLS spectrum (gtrap_blsstat_packed), the FP64 refinement of
+    every BLS curve's best peak (gtrap_bls_refine_packed, K 32, S 8, M 8), the GTLS peak
+    statistics of every S/N series (gtrap_peakstat) and detect_peaks over one 2^20-sample
+    series.  Each timed separately with CUDA events (L2 flushed before each call)."""
+    import torch
+    from gtrap_gb300 import _build, api, batch as B, detect_peaks as DP
+
+    _build.build()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    nc = args.nq or 2000
+    mix = make_mix(nc, 4000 + 100000 * rank)
+    bat = build_batch(mix, local_rank)
+    B.autotune(bat)
+    bat.launch()
+    torch.cuda.synchronize(dev)
+    rows = {}
+    nf_tot = int(sum(int(r["nf"]) for r in bat.bls_table))
+    ms, clk = _timed(lambda: bat.bls_stats(), args.steps, args.warmup, dev, world, flush=True)
+    hbm, hsrc = _hbm_peak_gbs()
+    achieved = 12.0 * nf_tot / (ms / 1e3) / 1e9
+    rows["blsstat_packed"] = {"curves": bat.n_bls, "ms": ms, "curves_per_s": bat.n_bls / (ms / 1e3),
+                              "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                                           "frac": achieved / hbm, "peak_source": hsrc,
+                                           "bytes": "12 B per frequency (SR, start, end read once)"}}
+    spec = bat.bls_spec
+    refine = lambda: api.bls_refine_packed(bat.blsp, bat.ph1, bat.ph2, bat.bls_curves, bat.t, bat.resid, spec.nb,
+                                           spec.kma, spec.kmi, count=bat.n_bls)
+    ms, _ = _timed(refine, args.steps, args.warmup, dev, world, flush=True)
+    rec = bat.bls_refine()
+    gain = rec["sr"][rec["sr_grid"] > 0] / rec["sr_grid"][rec["sr_grid"] > 0]
+    rows["bls_refine"] = {"curves": bat.n_bls, "ms": ms, "curves_per_s": bat.n_bls / (ms / 1e3),
+                          "trials_per_curve": 65, "sr_gain_median": float(np.median(gain)) if gain.size else None,
+                          "sr_gain_p90": float(np.percentile(gain, 90)) if gain.size else None}
+    ms, _ = _timed(lambda: bat.tls_peakstat(), args.steps, args.warmup, dev, world, flush=True)
+    rows["peakstat"] = {"curves": bat.n_tls, "ms": ms, "curves_per_s": bat.n_tls / (ms / 1e3),
+                        "epochs": bat.tls_evals}
+    x = np.random.default_rng(7).normal(size=1 << 20)
+    xd = torch.from_numpy(x).to(dev)
+    ms, _ = _timed(lambda: DP.detect_peaks(xd, mpd=10), args.steps, args.warmup, dev, world, flush=True)
+    rows["detect_peaks"] = {"samples": x.size, "ms": ms, "samples_per_s": x.size / (ms / 1e3)}
+    if rank != 0:
+        return
+    total_ms = rows["blsstat_packed"]["ms"] + rows["bls_refine"]["ms"] + rows["peakstat"]["ms"]
+    value = (bat.n_bls + bat.n_tls) / (total_ms / 1e3)
+    line = {"metric": EPI_METRIC, "value": value, "unit": "curves/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic",
+            "config": {"workload": "epilogue of the uneven mix (%d curves: %d BLS spectra, %d GTLS S/N series)"
+                                   % (nc, bat.n_bls, bat.n_tls), "l2": "flushed before each timed call"},
+            "kernels": rows, "gpu_launches": 6 * args.steps, "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 # ----------------------------------------------------------------------------- trapezoid grid fit
 
 FIT_UNIT = "templates/s"
@@ -1484,7 +1732,8 @@ def main():
         dist.init_process_group("nccl")
     try:
         {"ragged": run_ragged, "masked": run_masked, "served": run_served, "plain": run_image,
-         "tls": run_image, "tlsfold": run_tlsfold, "mock": run_mock, "tlsfit": run_tlsfit}[args.workload](
+         "tls": run_image, "tlsfold": run_tlsfold, "mock": run_mock, "tlsfit": run_tlsfit,
+         "epilogue": run_epilogue}[args.workload](
             args, rank, world, local_rank)
     finally:
         if world > 1:

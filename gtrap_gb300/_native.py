@@ -54,6 +54,11 @@ _SIGNATURES = {
                                  vp, vp, vp, vp]),
     "gtrap_blsstat": (C.c_int, [vp, vp, vp, u32, u32, f64, f64, u32, vp, vp, vp, vp, vp]),
     "gtrap_blsstat_packed": (C.c_int, [vp, vp, vp, vp, vp, u32, u32, vp, vp, vp, vp, vp]),
+    "gtrap_bls_refine_workspace_size": (sz, [u32, u32]),
+    "gtrap_bls_refine": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, u32, u32, u32, u32, u32, u32, u32, f32, f32,
+                                   u32, u32, u32, vp, vp, sz, vp]),
+    "gtrap_bls_refine_packed": (C.c_int, [vp, vp, vp, vp, vp, u32, vp, vp, u32, u32, u32, u32, u32, u32, vp,
+                                          vp, sz, vp]),
     "gtrap_getmax": (C.c_int, [vp, vp, vp, u32, u32, u32, vp, vp, vp, vp, vp, vp, vp]),
     "gtrap_gtls": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, i32, i32, i32, i32, i32, f32, f32, f32,
                              f32, f32, i32, u32, vp]),

@@ -182,6 +182,56 @@ def blsstat_packed(blsp, phase1, phase2, curves, sel=None, count=None, patch=0, 
     return pest, sde, b1, b2
 
 
+# Record layout of gtrap_bls_refined (include/gtrap_gb300.h).
+BLS_REFINED = _np.dtype([("freq", "<f8"), ("period", "<f8"), ("phase", "<f8"), ("duration", "<f8"),
+                         ("t0", "<f8"), ("depth", "<f8"), ("sr", "<f8"), ("sr_grid", "<f4"),
+                         ("jgrid", "<u4"), ("dk", "<i4"), ("kk", "<u4")])
+REFINE_DEFAULTS = dict(K=32, S=8, M=8)
+# a served BLS request's record: get_blsstat's statistics and the refined best peak
+BLS_STATS_REFINED = _np.dtype(BLS_STATS.descr + [("refined", BLS_REFINED)])
+
+
+def bls_refine(blsp, phase1, phase2, lc, tu, offset_, ntrue, nb, kma, kmi, kkmi, fmin, df, *, K=32, S=8, M=8,
+               stream=None):
+    """Refine each curve's best peak of a :func:`geebls` spectrum (``gtrap_bls_refine``):
+    2K+1 trial frequencies over +-df around the grid maximum; at each, every window of whole
+    bins within M bins of the grid window, then its edges on a phase grid S times finer than
+    nb; FP64 powers.  Returns a uint8 device
+    tensor of ``nq`` records (:data:`BLS_REFINED`); :func:`refined_to_numpy` reads it."""
+    lc = _f32(lc, "lc")
+    tu = _f32(tu, "tu")
+    n, nq = lc.shape
+    nf = blsp.shape[1]
+    dev = lc.device
+    out = torch.empty(nq * BLS_REFINED.itemsize, dtype=torch.uint8, device=dev)
+    ws = workspace(N.fn("gtrap_bls_refine_workspace_size")(nq, int(K)), slot="refine")
+    N.call("gtrap_bls_refine", as_ptr(blsp), as_ptr(phase1), as_ptr(phase2), as_ptr(lc), as_ptr(tu),
+           as_ptr(_f32(offset_, "offset")), as_ptr(_u32(ntrue, "ntrue")), n, nq, int(nf), int(nb), int(kma),
+           int(kmi), int(kkmi), float(fmin), float(df), int(K), int(S), int(M), as_ptr(out), as_ptr(ws),
+           ws.numel(), stream_handle(stream))
+    return out
+
+
+def bls_refine_packed(blsp, phase1, phase2, curves, t, x, nb, kma, kmi, *, sel=None, count=None, K=32, S=8, M=8,
+                      stream=None):
+    """:func:`bls_refine` for packed spectra (``gtrap_bls_refine_packed``): ``curves`` the device
+    table of ``gtrap_bls_curve`` rows, ``t``/``x`` the packed times and folded flux, ``sel`` an
+    optional int32 device tensor of row indices.  Returns a uint8 tensor of records."""
+    dev = blsp.device
+    if count is None:
+        count = int(sel.numel()) if sel is not None else curves.numel() // 56
+    out = torch.empty(max(count, 1) * BLS_REFINED.itemsize, dtype=torch.uint8, device=dev)
+    ws = workspace(N.fn("gtrap_bls_refine_workspace_size")(max(count, 1), int(K)), slot="refine")
+    N.call("gtrap_bls_refine_packed", as_ptr(blsp), as_ptr(phase1), as_ptr(phase2), as_ptr(curves),
+           as_ptr(sel) if sel is not None else None, int(count), as_ptr(t), as_ptr(x), int(nb), int(kma), int(kmi),
+           int(K), int(S), int(M), as_ptr(out), as_ptr(ws), ws.numel(), stream_handle(stream))
+    return out[:count * BLS_REFINED.itemsize]
+
+
+def refined_to_numpy(out: torch.Tensor) -> _np.ndarray:
+    return _np.frombuffer(out.cpu().numpy().tobytes(), BLS_REFINED)
+
+
 def getmax(blsp, phase1, phase2, patch, stream=None):
     """Per-patch partial statistics with the reference getmax kernel's outputs."""
     blsp = _f32(blsp, "blsp")

@@ -33,7 +33,7 @@ import torch
 
 from . import _native as N
 from . import api
-from ._dev import as_ptr, require_cuda, stream_handle
+from ._dev import as_ptr, require_cuda, stream_handle, workspace
 
 # Layouts of the C structs (include/gtrap_gb300.h).
 BLS_CURVE = np.dtype([("off", "<u8"), ("out", "<u8"), ("n", "<u4"), ("nf", "<u4"),
@@ -509,6 +509,18 @@ class RaggedBatch:
         return api.blsstat_packed(self.blsp, self.ph1, self.ph2, self.bls_curves, None, self.n_bls, patch,
                                   stream)
 
+    def bls_refine(self, K: int = 32, S: int = 8, M: int = 8, stream=None):
+        """Refine every BLS request's best peak on the device (``gtrap_bls_refine_packed``):
+        2K+1 trial frequencies over +-df around the grid maximum, windows within M bins of its
+        grid window with edges on a phase grid S times finer than nb, FP64 powers.  Returns the records (numpy,
+        :data:`api.BLS_REFINED`), one per BLS request."""
+        if not self.n_bls:
+            raise ValueError("no BLS requests in the batch")
+        s = self.bls_spec
+        out = api.bls_refine_packed(self.blsp, self.ph1, self.ph2, self.bls_curves, self.t, self.resid, s.nb,
+                                    s.kma, s.kmi, count=self.n_bls, K=K, S=S, M=M, stream=stream)
+        return api.refined_to_numpy(out)
+
     def fold_stats(self, patch: int = 0, stream=None):
         """The same statistics of every folded-search spectrum: (Pest, SDE, start bin and
         duration index at the maximum TSR)."""
@@ -661,3 +673,89 @@ def run_plain(batch: RaggedBatch, stream=None, bls_curves=None, tls_curves=None,
         api.gtls(r, t, nt, ts.nw, ts.nl, int(row["nsc"]), float(row["wmax"]), float(row["dw"]),
                  float(row["deltat"]), mode=ts.mode, fix_a=ts.fix_a,
                  out=tuple(v[o:o + nt].view(nt, 1) for v in batch.tls_outs), stream=stream)
+
+
+class ImageBatches:
+    """The requests of a packed batch as the reference's drivers launch them: curves in
+    arrival order, ``per_image`` to an ``[n, nq]`` image padded to the image's longest curve
+    (padding masked, t = -1000), one gfilter + get_offset + geebls (or gfilter + gtls) launch
+    sequence per image (``ipynb/example geebls  Kepler Planet.ipynb:273-286``,
+    ``kepler/gtls_mockkepler.py:228-312``).  A BLS image shares one frequency grid (the lowest
+    fmin and finest df of its curves, up to 2 per day) and one kkmi (its shortest curve's), so
+    it evaluates more (curve, frequency) pairs than the requests ask for; GTLS images hold
+    curves of one cadence (the kernel takes one epoch step).  The images are built on the
+    device once; :meth:`run` launches them.  Results differ from the per-request searches by
+    construction (common grid and kkmi); this is a throughput baseline."""
+
+    def __init__(self, batch: RaggedBatch, per_image: int = 256, fmax: float = 2.0):
+        if not batch.built:
+            batch.build()
+        self.batch = batch
+        dev = batch.device
+        offs = batch.offs_host
+        self.bls_images, self.tls_images = [], []
+        self.bls_pairs = 0   # (curve, frequency) pairs the images evaluate
+        self.tls_pairs = 0   # (curve, epoch) pairs
+
+        def image(idx):
+            ns = [int(offs[j + 1] - offs[j]) for j in idx]
+            n = max(ns)
+            x = torch.zeros((n, len(idx)), dtype=torch.float32, device=dev)
+            t = torch.full((n, len(idx)), -1000.0, dtype=torch.float32, device=dev)
+            for q, (j, m) in enumerate(zip(idx, ns)):
+                a = int(offs[j])
+                x[:m, q] = batch.x[a:a + m]
+                t[:m, q] = batch.t[a:a + m]
+            return x, t, ns
+
+        tab = batch.bls_table
+        for s in range(0, batch.n_bls, per_image):
+            ks = list(range(s, min(batch.n_bls, s + per_image)))
+            x, t, ns = image(ks)
+            fmin = float(np.float32(tab["fmin"][ks].min()))
+            df = float(np.float32(tab["df"][ks].min()))
+            nf = int(np.floor((fmax - fmin) / df)) + 1
+            kkmi = int(tab["kkmi"][ks].min())
+            ntrue = torch.from_numpy(tab["ntrue"][ks].astype(np.int32)).to(dev)
+            self.bls_images.append((x, t, ntrue, nf, fmin, df, kkmi))
+            self.bls_pairs += nf * len(ks)
+        ttab = batch.tls_table
+        first = batch.n_bls + batch.n_fold
+        for deltat in np.unique(ttab["deltat"]) if batch.n_tls else []:
+            members = [k for k in range(batch.n_tls) if ttab["deltat"][k] == deltat]
+            for s in range(0, len(members), per_image):
+                ks = members[s:s + per_image]
+                x, t, ns = image([first + k for k in ks])
+                # one scoop size and width grid per image: the widest of its curves
+                row = ttab[ks[int(np.argmax(ttab["nsc"][ks]))]]
+                self.tls_images.append((x, t, int(row["nsc"]), float(row["wmax"]), float(row["dw"]),
+                                        float(row["deltat"])))
+                self.tls_pairs += x.shape[0] * len(ks)
+        nq_b = max([im[0].shape[1] for im in self.bls_images], default=0)
+        nf_b = max([im[3] for im in self.bls_images], default=0)
+        self.bls_out = tuple(torch.empty(nq_b * nf_b, dtype=dt, device=dev)
+                             for dt in (torch.float32, torch.int32, torch.int32))
+        n_t = max([im[0].numel() for im in self.tls_images], default=0)
+        self.tls_out = tuple(torch.empty(n_t, dtype=torch.float32, device=dev) for _ in range(5))
+        if self.bls_images:  # size the geebls workspace for the largest image up front
+            need = max(int(N.fn("gtrap_geebls_workspace_size")(im[0].shape[0], im[0].shape[1], batch.bls_spec.flags))
+                       for im in self.bls_images)
+            workspace(need, slot="bls")
+
+    def run(self, stream=None):
+        b = self.batch
+        s, ts = b.bls_spec, b.tls_spec
+        r = b.detrend_r
+        for x, t, ntrue, nf, fmin, df, kkmi in self.bls_images:
+            nq = x.shape[1]
+            res = api.gfilter(x, r, stream=stream) if r is not None else x
+            off = api.offset(res, t, stream=stream)
+            out = tuple(o[:nq * nf].view(nq, nf) for o in self.bls_out)
+            api.geebls(res, t, off, ntrue, nf, s.nb, s.kma, s.kmi, kkmi, fmin, df, phase=s.phase, out=out,
+                       stream=stream)
+        for x, t, nsc, wmax, dw, deltat in self.tls_images:
+            n, nq = x.shape
+            res = api.gfilter(x, r, stream=stream) if r is not None else x
+            out = tuple(o[:n * nq].view(n, nq) for o in self.tls_out)
+            api.gtls(res, t, n, ts.nw, ts.nl, nsc, wmax, dw, deltat, mode=ts.mode, fix_a=ts.fix_a, out=out,
+                     stream=stream)

@@ -51,24 +51,7 @@ constexpr int kFastMaxCount = 512;
 // covers the rounding of the expanded denominator form (error <= ~5 ulp of blo*den).
 constexpr float kSlack = 1.0f - 1.0f / 32768.0f;
 
-// frac(t*f) * 2^64 for float32 t and f, exact whenever the product is >= 2^-17.
-__device__ __forceinline__ uint64_t frac64(float t, float f) {
-  const uint32_t bt = __float_as_uint(t), bf = __float_as_uint(f);
-  const uint32_t et = (bt >> 23) & 0xFFu, ef = (bf >> 23) & 0xFFu;
-  const uint64_t mt = (bt & 0x7FFFFFu) | (et ? 0x800000u : 0u);
-  const uint64_t mf = (bf & 0x7FFFFFu) | (ef ? 0x800000u : 0u);
-  // t*f = mt*mf * 2^(e), e = (et' - 150) + (ef' - 150) with et' = max(et, 1)
-  const int e = (int)(et ? et : 1u) + (int)(ef ? ef : 1u) - 300;
-  const uint64_t m = mt * mf;  // < 2^48
-  const int s = e + 64;        // fraction bits start 64 places below the binary point
-  uint64_t a;
-  if (s >= 64 || m == 0) a = 0;             // integer product
-  else if (s >= 0) a = m << s;              // bits above 2^0 fall off: frac
-  else if (s > -64) a = m >> (-s);          // product below 2^-16: truncated
-  else a = 0;
-  if ((bt ^ bf) >> 31) a = 0ull - a;        // frac(-x) = 1 - frac(x)
-  return a;
-}
+using gtrap::frac64;
 
 // ---------------------------------------------------------------------------
 // prep

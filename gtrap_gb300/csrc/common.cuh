@@ -59,6 +59,25 @@ int ragged_prepare(gtrap_bls_curve *curves, uint32_t ncurves, uint32_t max_n, co
                    const float *x, uint64_t total, void *pool, size_t pool_bytes, uint32_t flags,
                    double xq_cap, cudaStream_t stream);
 
+// frac(t*f) * 2^64 for float32 t and f, exact whenever the product is >= 2^-17.
+__device__ __forceinline__ uint64_t frac64(float t, float f) {
+  const uint32_t bt = __float_as_uint(t), bf = __float_as_uint(f);
+  const uint32_t et = (bt >> 23) & 0xFFu, ef = (bf >> 23) & 0xFFu;
+  const uint64_t mt = (bt & 0x7FFFFFu) | (et ? 0x800000u : 0u);
+  const uint64_t mf = (bf & 0x7FFFFFu) | (ef ? 0x800000u : 0u);
+  // t*f = mt*mf * 2^(e), e = (et' - 150) + (ef' - 150) with et' = max(et, 1)
+  const int e = (int)(et ? et : 1u) + (int)(ef ? ef : 1u) - 300;
+  const uint64_t m = mt * mf;  // < 2^48
+  const int s = e + 64;        // fraction bits start 64 places below the binary point
+  uint64_t a;
+  if (s >= 64 || m == 0) a = 0;             // integer product
+  else if (s >= 0) a = m << s;              // bits above 2^0 fall off: frac
+  else if (s > -64) a = m >> (-s);          // product below 2^-16: truncated
+  else a = 0;
+  if ((bt ^ bf) >> 31) a = 0ull - a;        // frac(-x) = 1 - frac(x)
+  return a;
+}
+
 inline bool is_pow2(uint32_t x) { return x && !(x & (x - 1)); }
 
 inline int ilog2u(uint32_t x) {

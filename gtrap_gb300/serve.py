@@ -90,8 +90,9 @@ class Result:
     done: float
     outputs: tuple   # bls: (blsp, phase1, phase2); fold: (tsr, start, duration index, depth);
     #                  tls: (sn, w, t0, l, hmax), or with tls_peaks (PEAK_STATS record, peak
-    #                  indices, peak heights); bls and fold with spectrum_stats: a BLS_STATS
-    #                  record (pest, sde, ph1, ph2; for fold ph1/ph2 = start bin, duration index)
+    #                  indices, peak heights); bls with spectrum_stats: a BLS_STATS_REFINED
+    #                  record (pest, sde, ph1, ph2 and the refined best peak); fold with
+    #                  spectrum_stats: a BLS_STATS record (ph1/ph2 = start bin, duration index)
     evals: int
 
     @property
@@ -198,7 +199,7 @@ class _Step:
     event: object
     finishing: list = field(default_factory=list)
     peaks: tuple = ()      # (stats, idx, val) device buffers of the GTLS requests it finishes
-    bstats: dict = field(default_factory=dict)  # kind -> (pest, sde, ph1, ph2) device buffers
+    bstats: dict = field(default_factory=dict)  # kind -> (pest, sde, ph1, ph2[, refined]) device buffers
 
 
 class TransitServer:
@@ -520,6 +521,11 @@ class TransitServer:
                     sel = self._upload_small([lv.desc for lv in fin], np.int32)
                     sels.append(sel)
                     bst[kind] = api.blsstat_packed(self.o[0], self.o[1], self.o[2], table, sel, len(fin), stream=st)
+                    if kind == "bls":  # and the refined best peak (FP64 neighbourhood search)
+                        bs = self.bls_spec
+                        ref = api.bls_refine_packed(self.o[0], self.o[1], self.o[2], table, self.t, self.resid,
+                                                    bs.nb, bs.kma, bs.kmi, sel=sel, count=len(fin), stream=st)
+                        bst[kind] = bst[kind] + (ref.view(len(fin), api.BLS_REFINED.itemsize),)
             ev = torch.cuda.Event()
             ev.record(st)
         step = _Step(si, ev, peaks=pk, bstats=bst)
@@ -586,8 +592,15 @@ class TransitServer:
                 now = time.perf_counter()
                 res = lv.result
                 if lv.st_slot >= 0:
-                    res = np.array((float(res[0].numpy()[0]), float(res[1].numpy()[0]), int(res[2].numpy()[0]),
-                                    int(res[3].numpy()[0])), dtype=api.BLS_STATS)
+                    stats = (float(res[0].numpy()[0]), float(res[1].numpy()[0]), int(res[2].numpy()[0]),
+                             int(res[3].numpy()[0]))
+                    if len(res) > 4:  # BLS: with the refined best peak
+                        rec = np.zeros((), api.BLS_STATS_REFINED)
+                        rec["pest"], rec["sde"], rec["ph1"], rec["ph2"] = stats
+                        rec["refined"] = np.frombuffer(res[4].numpy().tobytes(), api.BLS_REFINED)[0]
+                        res = rec
+                    else:
+                        res = np.array(stats, dtype=api.BLS_STATS)
                 elif lv.req.kind == "bls":
                     res = (res[0].numpy(), res[1].numpy().view(np.int32), res[2].numpy().view(np.int32))
                 elif lv.req.kind == "fold":

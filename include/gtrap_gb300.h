@@ -204,6 +204,54 @@ int gtrap_blsstat_packed(const float *blsp, const uint32_t *phase1, const uint32
                          uint32_t patch, double *pest, double *sde, uint32_t *ph1best,
                          uint32_t *ph2best, gtrap_stream_t stream);
 
+/* ---------------------------------------------------------------------------
+ * Best-peak refinement.  Extends the reference's epilogue (getmax + combine_stat,
+ * gtrap/getstat.py:14-57, 100-123, which stops at the grid maximum) by re-evaluating the
+ * statistic around each curve's grid peak: with j the first maximum of the spectrum and
+ * [p1, p2] its window (phase outputs of the search), 2K+1 trial frequencies
+ * f_j + (k - K) df / K, k = 0 .. 2K; at each, the samples within M bins of [p1, p2] are binned
+ * on a phase grid S times finer than nb, every window of whole bins in that neighbourhood
+ * (width in (kmi, kma] bins) and then every window with fine edges within one bin of the best
+ * one's edges is evaluated (more than max(kkmi, 5) samples): power = s^2 / (kk (N - kk)) in
+ * FP64 with N = ntrue; the best window by (power, lower start, lower end), the best trial by
+ * (power, lower k).
+ * Phases are exact 64-bit fractions referred at each trial to the middle of the curve's
+ * valid time span (t_ref = (t_min + t_max) / 2 in float32); flux sums are exact integers of
+ * the flux quantised to 2^-40 of its range (deterministic).
+ * nb a power of two in [2, 8192], K a power of two <= 1024, S in [1, 64], M <= 64,
+ * (kma + 2M) * S <= 4096.  A curve without a positive grid peak gets a zero record.
+ * ------------------------------------------------------------------------- */
+typedef struct {
+  double freq;      /* refined trial frequency (1/day) */
+  double period;    /* 1 / freq */
+  double phase;     /* window start in cycles of frac(t * freq), [0, 1) */
+  double duration;  /* window width in cycles */
+  double t0;        /* mid-window time nearest t_ref */
+  double depth;     /* mean flux outside the window minus inside (positive for a dip) */
+  double sr;        /* refined SR = sqrt(power) */
+  float sr_grid;    /* SR of the grid peak */
+  uint32_t jgrid;   /* grid index of the peak */
+  int32_t dk;       /* trial offset: freq = f_jgrid + dk * df / K */
+  uint32_t kk;      /* samples in the refined window */
+} gtrap_bls_refined; /* 72 bytes */
+
+/* Workspace bytes for ncurves curves at K. */
+size_t gtrap_bls_refine_workspace_size(uint32_t ncurves, uint32_t K);
+/* [n, nq] image form (the arguments of gtrap_geebls; blsp/phase1/phase2 its outputs,
+ * lc the flux it folded).  out: nq records (device). */
+int gtrap_bls_refine(const float *blsp, const uint32_t *phase1, const uint32_t *phase2, const float *lc,
+                     const float *tu, const float *offset, const uint32_t *ntrue, uint32_t n, uint32_t nq,
+                     uint32_t nf, uint32_t nb, uint32_t kma, uint32_t kmi, uint32_t kkmi, float fmin,
+                     float df, uint32_t K, uint32_t S, uint32_t M, gtrap_bls_refined *out, void *workspace,
+                     size_t workspace_bytes, gtrap_stream_t stream);
+/* Packed form: record c refines curve sel[c] (c when sel is NULL) of the device table, whose
+ * samples are t/x[off + i] (x the flux it folded) and spectrum [out, out + nf). */
+int gtrap_bls_refine_packed(const float *blsp, const uint32_t *phase1, const uint32_t *phase2,
+                            const gtrap_bls_curve *curves, const uint32_t *sel, uint32_t count,
+                            const float *t, const float *x, uint32_t nb, uint32_t kma, uint32_t kmi,
+                            uint32_t K, uint32_t S, uint32_t M, gtrap_bls_refined *out, void *workspace,
+                            size_t workspace_bytes, gtrap_stream_t stream);
+
 /* Per-patch partials with the getmax kernel's outputs (gtrap/getstat.py:14-57): for
  * patch p of `patch` frequencies of curve q, element p + npatch*q of each output holds
  * the patch maximum, its global index j + nf*q (lowest on ties), the patch sum and sum
