@@ -348,8 +348,8 @@ def run_masked(args, rank, world, local_rank):
         return
     # roofline of the dominant kernel (the BLS call: prep + fold/scan), FP32-pipe bound
     peak = fp32_peak_tflops(dev)
-    cand = NB * (kma - max(kmi, 1))            # accepted windows per evaluation
-    flop_per_eval = 7.0 * cand                  # s, kk, N-kk, den, s^2 and an FMA compare
+    # the exhaustive scan's work per evaluation: nb * kma windows at ~5 FP32 operations each
+    flop_per_eval = 5.0 * NB * kma
     achieved = flop_per_eval * nq * NF / (bls_ms / 1e3) / 1e12
     traffic = None
     prof = _profile("bls_fold_scan_traffic.json")
@@ -363,7 +363,8 @@ def run_masked(args, rank, world, local_rank):
                          "frac": achieved / peak, "traffic": traffic,
                          "kernel": "geebls (prep + bls_fold_scan_kernel)", "kernel_ms": bls_ms,
                          "peak_source": "live FP32 FMA-chain probe on this GPU (MEASURED_PEAKS.json has no FP32 figure)",
-                         "flop_per_eval": flop_per_eval},
+                         "flop_per_eval": flop_per_eval,
+                         "work": "exhaustive-scan equivalent: nb*kma windows x 5 FP32 ops per evaluation"},
             "gpu_launches": 6 * args.steps,
             "clocks": clk}
     if e2e:
@@ -1665,7 +1666,8 @@ def run_tlsfit(args, rank, world, local_rank):
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": fit_config(tl.size) | {"parallelism": "replicas x%d" % world},
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": achieved / peak, "traffic": None,
+                         "frac": achieved / peak,
+                         "traffic": (_profile("tlsfit_traffic.json") or {}).get("dram_bytes_per_launch"),
                          "kernel": "tlsfit_kernel (one thread per template) + nanargmax_kernel",
                          "algorithmic_flops": "%g FP64 flops per (template, window sample): mean, region sums "
                                               "and residual passes" % FIT_FLOPS,

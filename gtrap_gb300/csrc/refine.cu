@@ -32,6 +32,8 @@ using gtrap::frac64;
 constexpr int kThreads = 256;
 constexpr int kMaxFine = 4096;        // fine bins of one neighbourhood, (p2 - p1 + 1 + 2M) * S
 constexpr double kXqMax = 1099511627776.0;  // |quantised flux| < 2^40
+constexpr int kMaxGroup = 16;               // trials per block at most
+constexpr size_t kSmemBudget = 96 * 1024;   // fine histograms of one block (two blocks per SM)
 
 // One trial frequency's best window (and the curve's constants every block recomputes).
 struct Part {
@@ -62,6 +64,7 @@ struct RefArgs {
   uint32_t n, nq, nf, kkmi;
   float fmin, df;
   uint32_t nb, kma, kmi, K, S, M;
+  uint32_t G;                     // trials per block
   int lognb, logK;
   Part *part;                     // [count, 2K + 1]
   gtrap_bls_refined *out;
@@ -82,8 +85,23 @@ __device__ RefCurve curve_of(const RefArgs &a, uint32_t c) {
   return r;
 }
 
-__device__ __forceinline__ bool valid(float t, float x, double off) {
-  return t >= 0.0f && isfinite(t) && isfinite(x) && isfinite((double)x - off);
+// (x - offset is finite in double whenever both are finite floats; a non-finite offset is
+// checked once per curve)
+__device__ __forceinline__ bool valid(float t, float x) {
+  return t >= 0.0f && isfinite(t) && isfinite(x);
+}
+
+// rint((x - off) * 2^sx) for finite floats with |x - off| * 2^sx < 2^40 (at most one unit off
+// the exact rounding), in FP32 and integer instructions: x - off = s + e exactly (TwoSum),
+// s * 2^sx split into 20-bit halves.
+__device__ __forceinline__ long long quantise(float x, float off, int sx) {
+  const float s = __fsub_rn(x, off);
+  const float bv = __fsub_rn(s, x);
+  const float e = __fadd_rn(__fsub_rn(x, __fsub_rn(s, bv)), __fsub_rn(-off, bv));
+  const float S = ldexpf(s, sx), Es = ldexpf(e, sx);
+  const float hi = truncf(ldexpf(S, -20));
+  const float lo = __fsub_rn(S, ldexpf(hi, 20));  // exact: S with its top bits removed
+  return ((long long)__float2int_rz(hi) << 20) + (long long)__float2int_rn(lo) + (long long)__float2int_rn(Es);
 }
 
 // Block reductions (kThreads threads); every thread gets the result.
@@ -113,16 +131,22 @@ __device__ __forceinline__ bool better(double p, uint32_t a, uint32_t b, double 
   return p > bp || (p == bp && (a < ba || (a == ba && b < bb)));
 }
 
+// One block per (curve, group of G consecutive trials): the samples are read and their exact
+// phase pairs formed once for the group, and each trial gets its own fine histogram.
 __global__ void __launch_bounds__(kThreads) refine_trial_kernel(const RefArgs a) {
   extern __shared__ __align__(16) unsigned char dyn[];
   __shared__ float shf[kThreads / 32];
   __shared__ long long shl[kThreads / 32];
   __shared__ unsigned shu[kThreads / 32];
   __shared__ uint32_t sj;
-  const uint32_t c = blockIdx.x, k = blockIdx.y;
-  const int tid = threadIdx.x;
+  __shared__ float pmax_s[kMaxGroup];
+  const uint32_t c = blockIdx.x;
+  const uint32_t nk_all = 2 * a.K + 1;
+  const uint32_t k0 = blockIdx.y * a.G;
+  const uint32_t nk = min(a.G, nk_all - k0);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const RefCurve cv = curve_of(a, c);
-  Part *pt = a.part + (size_t)c * (2 * a.K + 1) + k;
+  Part *pt = a.part + (size_t)c * nk_all + k0;
 
   // ---- grid peak: first maximum of the spectrum
   float best = -INFINITY;
@@ -137,34 +161,32 @@ __global__ void __launch_bounds__(kThreads) refine_trial_kernel(const RefArgs a)
   if (best == gmax && bj != UINT_MAX) atomicMin(&sj, bj);
   __syncthreads();
   const uint32_t j = sj;
-  if (!(gmax > 0.0f) || j == UINT_MAX) {
-    if (tid == 0) { pt->pw = -1.0; pt->j = j == UINT_MAX ? 0u : j; }
-    return;
-  }
-  const uint32_t p1 = a.ph1[cv.out + j];
-  const uint32_t p2 = a.ph2[cv.out + j];
   const uint32_t nb = a.nb;
-  // a window the search cannot have produced (start past nb, end before start, wider than
-  // kma) is no peak: the neighbourhood must stay within the fine bins sized on the host
-  if (p1 >= nb || p2 < p1 || p2 - p1 + 1 > a.kma) {
-    if (tid == 0) { pt->pw = -1.0; pt->j = j; }
+  const uint32_t p1 = j == UINT_MAX ? 0u : a.ph1[cv.out + j];
+  const uint32_t p2 = j == UINT_MAX ? 0u : a.ph2[cv.out + j];
+  // no positive peak, or a window the search cannot have produced (start past nb, end before
+  // start, wider than kma): no refinement (the neighbourhood must fit the host-sized bins)
+  if (!(gmax > 0.0f) || j == UINT_MAX || p1 >= nb || p2 < p1 || p2 - p1 + 1 > a.kma) {
+    if (tid < (int)nk) { pt[tid].pw = -1.0; pt[tid].j = j == UINT_MAX ? 0u : j; }
     return;
   }
   // neighbourhood: grid window widened by M bins on each side, at most one cycle
   uint32_t M = a.M;
   const uint32_t w0 = p2 - p1 + 1;
   while (M > 0 && w0 + 2 * M > nb) --M;
-  const uint32_t L = w0 + 2 * M;           // coarse bins of the neighbourhood
-  const uint32_t LS = L * a.S;              // fine bins (checked on the host: <= kMaxFine)
+  const uint32_t L = w0 + 2 * M;            // coarse bins of the neighbourhood
+  const uint32_t S = a.S;
+  const uint32_t LS = L * S;                // fine bins (host check: <= kMaxFine)
+  const uint32_t E = LS + 1;                // prefix entries per trial
 
-  // ---- scale, mean time, valid count
-  const double off = (double)cv.offset;
+  // ---- scale, reference time, valid count (a non-finite offset leaves no valid sample)
+  const bool off_ok = isfinite(cv.offset);
   float amax = 0.0f, tlo = INFINITY, thi = -INFINITY;
   uint32_t cnt = 0;
-  for (uint32_t i = tid; i < cv.n; i += kThreads) {
+  for (uint32_t i = tid; i < cv.n && off_ok; i += kThreads) {
     const size_t idx = cv.off + (size_t)i * cv.stride;
     const float t = a.t[idx], x = a.x[idx];
-    if (valid(t, x, off)) {
+    if (valid(t, x)) {
       amax = fmaxf(amax, fabsf(__fsub_rz(x, cv.offset)));
       tlo = fminf(tlo, t);
       thi = fmaxf(thi, t);
@@ -179,66 +201,86 @@ __global__ void __launch_bounds__(kThreads) refine_trial_kernel(const RefArgs a)
   // reference time: the middle of the valid time span, in float32 (order-independent)
   const float tref = nv ? __fmul_rn(__fadd_rn(tlo, thi), 0.5f) : 0.0f;
 
-  // ---- exact phases at trial k: A + J*B' - (k - K)*R' with B' = frac(t df/K), R' = frac(tref df/K)
+  // ---- exact phases: trial k is A + J_k B' - (k - K) R' with B' = frac(t df/K), R' = frac(tref
+  // df/K) and J_k = j K + k - K; consecutive trials differ by B' - R'
   const float dfK = ldexpf(cv.df, -a.logK);
-  const long long J = (long long)j * a.K + ((long long)k - (long long)a.K);
-  const unsigned long long shift =
-      (unsigned long long)((long long)k - (long long)a.K) * frac64(tref, dfK);
+  const unsigned long long Rp = frac64(tref, dfK);
+  const long long J0 = (long long)j * a.K + ((long long)k0 - (long long)a.K);
+  const unsigned long long shift0 = (unsigned long long)((long long)k0 - (long long)a.K) * Rp;
   const unsigned long long lo =
       (unsigned long long)((p1 + nb - M) & (nb - 1)) << (64 - a.lognb);  // neighbourhood start
-
-  long long *hs = reinterpret_cast<long long *>(dyn);
-  int *hc = reinterpret_cast<int *>(hs + (LS + 1));
-  for (uint32_t b = tid; b <= LS; b += kThreads) { hs[b] = 0; hc[b] = 0; }
+  long long *hs = reinterpret_cast<long long *>(dyn);                 // [G][E] flux sums
+  int *hc = reinterpret_cast<int *>(hs + (size_t)a.G * E);            // [G][E] counts
+  float *pf = reinterpret_cast<float *>(hc + (size_t)a.G * E);        // [G][E] float prefix
+  for (uint32_t b = tid; b < nk * E; b += kThreads) { hs[b] = 0; hc[b] = 0; }
   __syncthreads();
   const double scale = ldexp(1.0, sx);
-  const uint64_t nbS = (uint64_t)nb * a.S;
+  const uint64_t nbS = (uint64_t)a.nb * S;
   long long stot = 0;
-  for (uint32_t i = tid; i < cv.n; i += kThreads) {
+  for (uint32_t i = tid; i < cv.n && off_ok; i += kThreads) {
     const size_t idx = cv.off + (size_t)i * cv.stride;
     const float t = a.t[idx], x = a.x[idx];
-    if (!valid(t, x, off)) continue;
-    const long long xq = __double2ll_rn(((double)x - off) * scale);
+    if (!valid(t, x)) continue;
+    const long long xq = quantise(x, cv.offset, sx);
     stot += xq;
-    const unsigned long long ph = frac64(t, cv.fmin) + (unsigned long long)J * frac64(t, dfK) - shift;
-    const uint64_t fb = __umul64hi(ph - lo, nbS);  // fine bin from the neighbourhood start
-    if (fb < LS) {
-      atomicAdd(reinterpret_cast<unsigned long long *>(hs + fb), (unsigned long long)xq);
-      atomicAdd(hc + fb, 1);
+    const unsigned long long bp = frac64(t, dfK);
+    unsigned long long ph = frac64(t, cv.fmin) + (unsigned long long)J0 * bp - shift0 - lo;
+    const unsigned long long step = bp - Rp;
+    for (uint32_t g = 0; g < nk; ++g, ph += step) {
+      const uint64_t fb = __umul64hi(ph, nbS);  // fine bin from the neighbourhood start
+      if (fb < LS) {
+        atomicAdd(reinterpret_cast<unsigned long long *>(hs + (size_t)g * E + fb), (unsigned long long)xq);
+        atomicAdd(hc + (size_t)g * E + fb, 1);
+      }
     }
   }
   stot = block_sum<long long>(stot, shl);
   __syncthreads();
-  // exclusive prefix over the fine bins, in place (LS + 1 entries): one thread, the bins are few
-  if (tid == 0) {
-    long long ps = 0;
-    int pc = 0;
-    for (uint32_t b = 0; b <= LS; ++b) {
-      const long long vs = hs[b];
-      const int vc = hc[b];
-      hs[b] = ps;
-      hc[b] = pc;
-      ps += vs;
-      pc += vc;
+  // ---- exclusive prefix sums, one warp per trial: each lane a run of entries, a warp scan of
+  // the runs' totals; the float copy (real flux units) and its largest magnitude for stage 1
+  const uint32_t run = (E + 31) / 32;
+  for (uint32_t g = warp; g < nk; g += kThreads / 32) {
+    long long *H = hs + (size_t)g * E;
+    int *C = hc + (size_t)g * E;
+    const uint32_t b0 = lane * run, b1 = min(E, b0 + run);
+    long long ls = 0;
+    int lc = 0;
+    for (uint32_t b = b0; b < b1; ++b) { ls += H[b]; lc += C[b]; }
+    long long es = ls;
+    int ec = lc;
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long us = __shfl_up_sync(0xffffffffu, es, o);
+      const int uc = __shfl_up_sync(0xffffffffu, ec, o);
+      if (lane >= o) { es += us; ec += uc; }
     }
+    es -= ls;
+    ec -= lc;
+    float pm = 0.0f;
+    for (uint32_t b = b0; b < b1; ++b) {
+      const long long vs = H[b];
+      const int vc = C[b];
+      H[b] = es;
+      C[b] = ec;
+      const float v = ldexpf(__ll2float_rn(es), -sx);
+      pf[(size_t)g * E + b] = v;
+      pm = fmaxf(pm, fabsf(v));
+      es += vs;
+      ec += vc;
+    }
+    for (int o = 16; o > 0; o >>= 1) pm = fmaxf(pm, __shfl_xor_sync(0xffffffffu, pm, o));
+    if (lane == 0) pmax_s[g] = pm;
   }
   __syncthreads();
 
-  // ---- windows [ws, we) in fine bins.  Stage 1: every window of whole bins inside the
-  // neighbourhood (width in (kmi, kma] bins); stage 2: fine edges within one bin of the
-  // stage-1 window's edges (width in (kmi S, kma S] fine bins).
-  const uint32_t S = a.S;
+  // ---- per trial: stage 1, every window of whole bins in the neighbourhood (width in
+  // (kmi, kma] bins), then stage 2, fine edges within one bin of the stage-1 window's edges
+  // (width in (kmi S, kma S] fine bins).  Stage 1 screens in FP32 with error bounds: windows
+  // whose upper bound reaches the largest lower bound are compared exactly in FP64.
   const double N = (double)cv.ntrue;
+  const float Nf = (float)cv.ntrue;
   const int kkmi = (int)(cv.kkmi < 5u ? 5u : cv.kkmi);
-  auto power = [&](uint32_t ws, uint32_t we, double &pw) -> bool {
-    const int kk = hc[we] - hc[ws];
-    if (kk <= kkmi) return false;
-    const double den = (double)kk * (N - (double)kk);
-    if (!(den > 0.0)) return false;
-    const double sv = (double)(hs[we] - hs[ws]) / scale;
-    pw = sv * sv / den;
-    return true;
-  };
+  const uint32_t kmaL = a.kma < L ? a.kma : L;
+  const uint32_t nw1 = L * kmaL;
   __shared__ double wp[kThreads / 32];
   __shared__ uint32_t wa[kThreads / 32], wb[kThreads / 32];
   auto block_best = [&](double &bp, uint32_t &ba, uint32_t &bb) {  // fixed-order argmax
@@ -249,49 +291,90 @@ __global__ void __launch_bounds__(kThreads) refine_trial_kernel(const RefArgs a)
       if (better(op, oa, ob, bp, ba, bb)) { bp = op; ba = oa; bb = ob; }
     }
     __syncthreads();
-    if ((tid & 31) == 0) { wp[tid >> 5] = bp; wa[tid >> 5] = ba; wb[tid >> 5] = bb; }
+    if (lane == 0) { wp[warp] = bp; wa[warp] = ba; wb[warp] = bb; }
     __syncthreads();
     bp = wp[0]; ba = wa[0]; bb = wb[0];
     for (int w = 1; w < kThreads / 32; ++w)
       if (better(wp[w], wa[w], wb[w], bp, ba, bb)) { bp = wp[w]; ba = wa[w]; bb = wb[w]; }
   };
-  double bp = -1.0;
-  uint32_t ba = UINT_MAX, bb = UINT_MAX;
-  const uint32_t kma = a.kma < L ? a.kma : L;
-  for (uint32_t q = tid; q < L * kma; q += kThreads) {
-    const uint32_t ac = q / kma, w = q - ac * kma + 1;
-    if (w <= a.kmi || ac + w > L) continue;
-    double pw;
-    if (power(ac * S, (ac + w) * S, pw) && better(pw, ac * S, (ac + w) * S, bp, ba, bb)) {
-      bp = pw; ba = ac * S; bb = (ac + w) * S;
+  for (uint32_t g = 0; g < nk; ++g) {
+    const long long *H = hs + (size_t)g * E;
+    const int *C = hc + (size_t)g * E;
+    const float *P = pf + (size_t)g * E;
+    // |P - exact| <= 2^-24 |exact| per entry, so a difference is off by at most 2^-23 pmax
+    // plus 2^-24 of itself (both taken twice here); den is exact to 2^-24 and the quotient
+    // from __fdividef within 2 ulp, inside the 2^-20 factors
+    const float e0 = ldexpf(pmax_s[g], -22);
+    auto power = [&](uint32_t ws, uint32_t we, double &pw) -> bool {
+      const int kk = C[we] - C[ws];
+      if (kk <= kkmi) return false;
+      const double den = (double)kk * (N - (double)kk);
+      if (!(den > 0.0)) return false;
+      const double sv = (double)(H[we] - H[ws]) / scale;
+      pw = sv * sv / den;
+      return true;
+    };
+    auto bounds = [&](uint32_t ws, uint32_t we, float &plo, float &phi) -> bool {
+      const int kk = C[we] - C[ws];
+      if (kk <= kkmi) return false;
+      const float den = (float)kk * (Nf - (float)kk);
+      if (!(den > 0.0f)) return false;
+      const float sv = fabsf(P[we] - P[ws]);
+      const float err = e0 + ldexpf(sv, -22);
+      const float lo_ = fmaxf(sv - err, 0.0f), hi_ = sv + err;
+      plo = __fdividef(lo_ * lo_, den) * (1.0f - 1.0f / 1048576.0f);
+      phi = __fdividef(hi_ * hi_, den) * (1.0f + 1.0f / 1048576.0f);
+      return true;
+    };
+    // (a float prefix near the underflow range would break the bounds: no screening there)
+    float thr = 0.0f;
+    for (uint32_t q = tid; q < nw1 && sx < 100; q += kThreads) {
+      const uint32_t ac = q / kmaL, w = q - ac * kmaL + 1;
+      if (w <= a.kmi || ac + w > L) continue;
+      float plo, phi;
+      if (bounds(ac * S, (ac + w) * S, plo, phi)) thr = fmaxf(thr, plo);
     }
-  }
-  block_best(bp, ba, bb);
-  if (ba != UINT_MAX) {
-    const uint32_t a0 = ba > S ? ba - S : 0u, a1 = ba + S < LS ? ba + S : LS;
-    const uint32_t b0 = bb > S ? bb - S : 0u, b1 = bb + S < LS ? bb + S : LS;
-    const uint32_t na = a1 - a0 + 1, nbw = b1 - b0 + 1;
-    const uint32_t wmin = a.kmi * S, wmax = a.kma * S;
-    for (uint32_t q = tid; q < na * nbw; q += kThreads) {
-      const uint32_t ws = a0 + q / nbw, we = b0 + (q - (q / nbw) * nbw);
-      if (we <= ws || we - ws <= wmin || we - ws > wmax) continue;
+    thr = block_max(thr, shf);
+    double bp = -1.0;
+    uint32_t ba = UINT_MAX, bb = UINT_MAX;
+    for (uint32_t q = tid; q < nw1; q += kThreads) {
+      const uint32_t ac = q / kmaL, w = q - ac * kmaL + 1;
+      if (w <= a.kmi || ac + w > L) continue;
+      float plo, phi;
+      if (!bounds(ac * S, (ac + w) * S, plo, phi) || phi < thr) continue;
       double pw;
-      if (power(ws, we, pw) && better(pw, ws, we, bp, ba, bb)) { bp = pw; ba = ws; bb = we; }
+      if (power(ac * S, (ac + w) * S, pw) && better(pw, ac * S, (ac + w) * S, bp, ba, bb)) {
+        bp = pw; ba = ac * S; bb = (ac + w) * S;
+      }
     }
     block_best(bp, ba, bb);
-  }
-  if (tid == 0) {
-    pt->pw = ba == UINT_MAX ? -1.0 : bp;
-    pt->s = ba == UINT_MAX ? 0 : hs[bb] - hs[ba];
-    pt->kk = ba == UINT_MAX ? 0u : (uint32_t)(hc[bb] - hc[ba]);
-    pt->a = ba;
-    pt->b = bb;
-    pt->stot = stot;
-    pt->nv = nv;
-    pt->j = j;
-    pt->p1 = (p1 + nb - M) & (nb - 1);  // neighbourhood start bin
-    pt->sx = sx;
-    pt->tref = tref;
+    if (ba != UINT_MAX) {
+      const uint32_t a0 = ba > S ? ba - S : 0u, a1 = ba + S < LS ? ba + S : LS;
+      const uint32_t b0 = bb > S ? bb - S : 0u, b1 = bb + S < LS ? bb + S : LS;
+      const uint32_t na = a1 - a0 + 1, nbw = b1 - b0 + 1;
+      const uint32_t wmin = a.kmi * S, wmax = a.kma * S;
+      for (uint32_t q = tid; q < na * nbw; q += kThreads) {
+        const uint32_t ws = a0 + q / nbw, we = b0 + (q - (q / nbw) * nbw);
+        if (we <= ws || we - ws <= wmin || we - ws > wmax) continue;
+        double pw;
+        if (power(ws, we, pw) && better(pw, ws, we, bp, ba, bb)) { bp = pw; ba = ws; bb = we; }
+      }
+      block_best(bp, ba, bb);
+    }
+    if (tid == 0) {
+      Part &o = pt[g];
+      o.pw = ba == UINT_MAX ? -1.0 : bp;
+      o.s = ba == UINT_MAX ? 0 : H[bb] - H[ba];
+      o.kk = ba == UINT_MAX ? 0u : (uint32_t)(C[bb] - C[ba]);
+      o.a = ba;
+      o.b = bb;
+      o.stot = stot;
+      o.nv = nv;
+      o.j = j;
+      o.p1 = (p1 + nb - M) & (nb - 1);  // neighbourhood start bin
+      o.sx = sx;
+      o.tref = tref;
+    }
   }
 }
 
@@ -375,9 +458,17 @@ int refine_common(RefArgs &a, uint32_t count, void *workspace, size_t workspace_
   a.lognb = gtrap::ilog2u(a.nb);
   a.logK = gtrap::ilog2u(a.K);
   a.part = reinterpret_cast<Part *>(workspace);
-  const size_t smem = (size_t)(kMaxFine + 1) * (sizeof(long long) + sizeof(int));
+  // trials per block: as many fine histograms (16 bytes an entry) as fit the block's budget
+  const size_t per_trial = (size_t)((a.kma + 2 * a.M) * a.S + 1) * 16;
+  uint32_t G = (uint32_t)(kSmemBudget / per_trial);
+  if (G < 1) G = 1;
+  if (G > (uint32_t)kMaxGroup) G = kMaxGroup;
+  if (G > 2 * a.K + 1) G = 2 * a.K + 1;
+  a.G = G;
+  const size_t smem = (size_t)G * per_trial;
   GTRAP_TRY(gtrap::ensure_smem((const void *)refine_trial_kernel, smem, name));
-  refine_trial_kernel<<<dim3(count, 2 * a.K + 1), kThreads, smem, stream>>>(a);
+  const uint32_t groups = (2 * a.K + 1 + G - 1) / G;
+  refine_trial_kernel<<<dim3(count, groups), kThreads, smem, stream>>>(a);
   GTRAP_TRY(gtrap::check_launch("refine_trial_kernel"));
   refine_pick_kernel<<<(count + 3) / 4, 128, 0, stream>>>(a, count);
   return gtrap::check_launch("refine_pick_kernel");

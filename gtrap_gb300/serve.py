@@ -416,8 +416,14 @@ class TransitServer:
         d = hb.to(self.dev, non_blocking=True)
         return d[:arr.nbytes].view(torch.int64 if arr.dtype == np.int64 else torch.int32)
 
-    def _take(self, live, budget):
-        segs, counts = [], []
+    def _take(self, live, budget, cost):
+        """Tiles of the oldest in-flight requests for one step.  When the work left is several
+        steps' worth the budget grows (up to 4x: fewer, longer steps amortise each launch's
+        tail); the step's segments are ordered by their tiles' cost (``cost`` of the request,
+        its sample count or scoop size) so the persistent blocks start on the longest tiles."""
+        left_all = sum(max(0, lv.tiles - lv.next_tile) for lv in live)
+        budget *= int(min(4, max(1, left_all // (2 * budget)))) if budget > 0 else 1
+        segs, counts, keys = [], [], []
         for lv in live:
             if budget <= 0:
                 break
@@ -427,8 +433,12 @@ class TransitServer:
             c = min(left, budget)
             segs.append((lv.desc, lv.next_tile))
             counts.append(c)
+            keys.append(cost(lv))
             lv.next_tile += c
             budget -= c
+        order = sorted(range(len(segs)), key=lambda k: -keys[k])
+        segs = [segs[k] for k in order]
+        counts = [counts[k] for k in order]
         sg = np.array(segs, SEGMENT) if segs else np.zeros(0, SEGMENT)
         cum = np.zeros(len(counts) + 1, np.uint32)
         if counts:
@@ -446,9 +456,9 @@ class TransitServer:
         self.live_bls += [lv for lv in new if lv.req.kind == "bls"]
         self.live_fold += [lv for lv in new if lv.req.kind == "fold"]
         self.live_tls += [lv for lv in new if lv.req.kind == "tls"]
-        bls_segs = self._take(self.live_bls, self.bls_tiles)
-        fold_segs = self._take(self.live_fold, self.fold_tiles)
-        tls_segs = self._take(self.live_tls, self.tls_tiles)
+        bls_segs = self._take(self.live_bls, self.bls_tiles, lambda lv: lv.req.n)
+        fold_segs = self._take(self.live_fold, self.fold_tiles, lambda lv: lv.req.n)
+        tls_segs = self._take(self.live_tls, self.tls_tiles, lambda lv: lv.req.nsc)
         if not new and not len(bls_segs[0]) and not len(tls_segs[0]) and not len(fold_segs[0]):
             return done
         si = self.step_count
@@ -556,7 +566,7 @@ class TransitServer:
                     bufs = step.bstats[lv.req.kind]
                     for t_ in bufs:
                         t_.record_stream(self.d2h)
-                    srcs = [b_[lv.st_slot:lv.st_slot + 1] for b_ in bufs]
+                    srcs = [b_[lv.st_slot:lv.st_slot + 1].reshape(-1) for b_ in bufs]
                 elif lv.req.kind == "tls" and lv.pk_slot >= 0:
                     st_, idx, val = step.peaks
                     for t_ in step.peaks:  # keep the buffers until the copies have run

@@ -146,7 +146,9 @@ def test_fold_requests_mixed_equal_plain(solo):
 
 def test_server_returns_spectrum_stats(solo, cuda):
     """With spectrum_stats, a BLS request returns get_blsstat's record of its spectrum, equal to
-    the image entry point on the solo run's spectrum; other requests are unchanged."""
+    the image entry point on the solo run's spectrum, with the refined best peak beside it
+    (its equality with the image refinement is tested in test_gpu_refine); other requests are
+    unchanged."""
     from gtrap_gb300 import api
     reqs, ref = solo
     srv = _server(spectrum_stats=True)
@@ -160,10 +162,13 @@ def test_server_returns_spectrum_stats(solo, cuda):
             continue
         nbls += 1
         rec = res[rid].outputs
-        assert rec.dtype == api.BLS_STATS
+        assert rec.dtype == api.BLS_STATS_REFINED
         w = [x.cpu().numpy()[0] for x in api.blsstat(d(ref[k][0]), d(ref[k][1]), d(ref[k][2]), reqs[k].df,
                                                      reqs[k].fmin)]
         assert (rec["pest"], rec["sde"], rec["ph1"], rec["ph2"]) == tuple(w), k
+        r = rec["refined"]
+        assert r["jgrid"] == int(np.argmax(ref[k][0])) and r["sr_grid"] == ref[k][0].max()
+        assert r["sr"] >= r["sr_grid"] * (1 - 1e-6)
     assert nbls >= 2
     # folded requests: the record of (tsr, start, duration index) of the plain per-request run
     curves = synth.ragged_mix(3, seed=5200, n_range=(500, 3000))
