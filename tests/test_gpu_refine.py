@@ -141,3 +141,55 @@ def test_refine_rejects_bad_grids(cuda):
         with pytest.raises(N.GtrapError, match=msg):
             api.bls_refine(d.view(1, 16), z.view(1, 16), z.view(1, 16), d.view(16, 1), d.view(16, 1), d[:1], z[:1],
                            args["nb"], args["kma"], 5, 10, 0.1, 0.01, K=args["K"], S=args["S"], M=2)
+
+
+@pytest.mark.parametrize("seed,nb,kma,kmi,n,cadence", [(81, 1024, 103, 5, 6000, 0.0204), (82, 2048, 205, 10, 9000, 0.0204),
+                                                     (83, 512, 52, 2, 4000, 0.00139), (84, 2048, 100, 20, 7000, 0.00139)])
+def test_refine_grids_and_cadences_match_oracle(cuda, seed, nb, kma, kmi, n, cadence):
+    """Bin grids, window limits and cadences (29.4 and 2 minutes), boxes at random phases
+    (some windows wrap past the last bin), against the oracle."""
+    rng = np.random.default_rng(seed)
+    nq = 3
+    t = np.empty((n, nq), np.float32)
+    lc = np.empty((n, nq), np.float32)
+    for q in range(nq):
+        tt = (np.arange(n) * cadence + rng.uniform(0, 0.5)).astype(np.float64)
+        per = rng.uniform(0.3, 0.25 * n * cadence)
+        ep = rng.uniform(0, per)
+        dur = per * rng.uniform(0.01, 0.08)
+        x = rng.normal(0, 5e-4, n) - 2e-3 * (np.mod(tt - ep, per) < dur)
+        g0 = rng.integers(0, n - n // 10)
+        tt[g0:g0 + n // 10] = -1000.0
+        t[:, q], lc[:, q] = tt.astype(np.float32), x.astype(np.float32)
+    ntrue = (t >= 0).sum(axis=0).astype(np.uint32)
+    off = oracle.offset(lc, t).astype(np.float32)
+    T = float(n * cadence)
+    nf = 300
+    fmin = np.float32(1.0 / T)
+    df = np.float32((2.0 / cadence / 20 - fmin) / (nf - 1))
+    g = dict(nf=nf, nb=nb, kma=kma, kmi=kmi, kkmi=int(n * 0.002), fmin=float(fmin), df=float(df))
+    sr, p1, p2, recs = _search_and_refine(lc, t, ntrue, off, g, cuda)
+    for q in range(nq):
+        o = OR.refine_curve(t[:, q], lc[:, q], off[q], ntrue[q], sr[q], p1[q], p2[q], g["fmin"], g["df"],
+                            nb, kma, kmi, g["kkmi"], K=KR, S=SR_, M=MR)
+        _check(recs[q], o)
+
+
+def test_refine_degenerate_curves(cuda):
+    """No positive grid peak (flat flux), a curve with every sample masked and a one-frequency
+    grid give zero records or the oracle's record."""
+    n, nq = 3000, 3
+    t = np.tile((np.arange(n) * np.float32(0.0204)).astype(np.float32)[:, None], (1, nq))
+    lc = np.random.default_rng(90).normal(0, 1e-3, (n, nq)).astype(np.float32)
+    lc[:, 0] = 0.0                     # flat: every window has zero power
+    t[:, 1] = -1000.0                  # every sample masked
+    ntrue = (t >= 0).sum(axis=0).astype(np.uint32)
+    off = np.zeros(nq, np.float32)
+    for nf in (1, 40):
+        g = dict(nf=nf, nb=1024, kma=103, kmi=5, kkmi=10, fmin=0.05, df=0.01)
+        sr, p1, p2, recs = _search_and_refine(lc, t, ntrue, off, g, cuda)
+        assert recs[0]["sr"] == 0.0 and recs[0]["freq"] == 0.0
+        assert recs[1]["sr"] == 0.0 and recs[1]["kk"] == 0
+        o = OR.refine_curve(t[:, 2], lc[:, 2], off[2], ntrue[2], sr[2], p1[2], p2[2], g["fmin"], g["df"],
+                            1024, 103, 5, 10, K=KR, S=SR_, M=MR)
+        _check(recs[2], o)

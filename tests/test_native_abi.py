@@ -164,6 +164,22 @@ def test_new_entry_points_validate_on_the_host(lib, no_device):
     assert lib.gtrap_trend(P, P, 0, 5.0, 0.0, 1.0, 0, None) == 0  # nothing to do
     assert lib.gtrap_trend(None, P, 4, 5.0, 0.0, 1.0, 0, None) == _native.ERR_INVALID_ARG
     assert lib.gtrap_blsstat_packed(None, P, P, P, None, 3, 0, P, P, P, P, None) == _native.ERR_INVALID_ARG
+    # best-peak refinement: grid and workspace checks on the host
+    def rf(nb=1024, kma=103, K=32, S=8, M=8, wsp=ws, nbytes=1 << 40, out=P):
+        return lib.gtrap_bls_refine(P, P, P, P, P, P, P, 1000, 2, 16, nb, kma, 5, 10, 0.1, 0.01, K, S, M, out, wsp,
+                                    nbytes, None)
+    assert rf(nb=1000) == _native.ERR_INVALID_ARG and b"power of two" in lib.gtrap_last_error()
+    assert rf(K=3) == _native.ERR_INVALID_ARG
+    assert rf(S=0) == _native.ERR_INVALID_ARG
+    assert rf(M=65) == _native.ERR_INVALID_ARG
+    assert rf(kma=600, S=8) == _native.ERR_INVALID_ARG and b"fine bins" in lib.gtrap_last_error()
+    assert rf(out=None) == _native.ERR_INVALID_ARG
+    assert rf(nbytes=64) == _native.ERR_WORKSPACE
+    assert rf(wsp=C.c_void_p(257)) == _native.ERR_WORKSPACE
+    assert lib.gtrap_bls_refine_workspace_size(10, 32) >= 10 * 65 * 56
+    assert lib.gtrap_bls_refine_packed(P, P, P, P, None, 0, P, P, 1024, 103, 5, 32, 8, 8, P, P, 1 << 40, None) == 0
+    assert lib.gtrap_bls_refine_packed(P, P, P, None, None, 3, P, P, 1024, 103, 5, 32, 8, 8, P, P, 1 << 40,
+                                       None) == _native.ERR_INVALID_ARG
     assert lib.gtrap_blsstat_packed(P, P, P, None, None, 3, 0, P, P, P, P, None) == _native.ERR_INVALID_ARG
 
     rec = np.zeros(1, api.TRANSIT_PARAMS)
