@@ -184,3 +184,42 @@ def test_server_returns_spectrum_stats(solo, cuda):
                                                      folds[k].fmin)]
         rec = res[rid].outputs
         assert (rec["pest"], rec["sde"], rec["ph1"], rec["ph2"]) == tuple(w), k
+
+
+def test_served_results_match_the_oracle(cuda):
+    """Requests served in a mix (arriving while others run) against the FP64 oracles directly,
+    each from its raw curve through scipy's median filter: BLS SR within 1e-4 with identical
+    or tie-equivalent bins (the offset is get_offset of the oracle's residual), GTLS S/N within
+    1e-4 (relative, absolute below 1) with identical epoch times."""
+    import oracle
+    reqs = _requests(count=8, seed=5400)
+    assert {r.kind for r in reqs} == {"bls", "tls"}
+    srv = _server()
+    rids = [srv.submit(r) for r in reqs[:3]]
+    srv.step()
+    rids += [srv.submit(r) for r in reqs[3:]]
+    res = {r.rid: r for r in srv.run_until_idle()}
+    for k, rid in enumerate(rids):
+        r = reqs[k]
+        t = np.asarray(r.t, np.float32)[:, None]
+        resid = oracle.medfilt_residual(np.asarray(r.x, np.float32)[:, None], R)
+        out = res[rid].outputs
+        if r.kind == "bls":
+            off = oracle.offset(resid, t).astype(np.float32)
+            ntrue = np.array([int((t >= 0).sum())], np.uint32)
+            kkmi = r.kkmi if r.kkmi is not None else int(r.n * 0.005)
+            osr, op1, op2, opmax = oracle.bls(resid, t, r.nf, BLS.nb, BLS.kma, BLS.kmi, kkmi, r.fmin, r.df,
+                                              offset=off, ntrue=ntrue)
+            sr, p1, p2 = out
+            fin = np.isfinite(osr[0])
+            rel = np.abs(sr[fin] - osr[0][fin]) / np.maximum(osr[0][fin], 1e-30)
+            assert rel.max() <= 1e-4, (k, rel.max())
+            for j in np.flatnonzero(((p1 != op1[0]) | (p2 != op2[0])) & fin):
+                pw = oracle.bls_window_power(resid, t, 0, j, int(p1[j]), int(p2[j]), BLS.nb, r.fmin, r.df,
+                                             offset=off, ntrue=ntrue)
+                assert abs(pw - opmax[0, j]) <= 1e-5 * opmax[0, j], (k, j)
+        else:
+            ref = oracle.gtls(resid, t, r.n, TLS.nw, TLS.nl, r.nsc, r.wmax, r.dw, r.deltat)
+            err = np.abs(out[0] - ref[0][:, 0]) / np.maximum(np.abs(ref[0][:, 0]), 1.0)
+            assert err.max() <= 1e-4, (k, err.max())
+            np.testing.assert_array_equal(out[2], ref[2][:, 0])
