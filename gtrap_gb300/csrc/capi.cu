@@ -120,4 +120,18 @@ const char *gtrap_last_error(void) { return gtrap::g_last_error; }
 
 int gtrap_version(void) { return 100; /* 0.1.0 */ }
 
+int gtrap_copy_async(const gtrap_copy *copies, uint32_t count, gtrap_stream_t stream) {
+  if (count == 0) return GTRAP_OK;
+  if (!copies) return gtrap::fail(GTRAP_ERR_INVALID_ARG, "copy_async: null copy list");
+  for (uint32_t k = 0; k < count; ++k) {
+    if (copies[k].bytes == 0) continue;
+    if (!copies[k].dst || !copies[k].src)
+      return gtrap::fail(GTRAP_ERR_INVALID_ARG, "copy_async: null pointer in copy %u", k);
+    const cudaError_t e = cudaMemcpyAsync(copies[k].dst, copies[k].src, copies[k].bytes, cudaMemcpyDefault, stream);
+    if (e != cudaSuccess)
+      return gtrap::fail(GTRAP_ERR_CUDA, "copy_async: copy %u of %u: %s", k, count, cudaGetErrorString(e));
+  }
+  return GTRAP_OK;
+}
+
 }  // extern "C"

@@ -45,6 +45,7 @@ from ._dev import as_ptr, require_cuda
 SAMPLE_BYTES = 32   # t, x, detrended x (4 B each) + quantised flux (4 B) + phase pair (16 B)
 OUTPUT_BYTES = 20   # five float32/int32 output arrays per output element
 ALIGN = 32          # arena granularity (elements)
+META_SLOT_BYTES = 4 << 20   # device metadata of one step (larger steps allocate their own)
 
 
 @dataclass
@@ -175,6 +176,24 @@ class _Staging:
         return self.cur[start:start + nbytes]
 
 
+class _Copies:
+    """Copies collected for one ``gtrap_copy_async`` call (one cudaMemcpyAsync each, in order):
+    a step's many small copies cost one native call instead of one framework call each."""
+
+    def __init__(self):
+        self.items = []
+
+    def add(self, dst: int, src: int, nbytes: int):
+        if nbytes:
+            self.items.append((int(dst), int(src), int(nbytes)))
+
+    def issue(self, stream_handle: int):
+        if self.items:
+            arr = np.array(self.items, dtype=np.uint64)   # gtrap_copy rows: dst, src, bytes
+            N.call("gtrap_copy_async", arr.ctypes.data, len(self.items), stream_handle)
+            self.items = []
+
+
 @dataclass
 class _Live:
     rid: int
@@ -256,6 +275,9 @@ class TransitServer:
                           3 * max_requests * 64)
         self.stream = torch.cuda.Stream(d)
         self.staging = _Staging(self.depth)
+        # device copies of each step's metadata, one slot per step of the pipeline depth (the
+        # slot a step fills was last read by a step that has finished, as for the staging)
+        self.meta_dev = [torch.empty(META_SLOT_BYTES, dtype=torch.uint8, device=d) for _ in range(self.depth)]
         self.h2d = torch.cuda.Stream(d)
         self.d2h = torch.cuda.Stream(d)
         self.waiting: collections.deque = collections.deque()
@@ -327,37 +349,39 @@ class TransitServer:
             new.append(lv)
         return new
 
-    def _upload_samples(self, new):
+    def _upload_samples(self, new, keep):
         """Copy the new curves' samples (pinned staging, copy stream); returns the event the
         compute stream waits for."""
         total = sum(lv.req.n for lv in new)
-        th = self.staging.take(4 * total).view(torch.float32)
-        xh = self.staging.take(4 * total).view(torch.float32)
-        tn, xn = th.numpy(), xh.numpy()
+        th = self.staging.take(4 * total)
+        xh = self.staging.take(4 * total)
+        keep += [th, xh]
+        tn, xn = th.numpy().view(np.float32), xh.numpy().view(np.float32)
+        cp = _Copies()
         p = 0
-        spans = []
+        tb, xb = th.data_ptr(), xh.data_ptr()
+        td, xd = self.t.data_ptr(), self.x.data_ptr()
         for lv in new:
             n = lv.req.n
             tn[p:p + n] = lv.req.t
             xn[p:p + n] = lv.req.x
-            spans.append((p, lv.soff, n))
+            cp.add(td + 4 * lv.soff, tb + 4 * p, 4 * n)
+            cp.add(xd + 4 * lv.soff, xb + 4 * p, 4 * n)
             p += n
         # Slots are freed only after the last step reading them has finished, so the copy
         # need not wait for the compute stream and overlaps the steps in flight.
-        with torch.cuda.stream(self.h2d):
-            for a, s, n in spans:
-                self.t[s:s + n].copy_(th[a:a + n], non_blocking=True)
-                self.x[s:s + n].copy_(xh[a:a + n], non_blocking=True)
+        cp.issue(self.h2d.cuda_stream)
         ev = torch.cuda.Event()
         ev.record(self.h2d)
         return ev
 
-    def _meta(self, new, bls_segs, tls_segs, fold_segs):
-        """One pinned buffer with the step's descriptor rows, detrend list and work queues."""
+    def _meta(self, si, new, bls_segs, tls_segs, fold_segs, extra, keep):
+        """The step's descriptor rows, detrend list, work queues and the index arrays of its
+        statistics (``extra``) in one pinned block, copied on the compute stream into the
+        step's device metadata slot; returns device views of the arrays, then nb, nt, nfd."""
         nb = [lv for lv in new if lv.req.kind == "bls"]
         nt = [lv for lv in new if lv.req.kind == "tls"]
         nfd = [lv for lv in new if lv.req.kind == "fold"]
-        parts = []
         g_off = np.array([lv.soff for lv in new], np.uint64)
         g_n = np.array([lv.req.n for lv in new], np.uint32)
         bt = np.zeros(len(nb), BLS_CURVE)
@@ -377,44 +401,48 @@ class TransitServer:
         bsg, bcum = bls_segs
         tsg, tcum = tls_segs
         fsg, fcum = fold_segs
-        for arr in (g_off, g_n, bsg, bcum, tsg, tcum, fsg, fcum):
-            parts.append(np.frombuffer(arr.tobytes(), np.uint8))
+        arrays = [g_off, g_n, bsg, bcum, tsg, tcum, fsg, fcum] + list(extra)
+        rows = [(bt, self.bls_table, nb, BLS_CURVE), (tt, self.tls_table, nt, TLS_CURVE),
+                (ft, self.fold_table, nfd, BLS_CURVE)]
         offs, p = [], 0
-        for a in parts:
+        for a in arrays:
             offs.append(p)
-            p += (a.size + 255) // 256 * 256
+            p += (a.nbytes + 255) // 256 * 256
+        arrays_end = p
+        roffs = []
+        for r_, _, _, _ in rows:
+            roffs.append(p)
+            p += (r_.nbytes + 255) // 256 * 256
         host = self.staging.take(max(p, 256))
+        keep.append(host)
         hn = host.numpy()
-        for a, o in zip(parts, offs):
-            hn[o:o + a.size] = a
-        devbuf = host.to(self.dev, non_blocking=True)   # on self.stream (current)
-        base = devbuf.data_ptr()
+        for a, o in zip(arrays, offs):
+            hn[o:o + a.nbytes] = np.frombuffer(a.tobytes(), np.uint8)
+        for (r_, _, _, _), o in zip(rows, roffs):
+            hn[o:o + r_.nbytes] = np.frombuffer(r_.tobytes(), np.uint8)
+        slot = self.meta_dev[si % len(self.meta_dev)]
+        if arrays_end > slot.numel():
+            slot = torch.empty(arrays_end, dtype=torch.uint8, device=self.dev)   # compute stream
+            keep.append(slot)
+        cp = _Copies()
+        hb, db = host.data_ptr(), slot.data_ptr()
+        cp.add(db, hb, arrays_end)
         # descriptor rows go straight to their slots (new requests get consecutive slots
         # when the descriptor arena is not fragmented; otherwise one copy per row)
-        for rows, table, live, dt in ((bt, self.bls_table, nb, BLS_CURVE), (tt, self.tls_table, nt, TLS_CURVE),
-                                      (ft, self.fold_table, nfd, BLS_CURVE)):
-            if not len(rows):
+        for (r_, table, live, dt), o in zip(rows, roffs):
+            if not len(r_):
                 continue
-            rb = np.frombuffer(rows.tobytes(), np.uint8)
-            hb = self.staging.take(rb.size)
-            hb.numpy()[:] = rb
             sz = dt.itemsize
             slots = [lv.desc for lv in live]
+            tb = table.data_ptr()
             if slots == list(range(slots[0], slots[0] + len(slots))):
-                table[slots[0] * sz:(slots[0] + len(slots)) * sz].copy_(hb, non_blocking=True)
+                cp.add(tb + slots[0] * sz, hb + o, len(slots) * sz)
             else:
                 for k, sl in enumerate(slots):
-                    table[sl * sz:(sl + 1) * sz].copy_(hb[k * sz:(k + 1) * sz], non_blocking=True)
-        return devbuf, [base + o for o in offs], nb, nt, nfd
-
-    def _upload_small(self, values, dtype):
-        """A small index array through the step's pinned staging slot (no per-step pinned
-        allocation); the copy runs on the current stream."""
-        arr = np.ascontiguousarray(values, dtype=dtype)
-        hb = self.staging.take(max(arr.nbytes, 8))
-        hb.numpy()[:arr.nbytes] = arr.view(np.uint8)
-        d = hb.to(self.dev, non_blocking=True)
-        return d[:arr.nbytes].view(torch.int64 if arr.dtype == np.int64 else torch.int32)
+                    cp.add(tb + sl * sz, hb + o + k * sz, sz)
+        cp.issue(self.stream.cuda_stream)
+        views = [slot[o:o + max(a.nbytes, 8)] for a, o in zip(arrays, offs)]
+        return views, nb, nt, nfd
 
     def _take(self, live, budget, cost):
         """Tiles of the oldest in-flight requests for one step.  When the work left is several
@@ -465,13 +493,28 @@ class TransitServer:
         self.step_count += 1
         self.staging.begin(si)
         st = self.stream
-        with torch.cuda.stream(st):
+        h = st.cuda_stream
+        keep = []   # pinned and device buffers the step's copies read: alive until it has run
+        # requests whose last tiles run in this step, and the index arrays of their statistics
+        fin_tls = [lv for lv in self.live_tls if lv.next_tile >= lv.tiles and lv.last_step < 0]
+        fin_tls = fin_tls if self.tls_peaks else []
+        fin_st = {}
+        if self.spectrum_stats:
+            for kind, live in (("bls", self.live_bls), ("fold", self.live_fold)):
+                fin = [lv for lv in live if lv.next_tile >= lv.tiles and lv.last_step < 0]
+                if fin:
+                    fin_st[kind] = fin
+        extra = []
+        if fin_tls:
+            extra += [np.array([lv.ooff for lv in fin_tls], np.int64), np.array([lv.req.n for lv in fin_tls], np.int32)]
+        for kind in fin_st:
+            extra.append(np.array([lv.desc for lv in fin_st[kind]], np.int32))
+        with torch.cuda.stream(st):   # the statistics' outputs are allocated on the compute stream
             if new:
-                ev = self._upload_samples(new)
+                ev = self._upload_samples(new, keep)
                 st.wait_event(ev)
-            devbuf, (p_goff, p_gn, p_bsg, p_bcum, p_tsg, p_tcum, p_fsg, p_fcum), nb, nt, nfd = \
-                self._meta(new, bls_segs, tls_segs, fold_segs)
-            h = st.cuda_stream
+            views, nb, nt, nfd = self._meta(si, new, bls_segs, tls_segs, fold_segs, extra, keep)
+            p_goff, p_gn, p_bsg, p_bcum, p_tsg, p_tcum, p_fsg, p_fcum = (v.data_ptr() for v in views[:8])
             if new:
                 N.call("gtrap_gfilter_packed", as_ptr(self.x), as_ptr(self.resid), p_goff, p_gn,
                        len(new), max(lv.req.n for lv in new), self.r, h)
@@ -509,38 +552,34 @@ class TransitServer:
                 N.call("gtrap_gtls_run", as_ptr(self.tls_table), p_tsg, p_tcum, len(tls_segs[0]),
                        as_ptr(self.t), as_ptr(self.resid), ts.nw, ts.nl, self.max_tls_nsc, ts.mode,
                        ts.flags, 0, as_ptr(self.counters[1:2]), *[as_ptr(a) for a in self.o], h)
-            fin_tls = [lv for lv in self.live_tls if lv.next_tile >= lv.tiles and lv.last_step < 0]
             pk = ()
-            if self.tls_peaks and fin_tls:
+            nx = 8
+            if fin_tls:
                 for j, lv in enumerate(fin_tls):
                     lv.pk_slot = j
-                po = self._upload_small([lv.ooff for lv in fin_tls], np.int64)
-                pn = self._upload_small([lv.req.n for lv in fin_tls], np.int32)
+                po = views[nx].view(torch.int64)[:len(fin_tls)]
+                pn = views[nx + 1].view(torch.int32)[:len(fin_tls)]
+                nx += 2
                 c = self.tls_peaks
                 pk = api.peakstat(self.o[0], po, pn, 1, max(lv.req.n for lv in fin_tls), c["mpd"],
                                   c["ntop"], c["k"], stream=st)
-            bst, sels = {}, []
-            if self.spectrum_stats:
-                for kind, live, table in (("bls", self.live_bls, self.bls_table),
-                                          ("fold", self.live_fold, self.fold_table)):
-                    fin = [lv for lv in live if lv.next_tile >= lv.tiles and lv.last_step < 0]
-                    if not fin:
-                        continue
-                    for j, lv in enumerate(fin):
-                        lv.st_slot = j
-                    sel = self._upload_small([lv.desc for lv in fin], np.int32)
-                    sels.append(sel)
-                    bst[kind] = api.blsstat_packed(self.o[0], self.o[1], self.o[2], table, sel, len(fin), stream=st)
-                    if kind == "bls":  # and the refined best peak (FP64 neighbourhood search)
-                        bs = self.bls_spec
-                        ref = api.bls_refine_packed(self.o[0], self.o[1], self.o[2], table, self.t, self.resid,
-                                                    bs.nb, bs.kma, bs.kmi, sel=sel, count=len(fin), stream=st)
-                        bst[kind] = bst[kind] + (ref.view(len(fin), api.BLS_REFINED.itemsize),)
+            bst = {}
+            for kind, fin in fin_st.items():
+                table = self.bls_table if kind == "bls" else self.fold_table
+                for j, lv in enumerate(fin):
+                    lv.st_slot = j
+                sel = views[nx].view(torch.int32)[:len(fin)]
+                nx += 1
+                bst[kind] = api.blsstat_packed(self.o[0], self.o[1], self.o[2], table, sel, len(fin), stream=st)
+                if kind == "bls":  # and the refined best peak (FP64 neighbourhood search)
+                    bs = self.bls_spec
+                    ref = api.bls_refine_packed(self.o[0], self.o[1], self.o[2], table, self.t, self.resid,
+                                                bs.nb, bs.kma, bs.kmi, sel=sel, count=len(fin), stream=st)
+                    bst[kind] = bst[kind] + (ref.view(len(fin), api.BLS_REFINED.itemsize),)
             ev = torch.cuda.Event()
             ev.record(st)
         step = _Step(si, ev, peaks=pk, bstats=bst)
-        step._sels = sels
-        step._keep = devbuf  # staging stays alive until the step has run
+        step._keep = keep
         for live in (self.live_bls, self.live_fold, self.live_tls):
             for lv in live:
                 if lv.next_tile >= lv.tiles and lv.last_step < 0:
@@ -559,36 +598,37 @@ class TransitServer:
         if not step.finishing:
             return
         self.d2h.wait_event(step.event)
-        with torch.cuda.stream(self.d2h):
-            for lv in step.finishing:
-                m, o = lv.req.outputs, lv.ooff
-                if lv.st_slot >= 0 and lv.req.kind in step.bstats:
-                    bufs = step.bstats[lv.req.kind]
-                    for t_ in bufs:
-                        t_.record_stream(self.d2h)
-                    srcs = [b_[lv.st_slot:lv.st_slot + 1].reshape(-1) for b_ in bufs]
-                elif lv.req.kind == "tls" and lv.pk_slot >= 0:
-                    st_, idx, val = step.peaks
-                    for t_ in step.peaks:  # keep the buffers until the copies have run
-                        t_.record_stream(self.d2h)
-                    rs = api.PEAK_STATS.itemsize
-                    srcs = (st_[lv.pk_slot * rs:(lv.pk_slot + 1) * rs], idx[lv.pk_slot], val[lv.pk_slot])
-                else:
-                    series = {"bls": 3, "fold": 4}.get(lv.req.kind, 5)
-                    srcs = [self.o[j][o:o + m] for j in range(series)]
-                # one pinned block for the request's outputs, one view per series
-                sizes = [(src.numel() * src.element_size() + 15) // 16 * 16 for src in srcs]
-                blk = torch.empty(sum(sizes), dtype=torch.uint8, pin_memory=True)
-                outs, o_ = [], 0
-                for src, sz in zip(srcs, sizes):
-                    h = blk[o_:o_ + src.numel() * src.element_size()].view(src.dtype)
-                    h.copy_(src, non_blocking=True)
-                    outs.append(h)
-                    o_ += sz
-                lv.result = tuple(outs)
-                ev = torch.cuda.Event()
-                ev.record(self.d2h)
-                lv.d2h_event = ev
+        for bufs in list(step.bstats.values()) + [step.peaks]:
+            for t_ in bufs:   # statistics buffers stay allocated until the copies have run
+                t_.record_stream(self.d2h)
+        cp = _Copies()
+        for lv in step.finishing:
+            m, o = lv.req.outputs, lv.ooff
+            if lv.st_slot >= 0 and lv.req.kind in step.bstats:
+                srcs = [b_[lv.st_slot:lv.st_slot + 1].reshape(-1) for b_ in step.bstats[lv.req.kind]]
+            elif lv.req.kind == "tls" and lv.pk_slot >= 0:
+                st_, idx, val = step.peaks
+                rs = api.PEAK_STATS.itemsize
+                srcs = (st_[lv.pk_slot * rs:(lv.pk_slot + 1) * rs], idx[lv.pk_slot], val[lv.pk_slot])
+            else:
+                series = {"bls": 3, "fold": 4}.get(lv.req.kind, 5)
+                srcs = [self.o[j][o:o + m] for j in range(series)]
+            # one pinned block for the request's outputs, one view per series
+            sizes = [(src.numel() * src.element_size() + 15) // 16 * 16 for src in srcs]
+            blk = torch.empty(sum(sizes), dtype=torch.uint8, pin_memory=True)
+            outs, o_ = [], 0
+            base = blk.data_ptr()
+            for src, sz in zip(srcs, sizes):
+                nbytes = src.numel() * src.element_size()
+                outs.append(blk[o_:o_ + nbytes].view(src.dtype))
+                cp.add(base + o_, src.data_ptr(), nbytes)
+                o_ += sz
+            lv.result = tuple(outs)
+        cp.issue(self.d2h.cuda_stream)
+        ev = torch.cuda.Event()
+        ev.record(self.d2h)
+        for lv in step.finishing:
+            lv.d2h_event = ev
         self.draining.extend(step.finishing)
 
     def poll(self) -> list:

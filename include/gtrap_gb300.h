@@ -54,6 +54,17 @@ enum gtrap_status {
 const char *gtrap_last_error(void);
 int gtrap_version(void); /* 10000*major + 100*minor + patch */
 
+/* Stream-ordered copies, one cudaMemcpyAsync each in list order (direction from the pointers:
+ * unified addressing; host memory should be pinned for the copies to be asynchronous).  One
+ * call issues the many small copies of a served step (samples, descriptor rows, work queues,
+ * results).  No counterpart in the reference, whose drivers copy with pycuda.driver. */
+typedef struct {
+  void *dst;
+  const void *src;
+  size_t bytes;
+} gtrap_copy;
+int gtrap_copy_async(const gtrap_copy *copies, uint32_t count, gtrap_stream_t stream);
+
 /* ---------------------------------------------------------------------------
  * Median-filter detrend.  Replaces the gfilter kernel (gtrap/gfilter.py:13-86)
  * launched by get_detrend (gtrap/gfilter.py:103-144):

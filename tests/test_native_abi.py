@@ -62,6 +62,17 @@ def test_validation_errors_need_no_gpu(lib, no_device):
     assert b"nw" in lib.gtrap_last_error()
 
 
+def test_copy_list_validation_needs_no_gpu(lib):
+    assert lib.gtrap_copy_async(None, 0, None) == 0                 # nothing to copy
+    assert lib.gtrap_copy_async(None, 3, None) == _native.ERR_INVALID_ARG
+    import numpy as np
+    rows = np.array([[0, 0, 16]], np.uint64)                        # null pointers, 16 bytes
+    assert lib.gtrap_copy_async(rows.ctypes.data, 1, None) == _native.ERR_INVALID_ARG
+    assert b"null pointer" in lib.gtrap_last_error()
+    rows[0, 2] = 0                                                  # empty copies are skipped
+    assert lib.gtrap_copy_async(rows.ctypes.data, 1, None) == 0
+
+
 def test_workspace_sizes_are_host_side(lib):
     a = lib.gtrap_geebls_workspace_size(65536, 1024, 0)
     b = lib.gtrap_geebls_workspace_size(65536, 1024, _native.BLS_PHASE_FP32_REF)
