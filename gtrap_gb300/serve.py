@@ -46,6 +46,7 @@ SAMPLE_BYTES = 32   # t, x, detrended x (4 B each) + quantised flux (4 B) + phas
 OUTPUT_BYTES = 20   # five float32/int32 output arrays per output element
 ALIGN = 32          # arena granularity (elements)
 META_SLOT_BYTES = 4 << 20   # device metadata of one step (larger steps allocate their own)
+_NO_SEGMENTS = (np.zeros(0, SEGMENT), np.zeros(1, np.uint32))   # an empty work queue
 
 
 @dataclass
@@ -449,6 +450,8 @@ class TransitServer:
         steps' worth the budget grows (up to 4x: fewer, longer steps amortise each launch's
         tail); the step's segments are ordered by their tiles' cost (``cost`` of the request,
         its sample count or scoop size) so the persistent blocks start on the longest tiles."""
+        if not live:
+            return _NO_SEGMENTS
         left_all = sum(max(0, lv.tiles - lv.next_tile) for lv in live)
         budget *= int(min(4, max(1, left_all // (2 * budget)))) if budget > 0 else 1
         segs, counts, keys = [], [], []
