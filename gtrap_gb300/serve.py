@@ -248,6 +248,7 @@ class TransitServer:
         self.fold_tiles = int(fold_tiles) if fold_tiles else sms * 2 * 8
         self.tls_tiles = int(tls_tiles) if tls_tiles else sms * 64
         self.depth = max(1, int(depth))
+        self.max_step_scale = 16  # a step's tile budget grows up to this factor under load
         self.tls_peaks = None if tls_peaks is None else dict(mpd=10, ntop=4, k=8) | dict(tls_peaks)
         self.spectrum_stats = bool(spectrum_stats)
         budget = int(hbm_budget)
@@ -447,13 +448,13 @@ class TransitServer:
 
     def _take(self, live, budget, cost):
         """Tiles of the oldest in-flight requests for one step.  When the work left is several
-        steps' worth the budget grows (up to 4x: fewer, longer steps amortise each launch's
-        tail); the step's segments are ordered by their tiles' cost (``cost`` of the request,
+        steps' worth the budget grows (up to ``max_step_scale`` times: fewer, longer steps
+        amortise each launch's tail); the step's segments are ordered by their tiles' cost (``cost`` of the request,
         its sample count or scoop size) so the persistent blocks start on the longest tiles."""
         if not live:
             return _NO_SEGMENTS
         left_all = sum(max(0, lv.tiles - lv.next_tile) for lv in live)
-        budget *= int(min(4, max(1, left_all // (2 * budget)))) if budget > 0 else 1
+        budget *= int(min(self.max_step_scale, max(1, left_all // (2 * budget)))) if budget > 0 else 1
         segs, counts, keys = [], [], []
         for lv in live:
             if budget <= 0:
