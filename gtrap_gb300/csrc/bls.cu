@@ -26,6 +26,8 @@
 //    division-free pre-test s^2 >= best' * den (best' = best*(1 - 2^-20)) admits every
 //    candidate that can tie or beat the running best; admitted candidates are compared
 //    exactly with a correctly rounded quotient and a lowest-(start, end) tie-break.
+#include <atomic>
+
 #include "common.cuh"
 
 #include <climits>
@@ -354,12 +356,24 @@ __device__ __forceinline__ bool better(float p, int i, int e, float bp, int bi, 
 template <int R, int MODE>
 __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
   extern __shared__ __align__(16) unsigned long long sm[];
-  __shared__ long long scan_x[kThreads / 32];
-  __shared__ int scan_c[kThreads / 32];
   __shared__ unsigned long long best_key[64];    // per frequency: best (power, -start, -end)
   __shared__ unsigned best_thr[64];              // per frequency: running best power (float bits)
-  __shared__ int scan_m[kThreads / 32];          // per-warp maximum bin count
-  __shared__ unsigned drop_cnt[64];              // FP32-phase samples landing on bin nb
+  // fold and prefix scratch, dead once the prefix pass has ended, shares its bytes with the
+  // scan's per-warp start-group statistics (the static total decides whether two blocks of
+  // F = 6 frequencies fit on an SM at nb = 2048)
+  __shared__ union {
+    struct {
+      long long x[kThreads / 32];
+      int c[kThreads / 32];
+      int m[kThreads / 32];                      // per-warp maximum bin count
+      unsigned drop[64];                         // FP32-phase samples landing on bin nb
+    } pre;
+    float2 grp[kThreads / 32][4];                // per warp job: its start groups' flux prefix (min, max)
+  } scr;
+  long long *const scan_x = scr.pre.x;
+  int *const scan_c = scr.pre.c;
+  int *const scan_m = scr.pre.m;
+  unsigned *const drop_cnt = scr.pre.drop;
 
   const uint32_t j0 = tj.j0;
   const uint32_t nfrem = tj.nfrem;
@@ -723,6 +737,9 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
           }
           g_c0 = __shfl_sync(0xffffffffu, Ps.y, lane & ~7);
           g_cl = __shfl_sync(0xffffffffu, Ps.y, (lane & ~7) + max(nrs_b, 1) - 1);
+          __syncwarp();  // the previous job's reads of scr.grp are done
+          if (mb == 0) scr.grp[warp][kb] = make_float2(g_min, g_max);
+          __syncwarp();
         }
         // bound of unit (start group kb, chunk c) on this lane; the count prefix at the last
         // entry of chunks c - 1 and c widens [kk_lo, kk_hi], which only loosens the bound
@@ -798,39 +815,57 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
         const int src = __ffs(live) - 1;
         live &= live - 1;
         const int k = src >> 3;
-        if ((t0 + k) * kRS != s0) {
+        const int sg = (t0 + k) * kRS;   // first start of the unit's group
+        const int cc = ((sg + kmi + 1) >> 5) + cbase + (src & 7);
+        const int nrs = min(kRS, nb - sg);
+        const int q = 32 * cc + lane;   // physical entry; its logical end bin:
+        const int e = swz(q);
+        // interior: every (lane, start) has k in range; otherwise windows outside
+        // (kmi, kma] or past the last end are masked before the fast test
+        const bool interior = nrs == kRS && 32 * cc >= sg + kRS + kmi && 32 * cc + 31 <= sg + kma;
+        const bool row_in = interior || (e >= sg + kmi + 1 && e <= min(sg + nrs - 1 + kma, elast));
+        // bound of the lane's row (end e against the group's starts), as the unit bound above
+        // with this end's own prefix: rows that cannot reach the running best skip the
+        // group's coefficients and the per-start test
+        const float2 Pe = row_in ? P[q] : make_float2(0.0f, 0.0f);
+        bool row = false;
+        {
+          const float kk_hi = Pe.y - P[swz(sg)].y;
+          if (row_in && kk_hi > kkmi_f) {
+            const float2 gx = scr.grp[warp][k];
+            const float thr = __uint_as_float(best_thr[f]) * kSlack;
+            const float kk_lo = fmaxf(Pe.y - P[swz(sg + nrs - 1)].y, kkmi_f + 1.0f);
+            const float den_min = fminf(kk_lo * (Nf - kk_lo), kk_hi * (Nf - kk_hi));
+            const float smax = fmaxf(Pe.x - gx.x, gx.y - Pe.x);
+            row = !(den_min > 0.0f && smax * smax < thr * den_min);
+          }
+        }
+        if (!__any_sync(0xffffffffu, row)) continue;
+        if (sg != s0) {
           if (s0 >= 0) flush();
-          s0 = (t0 + k) * kRS;
+          s0 = sg;
           const float4 *Q = reinterpret_cast<const float4 *>(P + s0);
           c0 = P[swz(s0)].y;
           blo = __uint_as_float(best_thr[f]) * kSlack;
 #pragma unroll
-          for (int q = 0; q < kRS / 2; ++q) {  // entries up to nb + kRS - 1 exist
-            const float4 v = Q[q];
-            ys[2 * q] = v.x;
-            ys[2 * q + 1] = v.z;
+          for (int h = 0; h < kRS / 2; ++h) {  // entries up to nb + kRS - 1 exist
+            const float4 v = Q[h];
+            ys[2 * h] = v.x;
+            ys[2 * h + 1] = v.z;
             const float a0 = v.y - c0, b0 = (Nf + v.y) - c0;
             const float a1 = v.w - c0, b1 = (Nf + v.w) - c0;
-            beta[2 * q] = -blo * (a0 + b0);
-            gamma[2 * q] = (blo * a0) * b0;
-            beta[2 * q + 1] = -blo * (a1 + b1);
-            gamma[2 * q + 1] = (blo * a1) * b1;
+            beta[2 * h] = -blo * (a0 + b0);
+            gamma[2 * h] = (blo * a0) * b0;
+            beta[2 * h + 1] = -blo * (a1 + b1);
+            gamma[2 * h + 1] = (blo * a1) * b1;
           }
         } else {
           const float gb = __uint_as_float(best_thr[f]) * kSlack;
           if (gb > blo) { blo = gb; coeffs(); }
         }
-        const int cc = ((s0 + kmi + 1) >> 5) + cbase + (src & 7);
-        const int nrs = min(kRS, nb - s0);
         const int hs = (s0 >> 4) & 7;
-        const int q = 32 * cc + lane;   // physical entry; its logical end bin:
-        const int e = swz(q);
         improved = false;
-        // interior: every (lane, start) has k in range; otherwise windows outside
-        // (kmi, kma] or past the last end are masked before the fast test
-        const bool interior = nrs == kRS && 32 * cc >= s0 + kRS + kmi && 32 * cc + 31 <= s0 + kma;
-        if (interior || (e >= s0 + kmi + 1 && e <= min(s0 + nrs - 1 + kma, elast))) {
-          const float2 Pe = P[q];
+        if (row) {
           const float u = Pe.y - c0;
           const float G = (blo * u) * u;
           const unsigned base = (unsigned)(e - s0 - kmi - 1);
@@ -969,6 +1004,35 @@ struct Plan {
   size_t smem;
 };
 
+// Largest static shared memory of the R = 8 tile kernels on the current device (cached per
+// device; 1024 bytes when it cannot be queried).  Two blocks share an SM only if both blocks'
+// dynamic and static bytes and the per-block reservation fit.
+size_t bls_static_smem() {
+  constexpr size_t kFallback = 1024;
+  static std::atomic<uint32_t> cached[64];  // value + 1 (0: not queried yet)
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    cudaGetLastError();
+    return kFallback;
+  }
+  const uint32_t c = cached[dev].load(std::memory_order_relaxed);
+  if (c) return c - 1;
+  const void *fns[] = {(const void *)bls_fold_scan_kernel<8, 0>, (const void *)bls_fold_scan_kernel<8, 1>,
+                       (const void *)bls_fold_scan_kernel<8, 2>, (const void *)bls_queue_kernel<8, 0>,
+                       (const void *)bls_queue_kernel<8, 1>, (const void *)bls_queue_kernel<8, 2>};
+  size_t mx = 0;
+  for (const void *fn : fns) {
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, fn) != cudaSuccess) {
+      cudaGetLastError();
+      return kFallback;
+    }
+    mx = fa.sharedSizeBytes > mx ? fa.sharedSizeBytes : mx;
+  }
+  cached[dev].store((uint32_t)mx + 1, std::memory_order_relaxed);
+  return mx;
+}
+
 // F_req > 0 forces the number of frequencies per block (batched runs fix it per batch).
 int make_plan(uint32_t nb, uint32_t kma, uint32_t nf, uint32_t F_req, Plan *p) {
   const int R = nb <= 4096 ? 8 : 16;
@@ -987,7 +1051,8 @@ int make_plan(uint32_t nb, uint32_t kma, uint32_t nf, uint32_t F_req, Plan *p) {
   const size_t per_f = (size_t)region * 8;
   // Frequencies per block: fill half an SM's shared memory so two blocks can overlap their
   // fold and scan phases; at least one round of groups.
-  const size_t budget = (size_t)gtrap::smem_per_sm() / 2 - 2048;
+  const size_t budget = (size_t)gtrap::smem_per_sm() / 2 - (size_t)gtrap::smem_reserved_per_block() -
+                        bls_static_smem();
   uint32_t F = (uint32_t)(budget / per_f);
   if (F < G) F = G;
   if (F > 64) F = 64;

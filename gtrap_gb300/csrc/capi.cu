@@ -15,6 +15,7 @@ constexpr int kMaxDevices = 64;
 int g_sm_count[kMaxDevices];
 int g_smem_optin[kMaxDevices];
 int g_smem_sm[kMaxDevices];
+int g_smem_reserved[kMaxDevices];  // stored + 1 (0: not queried yet)
 std::mutex g_attr_mutex;
 constexpr size_t kMaxFuncs = 256;
 const void *g_static_fn[kMaxFuncs];
@@ -71,6 +72,19 @@ int smem_per_sm() {
     g_smem_sm[dev] = v > 0 ? v : 100 * 1024;
   }
   return g_smem_sm[dev];
+}
+
+int smem_reserved_per_block() {
+  int dev = current_device();
+  if (!g_smem_reserved[dev]) {
+    int v = -1;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrReservedSharedMemoryPerBlock, dev) != cudaSuccess) {
+      cudaGetLastError();
+      v = -1;
+    }
+    g_smem_reserved[dev] = (v >= 0 ? v : 1024) + 1;
+  }
+  return g_smem_reserved[dev] - 1;
 }
 
 int ensure_smem(const void *func, size_t bytes, const char *what) {

@@ -25,6 +25,9 @@ int max_smem_optin();
 // Shared memory per SM of the current device (cached).
 int smem_per_sm();
 
+// Shared memory the system reserves for each resident block of the current device (cached).
+int smem_reserved_per_block();
+
 // Raise the dynamic shared-memory limit of `func` to `bytes` once per device.
 int ensure_smem(const void *func, size_t bytes, const char *what);
 
