@@ -358,6 +358,7 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
   extern __shared__ __align__(16) unsigned long long sm[];
   __shared__ unsigned long long best_key[64];    // per frequency: best (power, -start, -end)
   __shared__ unsigned best_thr[64];              // per frequency: running best power (float bits)
+  __shared__ unsigned job_next;                  // next scan job to take
   // fold and prefix scratch, dead once the prefix pass has ended, shares its bytes with the
   // scan's per-warp start-group statistics (the static total decides whether two blocks of
   // F = 6 frequencies fit on an SM at nb = 2048)
@@ -614,6 +615,7 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
     }
   }
   if (tid < 64) { best_key[tid] = 0ull; best_thr[tid] = 0u; }
+  if (tid == 0) job_next = 0u;
   __syncthreads();
 
   // ---- per 32-entry chunk of end bins: maximum and minimum of the flux prefix (float2 at
@@ -710,7 +712,14 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
   const int njob = (kma > kmi) ? (int)nfrem * ngrp_f : 0;
   const int span_chunks = ((kRS - 1 + kma - kmi - 1) >> 5) + 2;   // chunks one start group touches
   float ys[kRS] = {}, beta[kRS] = {}, gamma[kRS] = {};
-  for (int job = warp; job < njob; job += kThreads / 32) {
+  // Jobs are taken from a shared counter in frequency-major order: a frequency's surviving
+  // units cluster in the few jobs whose starts lie near its strongest windows, and a fixed
+  // job-to-warp assignment leaves the other warps waiting for those at the block barrier.
+  for (;;) {
+    int job = 0;
+    if (lane == 0) job = (int)atomicAdd(&job_next, 1u);
+    job = __shfl_sync(0xffffffffu, job, 0);
+    if (job >= njob) break;
     const int f = job / ngrp_f;
     const int t0 = (job - f * ngrp_f) * 4;
     const float2 *P = reinterpret_cast<const float2 *>(sm + (size_t)f * a.region);
