@@ -698,19 +698,25 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
   __syncthreads();
 
   // ---- candidate windows [i, e), k = e - i in (kmi, kma], kk > kkmi.  Work unit: a chunk of
-  // 32 consecutive end bins against kRS consecutive start bins.  The power of every window in
-  // the unit is bounded by
+  // 32 consecutive end bins against kGS = 16 consecutive start bins (a bound group).  The power
+  // of every window in the unit is bounded by
   //   max(Pmax - ys_min, ys_max - Pmin)^2 / min(den(kk_lo), den(kk_hi))
   // (den = kk (N - kk) is concave in kk), and units whose bound is below the frequency's shared
-  // running best (times the pre-test slack) cannot hold the maximum.  A warp takes four
-  // consecutive start groups; each lane bounds one (start group, chunk) unit, and the warp then
-  // evaluates the surviving units together, one end bin per lane.  A start group is one
-  // aligned 8-entry block: its entries are read with four 16-byte broadcast loads and used in
-  // slot order (slot j holds start s0 + (j ^ h), h = the block's swizzle).
-  const int ntask_f = (nb + kRS - 1) / kRS;          // start groups per frequency
-  const int ngrp_f = (ntask_f + 3) / 4;              // warp jobs per frequency
+  // running best (times the pre-test slack) cannot hold the maximum.  A warp job takes four
+  // consecutive bound groups; each lane bounds one (group, chunk) unit.  The warp then takes
+  // the surviving units one at a time, one end bin (row) per lane: each row is bounded the same
+  // way with its own prefix, and rows that pass run the per-start test on the group's two
+  // halves of kRS = 8 starts.  A half is one aligned 8-entry block: its entries are read with
+  // four 16-byte broadcast loads and used in slot order (slot j holds start s0 + (j ^ h),
+  // h = the block's swizzle).  Groups of 16 starts halve the unit bounds of 8-start groups
+  // and leave fewer units to walk; the row bound keeps the halves' tests rare.
+  constexpr int kGS = 2 * kRS;
+  const int ngs_f = (nb + kGS - 1) / kGS;            // bound groups per frequency
+  const int ngrp_f = (ngs_f + 3) / 4;                // warp jobs per frequency
   const int njob = (kma > kmi) ? (int)nfrem * ngrp_f : 0;
-  const int span_chunks = ((kRS - 1 + kma - kmi - 1) >> 5) + 2;   // chunks one start group touches
+  const int span_chunks = ((kGS - 1 + kma - kmi - 1) >> 5) + 2;   // chunks one group touches
+  // job / ngrp_f as a multiply-high: exact for job < 2^16 and ngrp_f <= 2^16
+  const unsigned long long jmag = 0xffffffffull / (unsigned)ngrp_f + 1ull;
   float ys[kRS] = {}, beta[kRS] = {}, gamma[kRS] = {};
   // Jobs are taken from a shared counter in frequency-major order: a frequency's surviving
   // units cluster in the few jobs whose starts lie near its strongest windows, and a fixed
@@ -720,40 +726,44 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
     if (lane == 0) job = (int)atomicAdd(&job_next, 1u);
     job = __shfl_sync(0xffffffffu, job, 0);
     if (job >= njob) break;
-    const int f = job / ngrp_f;
-    const int t0 = (job - f * ngrp_f) * 4;
+    const int f = (int)(((unsigned long long)(unsigned)job * jmag) >> 32);
+    const int t0 = (job - f * ngrp_f) * 4;           // first bound group of the job
     const float2 *P = reinterpret_cast<const float2 *>(sm + (size_t)f * a.region);
     const float2 *CM = reinterpret_cast<const float2 *>(sm + (size_t)f * a.region + lp);
     const float *CL = reinterpret_cast<const float *>(sm + (size_t)f * a.region + lp + nchunk);
     for (int cbase = 0; cbase < span_chunks; cbase += 8) {
       unsigned live;
       {
-        // the job's 32 starts, one per lane (an aligned 32-entry block): per group of 8 the
-        // minimum and maximum flux prefix and the count prefix at its first and last start
+        // the job's 64 starts, two per lane: per group of 16 the minimum and maximum flux
+        // prefix and the count prefix at its first and last start
         const int kb = lane >> 3, mb = lane & 7;
-        const int sb = (t0 + kb) * kRS;
-        const int nrs_b = min(kRS, nb - sb);
+        const int sb = (t0 + kb) * kGS;
+        const int nrs_b = min(kGS, nb - sb);
         float g_min, g_max, g_c0, g_cl;
         {
-          const int si = t0 * kRS + lane;
-          const float2 Ps = si < lp ? P[swz(si)] : make_float2(0.0f, 0.0f);
-          g_min = si < nb ? Ps.x : INFINITY;
-          g_max = si < nb ? Ps.x : -INFINITY;
+          const int si = t0 * kGS + 2 * lane;
+          const float2 Pa = si < nb ? P[swz(si)] : make_float2(0.0f, 0.0f);
+          const float2 Pb = si + 1 < nb ? P[swz(si + 1)] : make_float2(0.0f, 0.0f);
+          g_min = fminf(si < nb ? Pa.x : INFINITY, si + 1 < nb ? Pb.x : INFINITY);
+          g_max = fmaxf(si < nb ? Pa.x : -INFINITY, si + 1 < nb ? Pb.x : -INFINITY);
 #pragma unroll
           for (int o = 1; o < 8; o <<= 1) {
             g_min = fminf(g_min, __shfl_xor_sync(0xffffffffu, g_min, o));
             g_max = fmaxf(g_max, __shfl_xor_sync(0xffffffffu, g_max, o));
           }
-          g_c0 = __shfl_sync(0xffffffffu, Ps.y, lane & ~7);
-          g_cl = __shfl_sync(0xffffffffu, Ps.y, (lane & ~7) + max(nrs_b, 1) - 1);
+          const int r = max(nrs_b, 1) - 1;          // the group's last start, relative
+          g_c0 = __shfl_sync(0xffffffffu, Pa.y, lane & ~7);
+          const float ca = __shfl_sync(0xffffffffu, Pa.y, (lane & ~7) + (r >> 1));
+          const float cb = __shfl_sync(0xffffffffu, Pb.y, (lane & ~7) + (r >> 1));
+          g_cl = (r & 1) ? cb : ca;
           __syncwarp();  // the previous job's reads of scr.grp are done
           if (mb == 0) scr.grp[warp][kb] = make_float2(g_min, g_max);
           __syncwarp();
         }
-        // bound of unit (start group kb, chunk c) on this lane; the count prefix at the last
-        // entry of chunks c - 1 and c widens [kk_lo, kk_hi], which only loosens the bound
+        // bound of unit (group kb, chunk c) on this lane; the count prefix at the last entry of
+        // chunks c - 1 and c widens [kk_lo, kk_hi], which only loosens the bound
         bool keep = false;
-        if (t0 + kb < ntask_f) {
+        if (t0 + kb < ngs_f) {
           const int b_elo = sb + kmi + 1;
           const int b_ehi = min(sb + nrs_b - 1 + kma, elast);
           const int c = (b_elo >> 5) + cbase + mb;
@@ -773,9 +783,9 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
       }
       float blo = 0.0f, c0 = 0.0f, bpow = 0.0f;
       int bk = INT_MAX;  // best window of this lane: (start << 15) | end
-      int s0 = -1;       // first start of the loaded group (-1: none)
+      int s0 = -1;       // first start of the loaded half (-1: none)
       bool improved = false;
-      // pre-test coefficients of the loaded group at threshold blo, in slot order
+      // pre-test coefficients of the loaded half at threshold blo, in slot order
       auto coeffs = [&]() {
         const float4 *Q = reinterpret_cast<const float4 *>(P + s0);
 #pragma unroll
@@ -808,7 +818,7 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
           }
         }
       };
-      auto flush = [&]() {  // warp best of the loaded start group into the frequency record
+      auto flush = [&]() {  // warp best of the loaded half into the frequency record
         if (!__any_sync(0xffffffffu, bk != INT_MAX)) return;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
@@ -824,18 +834,15 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
         const int src = __ffs(live) - 1;
         live &= live - 1;
         const int k = src >> 3;
-        const int sg = (t0 + k) * kRS;   // first start of the unit's group
+        const int sg = (t0 + k) * kGS;   // first start of the unit's group
         const int cc = ((sg + kmi + 1) >> 5) + cbase + (src & 7);
-        const int nrs = min(kRS, nb - sg);
+        const int nrs = min(kGS, nb - sg);
         const int q = 32 * cc + lane;   // physical entry; its logical end bin:
         const int e = swz(q);
-        // interior: every (lane, start) has k in range; otherwise windows outside
-        // (kmi, kma] or past the last end are masked before the fast test
-        const bool interior = nrs == kRS && 32 * cc >= sg + kRS + kmi && 32 * cc + 31 <= sg + kma;
-        const bool row_in = interior || (e >= sg + kmi + 1 && e <= min(sg + nrs - 1 + kma, elast));
+        const bool row_in = e >= sg + kmi + 1 && e <= min(sg + nrs - 1 + kma, elast);
         // bound of the lane's row (end e against the group's starts), as the unit bound above
         // with this end's own prefix: rows that cannot reach the running best skip the
-        // group's coefficients and the per-start test
+        // halves' coefficients and per-start tests
         const float2 Pe = row_in ? P[q] : make_float2(0.0f, 0.0f);
         bool row = false;
         {
@@ -850,53 +857,63 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
           }
         }
         if (!__any_sync(0xffffffffu, row)) continue;
-        if (sg != s0) {
-          if (s0 >= 0) flush();
-          s0 = sg;
-          const float4 *Q = reinterpret_cast<const float4 *>(P + s0);
-          c0 = P[swz(s0)].y;
-          blo = __uint_as_float(best_thr[f]) * kSlack;
+        for (int h = 0; h < kGS / kRS; ++h) {
+          const int sh = sg + kRS * h;    // first start of the half
+          if (sh >= nb) break;
+          const int nrs_h = min(kRS, nb - sh);
+          // interior: every (lane, start) of the half has k in range; otherwise windows outside
+          // (kmi, kma] or past the last end are masked before the fast test
+          const bool interior = nrs_h == kRS && 32 * cc >= sh + kRS + kmi && 32 * cc + 31 <= sh + kma;
+          const bool go = row && (interior || (e >= sh + kmi + 1 && e <= min(sh + nrs_h - 1 + kma, elast)));
+          if (!__any_sync(0xffffffffu, go)) continue;
+          if (sh != s0) {
+            if (s0 >= 0) flush();
+            s0 = sh;
+            const float4 *Q = reinterpret_cast<const float4 *>(P + s0);
+            c0 = P[swz(s0)].y;
+            blo = __uint_as_float(best_thr[f]) * kSlack;
 #pragma unroll
-          for (int h = 0; h < kRS / 2; ++h) {  // entries up to nb + kRS - 1 exist
-            const float4 v = Q[h];
-            ys[2 * h] = v.x;
-            ys[2 * h + 1] = v.z;
-            const float a0 = v.y - c0, b0 = (Nf + v.y) - c0;
-            const float a1 = v.w - c0, b1 = (Nf + v.w) - c0;
-            beta[2 * h] = -blo * (a0 + b0);
-            gamma[2 * h] = (blo * a0) * b0;
-            beta[2 * h + 1] = -blo * (a1 + b1);
-            gamma[2 * h + 1] = (blo * a1) * b1;
+            for (int w = 0; w < kRS / 2; ++w) {  // entries up to nb + kRS - 1 exist
+              const float4 v = Q[w];
+              ys[2 * w] = v.x;
+              ys[2 * w + 1] = v.z;
+              const float a0 = v.y - c0, b0 = (Nf + v.y) - c0;
+              const float a1 = v.w - c0, b1 = (Nf + v.w) - c0;
+              beta[2 * w] = -blo * (a0 + b0);
+              gamma[2 * w] = (blo * a0) * b0;
+              beta[2 * w + 1] = -blo * (a1 + b1);
+              gamma[2 * w + 1] = (blo * a1) * b1;
+            }
+          } else {
+            const float gb = __uint_as_float(best_thr[f]) * kSlack;
+            if (gb > blo) { blo = gb; coeffs(); }
           }
-        } else {
-          const float gb = __uint_as_float(best_thr[f]) * kSlack;
-          if (gb > blo) { blo = gb; coeffs(); }
-        }
-        const int hs = (s0 >> 4) & 7;
-        improved = false;
-        if (row) {
-          const float u = Pe.y - c0;
-          const float G = (blo * u) * u;
-          const unsigned base = (unsigned)(e - s0 - kmi - 1);
-          unsigned neg = 0xffffffffu;
-#pragma unroll
-          for (int j = 0; j < kRS; ++j) {
-            const float s = Pe.x - ys[j];
-            const float t = fmaf(s, s, fmaf(u, beta[j], G + gamma[j]));
-            const bool in = interior || base - (unsigned)(j ^ hs) < (unsigned)(kma - kmi);
-            neg &= in ? __float_as_uint(t) : 0x80000000u;
-          }
-          if (!(neg >> 31)) {  // kk and the exact pre-test are checked in consider
+          const int hs = (s0 >> 4) & 7;
+          improved = false;
+          if (go) {
+            const float u = Pe.y - c0;
+            const float G = (blo * u) * u;
+            const unsigned base = (unsigned)(e - s0 - kmi - 1);
+            unsigned neg = 0xffffffffu;
 #pragma unroll
             for (int j = 0; j < kRS; ++j) {
               const float s = Pe.x - ys[j];
               const float t = fmaf(s, s, fmaf(u, beta[j], G + gamma[j]));
               const bool in = interior || base - (unsigned)(j ^ hs) < (unsigned)(kma - kmi);
-              if (in && !(t < 0.0f)) consider(j, Pe, e);
+              neg &= in ? __float_as_uint(t) : 0x80000000u;
+            }
+            if (!(neg >> 31)) {  // kk and the exact pre-test are checked in consider
+#pragma unroll
+              for (int j = 0; j < kRS; ++j) {
+                const float s = Pe.x - ys[j];
+                const float t = fmaf(s, s, fmaf(u, beta[j], G + gamma[j]));
+                const bool in = interior || base - (unsigned)(j ^ hs) < (unsigned)(kma - kmi);
+                if (in && !(t < 0.0f)) consider(j, Pe, e);
+              }
             }
           }
+          if (improved) atomicMax(best_thr + f, __float_as_uint(bpow));
         }
-        if (improved) atomicMax(best_thr + f, __float_as_uint(bpow));
       }
       if (s0 >= 0) flush();
     }
