@@ -733,6 +733,7 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
     const float *CL = reinterpret_cast<const float *>(sm + (size_t)f * a.region + lp + nchunk);
     for (int cbase = 0; cbase < span_chunks; cbase += 8) {
       unsigned live;
+      float h_min, h_max;   // flux prefix (min, max) over the lane's half: starts 8 (lane >> 2) ..
       {
         // the job's 64 starts, two per lane: per group of 16 the minimum and maximum flux
         // prefix and the count prefix at its first and last start
@@ -747,10 +748,14 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
           g_min = fminf(si < nb ? Pa.x : INFINITY, si + 1 < nb ? Pb.x : INFINITY);
           g_max = fmaxf(si < nb ? Pa.x : -INFINITY, si + 1 < nb ? Pb.x : -INFINITY);
 #pragma unroll
-          for (int o = 1; o < 8; o <<= 1) {
+          for (int o = 1; o < 4; o <<= 1) {
             g_min = fminf(g_min, __shfl_xor_sync(0xffffffffu, g_min, o));
             g_max = fmaxf(g_max, __shfl_xor_sync(0xffffffffu, g_max, o));
           }
+          h_min = g_min;   // the lane's half (8 starts)
+          h_max = g_max;
+          g_min = fminf(g_min, __shfl_xor_sync(0xffffffffu, g_min, 4));
+          g_max = fmaxf(g_max, __shfl_xor_sync(0xffffffffu, g_max, 4));
           const int r = max(nrs_b, 1) - 1;          // the group's last start, relative
           g_c0 = __shfl_sync(0xffffffffu, Pa.y, lane & ~7);
           const float ca = __shfl_sync(0xffffffffu, Pa.y, (lane & ~7) + (r >> 1));
@@ -864,7 +869,24 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
           // interior: every (lane, start) of the half has k in range; otherwise windows outside
           // (kmi, kma] or past the last end are masked before the fast test
           const bool interior = nrs_h == kRS && 32 * cc >= sh + kRS + kmi && 32 * cc + 31 <= sh + kma;
-          const bool go = row && (interior || (e >= sh + kmi + 1 && e <= min(sh + nrs_h - 1 + kma, elast)));
+          bool go = row && (interior || (e >= sh + kmi + 1 && e <= min(sh + nrs_h - 1 + kma, elast)));
+          // the row bound again over this half's starts alone
+          {
+            const float x_min = __shfl_sync(0xffffffffu, h_min, 8 * k + 4 * h);
+            const float x_max = __shfl_sync(0xffffffffu, h_max, 8 * k + 4 * h);
+            if (go) {
+              const float kk_hi = Pe.y - P[swz(sh)].y;
+              if (kk_hi > kkmi_f) {
+                const float thr = __uint_as_float(best_thr[f]) * kSlack;
+                const float kk_lo = fmaxf(Pe.y - P[swz(sh + nrs_h - 1)].y, kkmi_f + 1.0f);
+                const float den_min = fminf(kk_lo * (Nf - kk_lo), kk_hi * (Nf - kk_hi));
+                const float smax = fmaxf(Pe.x - x_min, x_max - Pe.x);
+                go = !(den_min > 0.0f && smax * smax < thr * den_min);
+              } else {
+                go = false;
+              }
+            }
+          }
           if (!__any_sync(0xffffffffu, go)) continue;
           if (sh != s0) {
             if (s0 >= 0) flush();
