@@ -27,6 +27,7 @@
 //    candidate that can tie or beat the running best; admitted candidates are compared
 //    exactly with a correctly rounded quotient and a lowest-(start, end) tie-break.
 #include <atomic>
+#include <type_traits>
 
 #include "common.cuh"
 
@@ -414,40 +415,54 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
     return __float2uint_rz(__fmul_rn(nbf, ph));
   };
   if (MODE != 2) {
-    // kU samples per thread per step, all loads issued before any is used
+    // kU samples per thread per step, all loads issued before any is used.  NF > 0: the tile
+    // has exactly NF frequencies (fully unrolled: no guarded iterations); NF == 0: nfrem.
     constexpr int kU = 4;
-    for (uint32_t k0 = tid; k0 < tj.n; k0 += kU * kThreads) {
-      int32_t xq[kU];
-      ulonglong2 ab[kU];
+    auto fold = [&](auto nf_c) {
+      constexpr int NF = decltype(nf_c)::value;
+      for (uint32_t k0 = tid; k0 < tj.n; k0 += kU * kThreads) {
+        int32_t xq[kU];
+        ulonglong2 ab[kU];
 #pragma unroll
-      for (int u = 0; u < kU; ++u) {
-        const uint32_t k = k0 + u * kThreads;
-        xq[u] = k < tj.n ? __ldg(Xq + k) : kMasked;
-        ab[u] = k < tj.n ? __ldg(ABq + k) : make_ulonglong2(0ull, 0ull);
-      }
+        for (int u = 0; u < kU; ++u) {
+          const uint32_t k = k0 + u * kThreads;
+          xq[u] = k < tj.n ? __ldg(Xq + k) : kMasked;
+          ab[u] = k < tj.n ? __ldg(ABq + k) : make_ulonglong2(0ull, 0ull);
+        }
 #pragma unroll
-      for (int u = 0; u < kU; ++u) {
-        if (xq[u] == kMasked) continue;
-        const unsigned wS = (unsigned)(xq[u] >> 10);
-        const unsigned wC = ((unsigned)(xq[u] & 1023) << 12) | 1u;
-        unsigned long long ph = ab[u].x + (unsigned long long)j0 * ab[u].y;
-        // S in the low word for bins with bit 4 clear, in the high word otherwise, so that
-        // the S (and the C) updates of a warp reach all 32 banks
-        auto add = [&](unsigned *h) {
-          const uint32_t bin = MODE == 0 ? (uint32_t)(ph >> shift) : (uint32_t)__umul64hi(ph, (unsigned long long)nb);
-          const uint32_t w = 2u * (uint32_t)swz((int)bin) + ((bin >> 4) & 1u);
-          atomicAdd(h + w, wS);
-          atomicAdd(h + (w ^ 1u), wC);
-          ph += ab[u].y;
-        };
-        if (nfrem <= 8) {
+        for (int u = 0; u < kU; ++u) {
+          if (xq[u] == kMasked) continue;
+          const unsigned wS = (unsigned)(xq[u] >> 10);
+          const unsigned wC = ((unsigned)(xq[u] & 1023) << 12) | 1u;
+          unsigned long long ph = ab[u].x + (unsigned long long)j0 * ab[u].y;
+          // S in the low word for bins with bit 4 clear, in the high word otherwise, so that
+          // the S (and the C) updates of a warp reach all 32 banks
+          auto add = [&](unsigned *h) {
+            const uint32_t bin = MODE == 0 ? (uint32_t)(ph >> shift) : (uint32_t)__umul64hi(ph, (unsigned long long)nb);
+            const uint32_t w = 2u * (uint32_t)swz((int)bin) + ((bin >> 4) & 1u);
+            atomicAdd(h + w, wS);
+            atomicAdd(h + (w ^ 1u), wC);
+            ph += ab[u].y;
+          };
+          if constexpr (NF > 0) {
 #pragma unroll
-          for (uint32_t f = 0; f < 8; ++f)
-            if (f < nfrem) add(h32 + f * 2 * a.region);
-        } else {
-          for (uint32_t f = 0; f < nfrem; ++f) add(h32 + f * 2 * a.region);
+            for (int f = 0; f < NF; ++f) add(h32 + f * 2 * a.region);
+          } else if (nfrem <= 8) {
+#pragma unroll
+            for (uint32_t f = 0; f < 8; ++f)
+              if (f < nfrem) add(h32 + f * 2 * a.region);
+          } else {
+            for (uint32_t f = 0; f < nfrem; ++f) add(h32 + f * 2 * a.region);
+          }
         }
       }
+    };
+    switch (nfrem) {
+      case 4: fold(std::integral_constant<int, 4>{}); break;
+      case 5: fold(std::integral_constant<int, 5>{}); break;
+      case 6: fold(std::integral_constant<int, 6>{}); break;
+      case 8: fold(std::integral_constant<int, 8>{}); break;
+      default: fold(std::integral_constant<int, 0>{}); break;
     }
   } else {
     for (uint32_t k = tid; k < tj.n; k += kThreads) {
