@@ -1460,6 +1460,25 @@ def run_served(args, rank, world, local_rank):
                       "evals_per_s": s["evals_per_s"],
                       "plain": {"requests": pm, "served_req_per_s": ps["req_per_s"],
                                 "p50_ms": ps["p50_ms"], "p99_ms": ps["p99_ms"]}})
+    # the same requests as one packed batch (detrend, offsets, encoding and one persistent
+    # launch per kind, with the server's tile size and block counts): the batched path's rate
+    # on identical content, the reference point for the server's saturation
+    bat = build_batch(curves, local_rank, tls_kind=args.tls_kind)
+    bat.set_config(srv.F)
+    bat.launch()
+    torch.cuda.synchronize()
+    b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    b0.record()
+    bat.launch()
+    b1.record()
+    torch.cuda.synchronize()
+    bms = b0.elapsed_time(b1)
+    bev = bat.bls_evals + bat.tls_evals + bat.fold_evals
+    same_pool = {"what": "the pool's requests as one packed batch (RaggedBatch.launch, the server's tile size "
+                         "and block counts, inputs resident, outputs left on the device)",
+                 "ms": bms, "evals": bev, "evals_per_s": bev / (bms / 1e3),
+                 "served_saturation_frac": sat["evals_per_s"] / (bev / (bms / 1e3))}
+    del bat
     if rank != 0:
         return
     # bytes a request returns to the host: full series, or the statistics records
@@ -1476,7 +1495,7 @@ def run_served(args, rank, world, local_rank):
                        "tls_tiles_per_step": srv.tls_tiles, "fold_tiles_per_step": srv.fold_tiles,
                        "returns": "statistics records only (get_blsstat / GTLS peak statistics)" if peaks_only
                        else "full spectra and S/N series", "mean_bytes_returned_per_request": float(np.mean(ret))},
-            "saturation": sat, "plain_saturation": psat, "sweep": sweep,
+            "saturation": sat, "plain_saturation": psat, "batched_same_pool": same_pool, "sweep": sweep,
             "hbm_high_water_bytes": srv.hbm_high_water()}
     print(json.dumps(line), flush=True)
 

@@ -33,6 +33,7 @@ _SIGNATURES = {
     "gtrap_last_error": (C.c_char_p, []),
     "gtrap_version": (C.c_int, []),
     "gtrap_copy_async": (C.c_int, [vp, u32, vp]),
+    "gtrap_gather_async": (C.c_int, [vp, u32, vp, u32, vp]),
     "gtrap_gfilter": (C.c_int, [vp, vp, u32, u32, u32, vp]),
     "gtrap_offset": (C.c_int, [vp, vp, vp, u32, u32, vp]),
     "gtrap_geebls_workspace_size": (sz, [u32, u32, u32]),

@@ -128,6 +128,32 @@ int ensure_smem(const void *func, size_t bytes, const char *what) {
 
 }  // namespace gtrap
 
+namespace {
+
+// One block per copy of the list (grid-stride over copies), each moving its bytes in the
+// widest unit (16, 8, 4, 2 or 1 bytes) that divides both addresses and the size.
+template <typename T>
+__device__ __forceinline__ void gather_move(void *dst, const void *src, size_t bytes) {
+  T *d = static_cast<T *>(dst);
+  const T *s = static_cast<const T *>(src);
+  const size_t n = bytes / sizeof(T);
+  for (size_t i = threadIdx.x; i < n; i += blockDim.x) d[i] = s[i];
+}
+
+__global__ void __launch_bounds__(256) gather_kernel(const gtrap_copy *list, uint32_t count) {
+  for (uint32_t k = blockIdx.x; k < count; k += gridDim.x) {
+    const gtrap_copy c = list[k];
+    const uintptr_t a = reinterpret_cast<uintptr_t>(c.dst) | reinterpret_cast<uintptr_t>(c.src) | (uintptr_t)c.bytes;
+    if ((a & 15) == 0) gather_move<uint4>(c.dst, c.src, c.bytes);
+    else if ((a & 7) == 0) gather_move<uint2>(c.dst, c.src, c.bytes);
+    else if ((a & 3) == 0) gather_move<uint32_t>(c.dst, c.src, c.bytes);
+    else if ((a & 1) == 0) gather_move<uint16_t>(c.dst, c.src, c.bytes);
+    else gather_move<uint8_t>(c.dst, c.src, c.bytes);
+  }
+}
+
+}  // namespace
+
 extern "C" {
 
 const char *gtrap_last_error(void) { return gtrap::g_last_error; }
@@ -146,6 +172,24 @@ int gtrap_copy_async(const gtrap_copy *copies, uint32_t count, gtrap_stream_t st
       return gtrap::fail(GTRAP_ERR_CUDA, "copy_async: copy %u of %u: %s", k, count, cudaGetErrorString(e));
   }
   return GTRAP_OK;
+}
+
+int gtrap_gather_async(const gtrap_copy *copies, uint32_t count, gtrap_copy *list_dev, uint32_t list_cap,
+                       gtrap_stream_t stream) {
+  if (count == 0) return GTRAP_OK;
+  if (!copies || !list_dev) return gtrap::fail(GTRAP_ERR_INVALID_ARG, "gather_async: null copy list");
+  if (count > list_cap)
+    return gtrap::fail(GTRAP_ERR_INVALID_ARG, "gather_async: %u copies, device list holds %u", count, list_cap);
+  for (uint32_t k = 0; k < count; ++k) {
+    if (copies[k].bytes == 0) continue;
+    if (!copies[k].dst || !copies[k].src)
+      return gtrap::fail(GTRAP_ERR_INVALID_ARG, "gather_async: null pointer in copy %u", k);
+  }
+  cudaError_t e = cudaMemcpyAsync(list_dev, copies, (size_t)count * sizeof(gtrap_copy), cudaMemcpyHostToDevice, stream);
+  if (e != cudaSuccess) return gtrap::fail(GTRAP_ERR_CUDA, "gather_async: list copy: %s", cudaGetErrorString(e));
+  const uint32_t blocks = count < 65535u ? count : 65535u;
+  gather_kernel<<<blocks, 256, 0, stream>>>(list_dev, count);
+  return gtrap::check_launch("gather_kernel");
 }
 
 }  // extern "C"

@@ -195,6 +195,9 @@ class _Copies:
             self.items = []
 
 
+GATHER_MIN = 16   # a step's output copies from this many on go through one device gather
+
+
 @dataclass
 class _Live:
     rid: int
@@ -228,13 +231,15 @@ class TransitServer:
     ``hbm_budget`` bytes are split between the sample arena (``SAMPLE_BYTES`` per sample)
     and the output arena (``OUTPUT_BYTES`` per output element) in the ratio
     ``sample_share``; a request whose samples or outputs alone exceed an arena is rejected
-    by :meth:`submit`."""
+    by :meth:`submit`.  Results are returned by :meth:`step`, :meth:`poll` and
+    :meth:`run_until_idle`; ``history`` > 0 also keeps the last ``history`` of them in
+    ``results`` (their arrays hold pinned host memory until released)."""
 
     def __init__(self, bls: BlsSpec = BlsSpec(), tls: TlsSpec = TlsSpec(), detrend_r: int = 24,
                  hbm_budget: float = 100e9, sample_share: float = 0.8, bls_tiles: int | None = None,
                  tls_tiles: int | None = None, F: int | None = None, max_requests: int = 1 << 16,
                  depth: int = 2, tls_peaks: dict | None = None, device=None, fold: FoldSpec = FoldSpec(),
-                 fold_tiles: int | None = None, spectrum_stats: bool = False):
+                 fold_tiles: int | None = None, spectrum_stats: bool = False, history: int = 0):
         require_cuda()
         self.dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         self.bls_spec, self.tls_spec, self.fold_spec = bls, tls, fold
@@ -282,13 +287,18 @@ class TransitServer:
         self.meta_dev = [torch.empty(META_SLOT_BYTES, dtype=torch.uint8, device=d) for _ in range(self.depth)]
         self.h2d = torch.cuda.Stream(d)
         self.d2h = torch.cuda.Stream(d)
+        self._gstage = None   # output gathers: device staging buffer and copy list
+        self._glist = None
         self.waiting: collections.deque = collections.deque()
         self.live_bls: list = []
         self.live_fold: list = []
         self.live_tls: list = []
         self.steps: collections.deque = collections.deque()
         self.draining: list = []
-        self.results: list = []
+        # the last ``history`` results (0: none); every result is returned by step(), poll()
+        # or run_until_idle() in any case.  A result's arrays are views of its step's pinned
+        # block, which returns to the pinned cache once all of that step's results are dropped
+        self.results: collections.deque = collections.deque(maxlen=max(0, int(history)))
         self.step_count = 0
         self.next_rid = 0
         self.max_tls_nsc = 1
@@ -598,42 +608,77 @@ class TransitServer:
 
     def _issue_copies(self, step):
         """Queue the output copies of the requests a step finishes on the copy stream, behind
-        the step's kernels (the host does not wait for the step to see that it has run)."""
+        the step's kernels (the host does not wait for the step to see that it has run).  The
+        step's finishing requests share one pinned block; each request's result is a tuple of
+        numpy views into it, one per output series."""
         if not step.finishing:
             return
         self.d2h.wait_event(step.event)
         for bufs in list(step.bstats.values()) + [step.peaks]:
             for t_ in bufs:   # statistics buffers stay allocated until the copies have run
                 t_.record_stream(self.d2h)
-        cp = _Copies()
+        # per request and output series: (device address, bytes, numpy dtype)
+        plans = []
         for lv in step.finishing:
             m, o = lv.req.outputs, lv.ooff
             if lv.st_slot >= 0 and lv.req.kind in step.bstats:
-                srcs = [b_[lv.st_slot:lv.st_slot + 1].reshape(-1) for b_ in step.bstats[lv.req.kind]]
+                srcs = [_row(b_, lv.st_slot) for b_ in step.bstats[lv.req.kind]]
             elif lv.req.kind == "tls" and lv.pk_slot >= 0:
                 st_, idx, val = step.peaks
                 rs = api.PEAK_STATS.itemsize
-                srcs = (st_[lv.pk_slot * rs:(lv.pk_slot + 1) * rs], idx[lv.pk_slot], val[lv.pk_slot])
+                srcs = [(st_.data_ptr() + lv.pk_slot * rs, rs, np.dtype(np.uint8)),
+                        _row(idx, lv.pk_slot), _row(val, lv.pk_slot)]
             else:
                 series = {"bls": 3, "fold": 4}.get(lv.req.kind, 5)
-                srcs = [self.o[j][o:o + m] for j in range(series)]
-            # one pinned block for the request's outputs, one view per series
-            sizes = [(src.numel() * src.element_size() + 15) // 16 * 16 for src in srcs]
-            blk = torch.empty(sum(sizes), dtype=torch.uint8, pin_memory=True)
-            outs, o_ = [], 0
+                srcs = [(self.o[j].data_ptr() + 4 * o, 4 * m, np.dtype(np.float32)) for j in range(series)]
+            plans.append(srcs)
+        total = sum((nb + 15) // 16 * 16 for srcs in plans for _, nb, _ in srcs)
+        # a power-of-two block (at least 64 KB), so that released blocks serve later steps
+        blk = torch.empty(1 << max(16, (total - 1).bit_length()), dtype=torch.uint8, pin_memory=True)
+        hn = blk.numpy()   # holds the block: the views below keep it alive
+        ncopy = sum(len(srcs) for srcs in plans)
+        # many ranges: gathered on the device into one staging buffer (one copy and one launch)
+        # and copied to the host in one piece; few: one copy each
+        gather = ncopy >= GATHER_MIN
+        if gather:
+            stage, lst = self._gather_buffers(total, ncopy)
+            base = stage.data_ptr()
+        else:
             base = blk.data_ptr()
-            for src, sz in zip(srcs, sizes):
-                nbytes = src.numel() * src.element_size()
-                outs.append(blk[o_:o_ + nbytes].view(src.dtype))
-                cp.add(base + o_, src.data_ptr(), nbytes)
-                o_ += sz
+        cp = _Copies()
+        off = 0
+        for lv, srcs in zip(step.finishing, plans):
+            outs = []
+            for ptr, nb, dt in srcs:
+                cp.add(base + off, ptr, nb)
+                outs.append(hn[off:off + nb].view(dt))
+                off += (nb + 15) // 16 * 16
             lv.result = tuple(outs)
+        if gather:
+            rows = np.array(cp.items, dtype=np.uint64)   # gtrap_copy rows: dst, src, bytes
+            N.call("gtrap_gather_async", rows.ctypes.data, len(cp.items), lst.data_ptr(),
+                   lst.numel() // 24, self.d2h.cuda_stream)
+            cp.items = []
+            cp.add(blk.data_ptr(), base, total)
         cp.issue(self.d2h.cuda_stream)
         ev = torch.cuda.Event()
         ev.record(self.d2h)
         for lv in step.finishing:
             lv.d2h_event = ev
         self.draining.extend(step.finishing)
+
+    def _gather_buffers(self, nbytes: int, ncopy: int):
+        """The device staging buffer and copy list of the output gathers.  Gathers and their
+        device-to-host copies all run on the copy stream, in order, so one buffer of each
+        serves every step; a larger request replaces it (the caching allocator reuses the old
+        block only for later work on the same stream)."""
+        if self._gstage is None or self._gstage.numel() < nbytes:
+            with torch.cuda.stream(self.d2h):
+                self._gstage = torch.empty(max(nbytes, 1 << 20) * 5 // 4, dtype=torch.uint8, device=self.dev)
+        if self._glist is None or self._glist.numel() < 24 * ncopy:
+            with torch.cuda.stream(self.d2h):
+                self._glist = torch.empty(24 * max(ncopy, 1024) * 5 // 4, dtype=torch.uint8, device=self.dev)
+        return self._gstage, self._glist
 
     def poll(self) -> list:
         """Retire finished steps and return the requests whose outputs have arrived."""
@@ -644,27 +689,22 @@ class TransitServer:
         for lv in self.draining:
             if lv.d2h_event.query():
                 now = time.perf_counter()
-                res = lv.result
+                res = lv.result   # numpy views of the step's pinned block
                 if lv.st_slot >= 0:
-                    stats = (float(res[0].numpy()[0]), float(res[1].numpy()[0]), int(res[2].numpy()[0]),
-                             int(res[3].numpy()[0]))
+                    stats = (float(res[0][0]), float(res[1][0]), int(res[2][0]), int(res[3][0]))
                     if len(res) > 4:  # BLS: with the refined best peak
                         rec = np.zeros((), api.BLS_STATS_REFINED)
                         rec["pest"], rec["sde"], rec["ph1"], rec["ph2"] = stats
-                        rec["refined"] = np.frombuffer(res[4].numpy().tobytes(), api.BLS_REFINED)[0]
+                        rec["refined"] = np.frombuffer(res[4].tobytes(), api.BLS_REFINED)[0]
                         res = rec
                     else:
                         res = np.array(stats, dtype=api.BLS_STATS)
                 elif lv.req.kind == "bls":
-                    res = (res[0].numpy(), res[1].numpy().view(np.int32), res[2].numpy().view(np.int32))
+                    res = (res[0], res[1].view(np.int32), res[2].view(np.int32))
                 elif lv.req.kind == "fold":
-                    res = (res[0].numpy(), res[1].numpy().view(np.int32), res[2].numpy().view(np.int32),
-                           res[3].numpy())
+                    res = (res[0], res[1].view(np.int32), res[2].view(np.int32), res[3])
                 elif lv.pk_slot >= 0:
-                    res = (np.frombuffer(res[0].numpy().tobytes(), api.PEAK_STATS)[0], res[1].numpy(),
-                           res[2].numpy())
-                else:
-                    res = tuple(a.numpy() for a in res)
+                    res = (np.frombuffer(res[0].tobytes(), api.PEAK_STATS)[0], res[1], res[2])
                 self.samples.free(lv.soff, lv.req.n)
                 self.outs.free(lv.ooff, lv.req.outputs)
                 self._desc_arena(lv.req.kind).free(lv.desc, 1)
@@ -704,6 +744,19 @@ class TransitServer:
     def hbm_high_water(self) -> int:
         """Bytes of arena space held by admitted requests at the busiest moment."""
         return self.samples.high_water * SAMPLE_BYTES + self.outs.high_water * OUTPUT_BYTES
+
+
+_NP_DTYPES = {}
+
+
+def _row(t: torch.Tensor, k: int):
+    """(device address, bytes, numpy dtype) of row k of a contiguous device tensor (element k
+    of a 1-D one)."""
+    per = t.numel() // t.shape[0] * t.element_size()
+    dt = _NP_DTYPES.get(t.dtype)
+    if dt is None:
+        dt = _NP_DTYPES[t.dtype] = torch.empty(0, dtype=t.dtype).numpy().dtype
+    return t.data_ptr() + k * per, per, dt
 
 
 def _runs(slots):

@@ -64,6 +64,14 @@ typedef struct {
   size_t bytes;
 } gtrap_copy;
 int gtrap_copy_async(const gtrap_copy *copies, uint32_t count, gtrap_stream_t stream);
+/* Stream-ordered device-to-device gather in one kernel: copy k moves copies[k].bytes from
+ * device address copies[k].src to device address copies[k].dst.  The host list (count <=
+ * list_cap entries, null pointers rejected) is first copied into list_dev, a device buffer the
+ * caller keeps for the stream; many small ranges then cost one copy and one launch instead of
+ * one copy each (a served step gathers its finishing requests' outputs into one buffer for a
+ * single device-to-host copy).  No counterpart in the reference. */
+int gtrap_gather_async(const gtrap_copy *copies, uint32_t count, gtrap_copy *list_dev, uint32_t list_cap,
+                       gtrap_stream_t stream);
 
 /* ---------------------------------------------------------------------------
  * Median-filter detrend.  Replaces the gfilter kernel (gtrap/gfilter.py:13-86)

@@ -22,6 +22,7 @@ def _server(**kw):
     kw.setdefault("hbm_budget", 64e6)
     kw.setdefault("bls_tiles", 60)   # small steps: requests span several steps
     kw.setdefault("tls_tiles", 30)
+    kw.setdefault("history", 1000)   # results returned by earlier step() calls, for the tests
     return S.TransitServer(BLS, TLS, detrend_r=R, **kw)
 
 

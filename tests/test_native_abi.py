@@ -73,6 +73,15 @@ def test_copy_list_validation_needs_no_gpu(lib):
     assert lib.gtrap_copy_async(rows.ctypes.data, 1, None) == 0
 
 
+def test_gather_list_validation_needs_no_gpu(lib):
+    assert lib.gtrap_gather_async(None, 0, None, 0, None) == 0       # nothing to gather
+    assert lib.gtrap_gather_async(None, 3, None, 8, None) == _native.ERR_INVALID_ARG
+    import numpy as np
+    rows = np.array([[0, 0, 16]], np.uint64)
+    assert lib.gtrap_gather_async(rows.ctypes.data, 1, None, 8, None) == _native.ERR_INVALID_ARG
+    assert b"null" in lib.gtrap_last_error()
+
+
 def test_workspace_sizes_are_host_side(lib):
     a = lib.gtrap_geebls_workspace_size(65536, 1024, 0)
     b = lib.gtrap_geebls_workspace_size(65536, 1024, _native.BLS_PHASE_FP32_REF)
