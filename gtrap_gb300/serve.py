@@ -233,13 +233,16 @@ class TransitServer:
     ``sample_share``; a request whose samples or outputs alone exceed an arena is rejected
     by :meth:`submit`.  Results are returned by :meth:`step`, :meth:`poll` and
     :meth:`run_until_idle`; ``history`` > 0 also keeps the last ``history`` of them in
-    ``results`` (their arrays hold pinned host memory until released)."""
+    ``results`` (their arrays hold pinned host memory until released).  A step admits at
+    most ``admit_samples`` samples of new requests (at least one request), so that a burst is
+    staged over several steps while the earlier steps' kernels run."""
 
     def __init__(self, bls: BlsSpec = BlsSpec(), tls: TlsSpec = TlsSpec(), detrend_r: int = 24,
                  hbm_budget: float = 100e9, sample_share: float = 0.8, bls_tiles: int | None = None,
                  tls_tiles: int | None = None, F: int | None = None, max_requests: int = 1 << 16,
                  depth: int = 2, tls_peaks: dict | None = None, device=None, fold: FoldSpec = FoldSpec(),
-                 fold_tiles: int | None = None, spectrum_stats: bool = False, history: int = 0):
+                 fold_tiles: int | None = None, spectrum_stats: bool = False, history: int = 0,
+                 admit_samples: int = 1 << 22):
         require_cuda()
         self.dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         self.bls_spec, self.tls_spec, self.fold_spec = bls, tls, fold
@@ -254,6 +257,7 @@ class TransitServer:
         self.tls_tiles = int(tls_tiles) if tls_tiles else sms * 64
         self.depth = max(1, int(depth))
         self.max_step_scale = 16  # a step's tile budget grows up to this factor under load
+        self.admit_samples = max(1, int(admit_samples))   # samples admitted a step (32 MB staged)
         self.tls_peaks = None if tls_peaks is None else dict(mpd=10, ntop=4, k=8) | dict(tls_peaks)
         self.spectrum_stats = bool(spectrum_stats)
         budget = int(hbm_budget)
@@ -334,9 +338,14 @@ class TransitServer:
     # -- one step -------------------------------------------------------------------------
     def _admit(self, now):
         new = []
+        staged = 0
         while self.waiting:
             lv = self.waiting[0]
             req = lv.req
+            # at most admit_samples samples a step (at least one request): a burst is staged
+            # over several steps, each upload overlapping the kernels of the steps before it
+            if new and staged + req.n > self.admit_samples:
+                break
             desc_arena = self._desc_arena(req.kind)
             s = self.samples.alloc(req.n)
             if s is None:
@@ -351,6 +360,7 @@ class TransitServer:
                 self.outs.free(o, req.outputs)
                 break
             self.waiting.popleft()
+            staged += req.n
             lv.soff, lv.ooff, lv.desc, lv.admitted = s, o, dsl, now
             if req.kind == "bls":
                 lv.tiles = (req.nf + self.F - 1) // self.F

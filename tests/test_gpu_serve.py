@@ -79,6 +79,18 @@ def test_admission_by_hbm_budget(solo):
         srv.submit(big)
 
 
+def test_admission_cap_spreads_a_burst(solo):
+    """A burst larger than admit_samples is admitted over several steps (at least one request
+    a step), with every result equal to its solo run."""
+    reqs, ref = solo
+    srv = _server(admit_samples=6000)
+    rids = [srv.submit(r) for r in reqs]
+    res = {r.rid: r for r in srv.run_until_idle()}
+    assert len({r.admitted for r in res.values()}) > 2
+    for k, rid in enumerate(rids):
+        _eq(res[rid].outputs, ref[k])
+
+
 def test_plain_server_and_trace(solo):
     reqs, ref = solo
     plain = S.PlainServer(BLS, TLS, detrend_r=R)
