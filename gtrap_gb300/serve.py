@@ -371,15 +371,13 @@ class TransitServer:
             new.append(lv)
         return new
 
-    def _upload_samples(self, new, keep):
-        """Copy the new curves' samples (pinned staging, copy stream); returns the event the
-        compute stream waits for."""
+    def _upload_samples(self, new, keep, cp):
+        """Stage the new curves' samples (pinned) and add their copies to ``cp``."""
         total = sum(lv.req.n for lv in new)
         th = self.staging.take(4 * total)
         xh = self.staging.take(4 * total)
         keep += [th, xh]
         tn, xn = th.numpy().view(np.float32), xh.numpy().view(np.float32)
-        cp = _Copies()
         p = 0
         tb, xb = th.data_ptr(), xh.data_ptr()
         td, xd = self.t.data_ptr(), self.x.data_ptr()
@@ -390,17 +388,12 @@ class TransitServer:
             cp.add(td + 4 * lv.soff, tb + 4 * p, 4 * n)
             cp.add(xd + 4 * lv.soff, xb + 4 * p, 4 * n)
             p += n
-        # Slots are freed only after the last step reading them has finished, so the copy
-        # need not wait for the compute stream and overlaps the steps in flight.
-        cp.issue(self.h2d.cuda_stream)
-        ev = torch.cuda.Event()
-        ev.record(self.h2d)
-        return ev
 
-    def _meta(self, si, new, bls_segs, tls_segs, fold_segs, extra, keep):
+    def _meta(self, si, new, bls_segs, tls_segs, fold_segs, extra, keep, cp):
         """The step's descriptor rows, detrend list, work queues and the index arrays of its
         statistics (``extra``) in one pinned block, copied on the compute stream into the
-        step's device metadata slot; returns device views of the arrays, then nb, nt, nfd."""
+        step's device metadata slot; returns the device addresses of the detrend list and the
+        work queues followed by device views of the ``extra`` arrays, then nb, nt, nfd."""
         nb = [lv for lv in new if lv.req.kind == "bls"]
         nt = [lv for lv in new if lv.req.kind == "tls"]
         nfd = [lv for lv in new if lv.req.kind == "fold"]
@@ -439,14 +432,15 @@ class TransitServer:
         keep.append(host)
         hn = host.numpy()
         for a, o in zip(arrays, offs):
-            hn[o:o + a.nbytes] = np.frombuffer(a.tobytes(), np.uint8)
+            if a.nbytes:
+                hn[o:o + a.nbytes] = np.ascontiguousarray(a).reshape(-1).view(np.uint8)
         for (r_, _, _, _), o in zip(rows, roffs):
-            hn[o:o + r_.nbytes] = np.frombuffer(r_.tobytes(), np.uint8)
+            if r_.nbytes:
+                hn[o:o + r_.nbytes] = r_.view(np.uint8)
         slot = self.meta_dev[si % len(self.meta_dev)]
         if arrays_end > slot.numel():
             slot = torch.empty(arrays_end, dtype=torch.uint8, device=self.dev)   # compute stream
             keep.append(slot)
-        cp = _Copies()
         hb, db = host.data_ptr(), slot.data_ptr()
         cp.add(db, hb, arrays_end)
         # descriptor rows go straight to their slots (new requests get consecutive slots
@@ -462,8 +456,10 @@ class TransitServer:
             else:
                 for k, sl in enumerate(slots):
                     cp.add(tb + sl * sz, hb + o + k * sz, sz)
-        cp.issue(self.stream.cuda_stream)
-        views = [slot[o:o + max(a.nbytes, 8)] for a, o in zip(arrays, offs)]
+        # device addresses of the work-queue arrays; torch views only of the statistics' index
+        # arrays, which the statistics functions take as tensors
+        sb = slot.data_ptr()
+        views = [sb + o for o in offs[:8]] + [slot[o:o + max(a.nbytes, 8)] for a, o in zip(arrays[8:], offs[8:])]
         return views, nb, nt, nfd
 
     def _take(self, live, budget, cost):
@@ -534,11 +530,22 @@ class TransitServer:
         for kind in fin_st:
             extra.append(np.array([lv.desc for lv in fin_st[kind]], np.int32))
         with torch.cuda.stream(st):   # the statistics' outputs are allocated on the compute stream
+            # the new samples and the step's metadata in one copy list: on the copy stream
+            # when there are samples (overlapping the steps in flight; the metadata slot and
+            # the staging were last read by a step that has finished), else on the compute
+            # stream
+            cp = _Copies()
             if new:
-                ev = self._upload_samples(new, keep)
+                self._upload_samples(new, keep, cp)
+            views, nb, nt, nfd = self._meta(si, new, bls_segs, tls_segs, fold_segs, extra, keep, cp)
+            if new:
+                cp.issue(self.h2d.cuda_stream)
+                ev = torch.cuda.Event()
+                ev.record(self.h2d)
                 st.wait_event(ev)
-            views, nb, nt, nfd = self._meta(si, new, bls_segs, tls_segs, fold_segs, extra, keep)
-            p_goff, p_gn, p_bsg, p_bcum, p_tsg, p_tcum, p_fsg, p_fcum = (v.data_ptr() for v in views[:8])
+            else:
+                cp.issue(h)
+            p_goff, p_gn, p_bsg, p_bcum, p_tsg, p_tcum, p_fsg, p_fcum = views[:8]
             if new:
                 N.call("gtrap_gfilter_packed", as_ptr(self.x), as_ptr(self.resid), p_goff, p_gn,
                        len(new), max(lv.req.n for lv in new), self.r, h)
