@@ -91,6 +91,33 @@ def test_admission_cap_spreads_a_burst(solo):
         _eq(res[rid].outputs, ref[k])
 
 
+def test_gathered_output_copies_equal_solo(solo, monkeypatch):
+    """Every step's output copies through the device gather (one kernel, one device-to-host
+    copy): results equal the solo runs, with full outputs and with the statistics records."""
+    reqs, ref = solo
+    monkeypatch.setattr(S, "GATHER_MIN", 1)
+    srv = _server()
+    rids = [srv.submit(r) for r in reqs]
+    res = {r.rid: r for r in srv.run_until_idle()}
+    for k, rid in enumerate(rids):
+        _eq(res[rid].outputs, ref[k])
+    monkeypatch.setattr(S, "GATHER_MIN", 1 << 30)   # one copy per range
+    plain = _server(tls_peaks=dict(mpd=10, ntop=4, k=5), spectrum_stats=True)
+    rids = [plain.submit(r) for r in reqs]
+    direct = {r.rid: r.outputs for r in plain.run_until_idle()}
+    monkeypatch.setattr(S, "GATHER_MIN", 1)         # every range through the gather
+    srv = _server(tls_peaks=dict(mpd=10, ntop=4, k=5), spectrum_stats=True)
+    rids2 = [srv.submit(r) for r in reqs]
+    got = {r.rid: r.outputs for r in srv.run_until_idle()}
+    for a, b in zip(rids, rids2):
+        x, y = direct[a], got[b]
+        if isinstance(x, tuple):
+            for u, v in zip(x, y):
+                np.testing.assert_array_equal(u, v)
+        else:
+            assert x.tobytes() == y.tobytes()
+
+
 def test_plain_server_and_trace(solo):
     reqs, ref = solo
     plain = S.PlainServer(BLS, TLS, detrend_r=R)
