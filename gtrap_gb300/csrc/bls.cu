@@ -253,12 +253,26 @@ __global__ void __launch_bounds__(32) bls_ragged_offset_kernel(gtrap_bls_curve *
                                                                const float *__restrict__ resid) {
   const gtrap_bls_curve c = curves[blockIdx.x];
   float sum = 0.0f, comp = 0.0f;
-  for (uint32_t i = threadIdx.x; i < c.n; i += 32) {
-    if (!(__ldg(t + c.off + i) < 0.0f)) {
-      const float v = __ldg(resid + c.off + i);
-      const float s = sum + v;
-      comp += (fabsf(sum) >= fabsf(v)) ? ((sum - s) + v) : ((v - s) + sum);
-      sum = s;
+  // lane k adds samples k, k + 32, ... in order (the image kernel's partition, so the two
+  // offsets agree bit for bit); kU of them are loaded before any is added, which keeps
+  // the loads in flight instead of one memory latency per sample
+  constexpr int kU = 16;
+  for (uint32_t i0 = threadIdx.x; i0 < c.n; i0 += 32 * kU) {
+    float tv[kU], rv[kU];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const uint32_t i = i0 + 32 * u;
+      tv[u] = i < c.n ? __ldg(t + c.off + i) : -1.0f;
+      rv[u] = i < c.n ? __ldg(resid + c.off + i) : 0.0f;
+    }
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      if (!(tv[u] < 0.0f)) {
+        const float v = rv[u];
+        const float s = sum + v;
+        comp += (fabsf(sum) >= fabsf(v)) ? ((sum - s) + v) : ((v - s) + sum);
+        sum = s;
+      }
     }
   }
   const double part = (double)sum + (double)comp;

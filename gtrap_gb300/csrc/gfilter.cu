@@ -155,14 +155,26 @@ __global__ void __launch_bounds__(1024) offset_kernel(const float *__restrict__ 
   const int q = blockIdx.x * 32 + lane;
   float sum = 0.0f, comp = 0.0f;
   if (q < nq) {
-    for (long long i = row; i < n; i += 32) {
-      const size_t idx = (size_t)i * nq + q;
-      const float t = __ldg(tu + idx);
-      if (!(t < 0.0f)) {
-        const float v = __ldg(resid + idx);
-        const float s = sum + v;
-        comp += (fabsf(sum) >= fabsf(v)) ? ((sum - s) + v) : ((v - s) + sum);
-        sum = s;
+    // rows row, row + 32, ... in order; kU of them loaded before any is added (the loads
+    // stay in flight instead of one memory latency per row)
+    constexpr int kU = 8;
+    for (long long i0 = row; i0 < n; i0 += 32 * kU) {
+      float tv[kU], rv[kU];
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        const long long i = i0 + 32 * u;
+        const size_t idx = (size_t)i * nq + q;
+        tv[u] = i < n ? __ldg(tu + idx) : -1.0f;
+        rv[u] = i < n ? __ldg(resid + idx) : 0.0f;
+      }
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        if (!(tv[u] < 0.0f)) {
+          const float v = rv[u];
+          const float s = sum + v;
+          comp += (fabsf(sum) >= fabsf(v)) ? ((sum - s) + v) : ((v - s) + sum);
+          sum = s;
+        }
       }
     }
   }
@@ -233,9 +245,10 @@ int gtrap_gfilter_packed(const float *in, float *out, const uint64_t *off, const
   while (warps > 1 && per_warp * warps > 56 * 1024) --warps;
   // rows per lane: long runs amortise each lane's initial sort (about w^2 / 4 steps) over a
   // big batch; a few curves (a served step) get short runs so that their rows still spread
-  // over about 20,000 lanes (a run costs about its length in dependent row updates)
+  // over many lanes (a run costs about its length in dependent row updates)
   const size_t rows = (size_t)max_n * ncurves;  // upper bound of the batch's rows
-  const size_t lanes_wanted = (size_t)sm_count() * 128;
+  // rows is an upper bound (the longest curve times the count), so aim at 512 lanes an SM
+  const size_t lanes_wanted = (size_t)sm_count() * 512;
   size_t run_fill = (rows + lanes_wanted - 1) / lanes_wanted;
   int run = (int)(8 * w);
   if (run < 64) run = 64;
