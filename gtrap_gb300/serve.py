@@ -31,6 +31,7 @@ drivers launch one kernel per image (gtrap/geebls.py:10-22, gtrap/gtls.py:11-27)
 from __future__ import annotations
 
 import collections
+import functools
 import time
 from dataclasses import dataclass, field
 
@@ -67,8 +68,9 @@ class Request:
     dw: float = 0.0
     deltat: float = 0.0
 
-    @property
+    @functools.cached_property
     def n(self) -> int:
+        """Samples (computed once: the server reads it many times per request)."""
         return int(np.asarray(self.t).size)
 
     @property
@@ -196,6 +198,7 @@ class _Copies:
 
 
 GATHER_MIN = 16   # a step's output copies from this many on go through one device gather
+_SERIES = {"bls": 3, "fold": 4, "tls": 5}   # output series a request of each kind returns
 
 
 @dataclass
@@ -636,6 +639,8 @@ class TransitServer:
                 t_.record_stream(self.d2h)
         # per request and output series: (device address, bytes, numpy dtype)
         plans = []
+        optr = [a.data_ptr() for a in self.o]
+        f32 = np.dtype(np.float32)
         for lv in step.finishing:
             m, o = lv.req.outputs, lv.ooff
             if lv.st_slot >= 0 and lv.req.kind in step.bstats:
@@ -646,8 +651,7 @@ class TransitServer:
                 srcs = [(st_.data_ptr() + lv.pk_slot * rs, rs, np.dtype(np.uint8)),
                         _row(idx, lv.pk_slot), _row(val, lv.pk_slot)]
             else:
-                series = {"bls": 3, "fold": 4}.get(lv.req.kind, 5)
-                srcs = [(self.o[j].data_ptr() + 4 * o, 4 * m, np.dtype(np.float32)) for j in range(series)]
+                srcs = [(optr[j] + 4 * o, 4 * m, f32) for j in range(_SERIES[lv.req.kind])]
             plans.append(srcs)
         total = sum((nb + 15) // 16 * 16 for srcs in plans for _, nb, _ in srcs)
         # a power-of-two block (at least 64 KB), so that released blocks serve later steps
@@ -703,8 +707,13 @@ class TransitServer:
             self.steps.popleft()
         out = []
         keep = []
+        done_ev = {}   # one query per copy event (a step's requests share one)
         for lv in self.draining:
-            if lv.d2h_event.query():
+            ev = lv.d2h_event
+            ready = done_ev.get(id(ev))
+            if ready is None:
+                ready = done_ev[id(ev)] = ev.query()
+            if ready:
                 now = time.perf_counter()
                 res = lv.result   # numpy views of the step's pinned block
                 if lv.st_slot >= 0:
