@@ -160,7 +160,7 @@ class _Staging:
     step is launched only while fewer than ``depth`` are in flight, and a step's kernels
     wait for its uploads).  A step that needs more than a slot gets a fresh pinned buffer."""
 
-    def __init__(self, depth: int, slot_bytes: int = 32 << 20):
+    def __init__(self, depth: int, slot_bytes: int = 40 << 20):
         self.slot_bytes = slot_bytes
         self.slots = [torch.empty(slot_bytes, dtype=torch.uint8, pin_memory=True) for _ in range(depth)]
         self.cur = None
@@ -260,7 +260,9 @@ class TransitServer:
         self.tls_tiles = int(tls_tiles) if tls_tiles else sms * 64
         self.depth = max(1, int(depth))
         self.max_step_scale = 16  # a step's tile budget grows up to this factor under load
-        self.admit_samples = max(1, int(admit_samples))   # samples admitted a step (32 MB staged)
+        # samples admitted a step: 4 M samples are 32 MB of staged times and fluxes, which with
+        # the step's metadata fit one 40 MB staging slot
+        self.admit_samples = max(1, int(admit_samples))
         self.tls_peaks = None if tls_peaks is None else dict(mpd=10, ntop=4, k=8) | dict(tls_peaks)
         self.spectrum_stats = bool(spectrum_stats)
         budget = int(hbm_budget)
