@@ -691,6 +691,9 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
   if (kma > kmi) {
     // each thread takes the starts kSeedStride * (tid + kThreads j) of one frequency at a time
     // and keeps its best; one warp argmax and one exact quotient per warp and frequency
+    // unrolled by three: independent frequencies' load and shuffle chains interleave
+    // (measured 0.4 % faster than one frequency at a time)
+#pragma unroll 3
     for (uint32_t f = 0; f < nfrem; ++f) {
       const float2 *P = reinterpret_cast<const float2 *>(sm + (size_t)f * a.region);
       float pa = 0.0f;
