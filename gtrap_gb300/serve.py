@@ -804,14 +804,15 @@ def _runs(slots):
 class PlainServer:
     """Baseline: each request is processed alone, in arrival order, by the plain entry points
     (copy in, gfilter, get_offset, geebls, tls_fold or gtls, copy out), as a caller of the
-    reference's per-image kernels does."""
+    reference's per-image kernels does.  ``process`` returns each result; ``history`` > 0 also
+    keeps the last ``history`` of them in ``results``."""
 
     def __init__(self, bls: BlsSpec = BlsSpec(), tls: TlsSpec = TlsSpec(), detrend_r: int = 24,
-                 device=None, fold: FoldSpec = FoldSpec()):
+                 device=None, fold: FoldSpec = FoldSpec(), history: int = 0):
         require_cuda()
         self.dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         self.bls_spec, self.tls_spec, self.fold_spec, self.r = bls, tls, fold, int(detrend_r)
-        self.results: list = []
+        self.results: collections.deque = collections.deque(maxlen=max(0, int(history)))
         self.next_rid = 0
 
     def process(self, req: Request, arrival: float | None = None) -> Result:
