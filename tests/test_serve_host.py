@@ -70,3 +70,19 @@ def test_request_outputs_per_kind():
         r = S.Request.from_curve(c)
         assert r.kind == c["kind"] and r.n == c["x"].size
         assert r.outputs == (c["nf"] if c["kind"] == "bls" else c["x"].size)
+
+
+def test_row_addresses_of_statistics_buffers():
+    """The result copies address row k of a statistics buffer (element k of a 1-D one) with
+    its byte size and numpy dtype, without framework views."""
+    import torch
+    from gtrap_gb300.serve import _row
+    a = torch.zeros(7, dtype=torch.float64)
+    p, nb, dt = _row(a, 3)
+    assert p == a.data_ptr() + 3 * 8 and nb == 8 and dt == np.float64
+    b = torch.zeros((5, 96), dtype=torch.uint8)
+    p, nb, dt = _row(b, 4)
+    assert p == b.data_ptr() + 4 * 96 and nb == 96 and dt == np.uint8
+    c = torch.zeros((3, 8), dtype=torch.int32)
+    p, nb, dt = _row(c, 2)
+    assert p == c.data_ptr() + 2 * 32 and nb == 32 and dt == np.int32
