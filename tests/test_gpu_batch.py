@@ -195,3 +195,13 @@ def test_degenerate_curves_equal_plain(cuda):
             for a, b in zip(g, w):
                 np.testing.assert_array_equal(a, b)
     assert np.all(got[0][2][0] == 0) and np.all(got[1][2][0] == 0)  # all masked: no window
+
+
+def test_tile_plan_keeps_two_blocks_per_sm(cuda):
+    """At the benchmark's grid (nb 2048, kma 205) a tile holds six frequencies and two blocks
+    share an SM: the tile budget counts the kernels' static shared memory and the per-block
+    reservation (a few hundred more static bytes once cost the second block)."""
+    from gtrap_gb300 import _native as N
+    # the plan subtracts the kernels' queried static shared memory and the reservation from
+    # half an SM: more static bytes would drop F to 5 here
+    assert int(N.fn("gtrap_bls_tile_frequencies")(2048, 205)) == 6
