@@ -69,7 +69,8 @@ int gtrap_copy_async(const gtrap_copy *copies, uint32_t count, gtrap_stream_t st
  * list_cap entries, null pointers rejected) is first copied into list_dev, a device buffer the
  * caller keeps for the stream; many small ranges then cost one copy and one launch instead of
  * one copy each (a served step gathers its finishing requests' outputs into one buffer for a
- * single device-to-host copy).  No counterpart in the reference. */
+ * single device-to-host copy).  The copies run concurrently: destination ranges must not
+ * overlap each other or any source range.  No counterpart in the reference. */
 int gtrap_gather_async(const gtrap_copy *copies, uint32_t count, gtrap_copy *list_dev, uint32_t list_cap,
                        gtrap_stream_t stream);
 
