@@ -89,6 +89,13 @@ def test_admission_cap_spreads_a_burst(solo):
     assert len({r.admitted for r in res.values()}) > 2
     for k, rid in enumerate(rids):
         _eq(res[rid].outputs, ref[k])
+    # a cap below every request's size: one request a step
+    srv = _server(admit_samples=100)
+    rids = [srv.submit(r) for r in reqs]
+    res = {r.rid: r for r in srv.run_until_idle()}
+    assert len({r.admitted for r in res.values()}) == len(reqs)
+    for k, rid in enumerate(rids):
+        _eq(res[rid].outputs, ref[k])
 
 
 def test_gathered_output_copies_equal_solo(solo, monkeypatch):
