@@ -660,6 +660,18 @@ def ragged_parity(mix, bat, n_curves=16, fstride=8):
     return out
 
 
+def saturation(S, server, pool, out=None):
+    """Every request of ``pool`` offered at once; throughput and latency over the whole run.
+    Each result's arrays are released as it arrives (its byte count kept); ``out`` collects
+    the results."""
+    t0 = time.perf_counter()
+    res = S.serve_trace(server, pool, np.zeros(len(pool)), keep_outputs=False)
+    wall = time.perf_counter() - t0
+    if out is not None:
+        out.extend(res)
+    return S.latency_summary(res, wall)
+
+
 def served_block(dev, rank, npool=600, fracs=(0.1, 0.5, 0.9)):
     """The continuous-batching server on a Poisson pool of single-curve requests (BLS or GTLS
     50/50, detrended; n log-uniform [1000, 70000]): saturation throughput and p50/p99 latency
@@ -671,22 +683,21 @@ def served_block(dev, rank, npool=600, fracs=(0.1, 0.5, 0.9)):
     for r in pool[:40]:
         srv.submit(r)
     srv.run_until_idle()
-    t0 = time.perf_counter()
-    for r in pool:
-        srv.submit(r, t0)
-    sat = S.latency_summary(srv.run_until_idle(), time.perf_counter() - t0)
+    # results are released as they arrive (a consuming client), in every run below
+    sat = saturation(S, srv, pool)
     plain = S.PlainServer(detrend_r=R_MEDIAN)
     for r in pool[:10]:
         plain.process(r)
-    t0 = time.perf_counter()
-    psat = S.latency_summary([plain.process(r, t0) for r in pool[:200]], time.perf_counter() - t0)
+    psat = saturation(S, plain, pool[:200])
     sweep = []
     for frac in fracs:
         rate = frac * sat["req_per_s"]
         m = min(npool, max(200, int(rate * 1.0)))
-        s = S.latency_summary(S.serve_trace(srv, pool[:m], S.poisson_trace(m, rate, seed=int(frac * 1000))))
+        s = S.latency_summary(S.serve_trace(srv, pool[:m], S.poisson_trace(m, rate, seed=int(frac * 1000)),
+                                            keep_outputs=False))
         pm = min(200, max(60, int(rate * 0.3)))
-        ps = S.latency_summary(S.serve_trace(plain, pool[:pm], S.poisson_trace(pm, rate, seed=int(frac * 1000))))
+        ps = S.latency_summary(S.serve_trace(plain, pool[:pm], S.poisson_trace(pm, rate, seed=int(frac * 1000)),
+                                             keep_outputs=False))
         sweep.append({"offered_frac": frac, "offered_req_per_s": rate, "requests": m,
                       "served_req_per_s": s["req_per_s"], "p50_ms": s["p50_ms"], "p99_ms": s["p99_ms"],
                       "evals_per_s": s["evals_per_s"],
@@ -1453,26 +1464,23 @@ def run_served(args, rank, world, local_rank):
     for r in pool[:40]:
         srv.submit(r)
     srv.run_until_idle()
-    t0 = time.perf_counter()
-    for r in pool:
-        srv.submit(r, t0)
-    res = srv.run_until_idle()
-    sat = S.latency_summary(res, time.perf_counter() - t0)
+    # results are released as they arrive (a consuming client), in every run below
+    res = []
+    sat = saturation(S, srv, pool, res)
     plain = S.PlainServer(detrend_r=R_MEDIAN, fold=fspec)
     for r in pool[:10]:
         plain.process(r)
-    t0 = time.perf_counter()
-    pres = [plain.process(r, t0) for r in pool[:300]]
-    psat = S.latency_summary(pres, time.perf_counter() - t0)
+    psat = saturation(S, plain, pool[:300])
     sweep = []
     for frac in (0.1, 0.5, 0.9) if fold or peaks_only else (0.1, 0.2, 0.3, 0.4, 0.5, 0.6, 0.7, 0.8, 0.9, 1.0, 1.1, 1.2):
         rate = frac * sat["req_per_s"]
         m = min(npool, max(200, int(rate * 1.5)))
         offs = S.poisson_trace(m, rate, seed=int(frac * 1000))
-        s = S.latency_summary(S.serve_trace(srv, pool[:m], offs))
+        s = S.latency_summary(S.serve_trace(srv, pool[:m], offs, keep_outputs=False))
         prate = frac * sat["req_per_s"]
         pm = min(300, max(60, int(prate * 0.5)))
-        ps = S.latency_summary(S.serve_trace(plain, pool[:pm], S.poisson_trace(pm, prate, seed=int(frac * 1000))))
+        ps = S.latency_summary(S.serve_trace(plain, pool[:pm], S.poisson_trace(pm, prate, seed=int(frac * 1000)),
+                                             keep_outputs=False))
         sweep.append({"offered_frac": frac, "offered_req_per_s": rate, "requests": m,
                       "served_req_per_s": s["req_per_s"], "p50_ms": s["p50_ms"], "p99_ms": s["p99_ms"],
                       "evals_per_s": s["evals_per_s"],
@@ -1500,8 +1508,7 @@ def run_served(args, rank, world, local_rank):
     if rank != 0:
         return
     # bytes a request returns to the host: full series, or the statistics records
-    ret = [sum(np.asarray(o).nbytes for o in r.outputs) if isinstance(r.outputs, tuple) else np.asarray(r.outputs).nbytes
-           for r in res]
+    ret = [r.nbytes for r in res]
     line = {"metric": METRIC, "value": sat["evals_per_s"], "unit": UNIT, "n_gpus": world,
             "steps": 1, "warmup": 1, "ms_per_step": 1e3 * npool / sat["req_per_s"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+i64",

@@ -98,10 +98,18 @@ class Result:
     #                  record (pest, sde, ph1, ph2 and the refined best peak); fold with
     #                  spectrum_stats: a BLS_STATS record (ph1/ph2 = start bin, duration index)
     evals: int
+    nbytes: int = -1  # bytes of ``outputs``, recorded when a trace releases them (-1: not recorded)
 
     @property
     def latency(self) -> float:
         return self.done - self.arrival
+
+
+def output_nbytes(outputs) -> int:
+    """Bytes a result returns to the host: its arrays, or its statistics record."""
+    if isinstance(outputs, tuple):
+        return int(sum(np.asarray(o).nbytes for o in outputs))
+    return int(np.asarray(outputs).nbytes)
 
 
 class Arena:
@@ -746,17 +754,21 @@ class TransitServer:
 
     def wait(self, until: float | None = None):
         """Block until something can change: the oldest step finishes when the pipeline is
-        full, else a short sleep (bounded by ``until``, a perf_counter time)."""
+        full, else a short busy wait (bounded by ``until``, a perf_counter time).  The wait
+        spins instead of sleeping: a sleep's wake-up comes 50-100 us late on a loaded host, and
+        that delay would be added to the latency of every request arriving or finishing
+        meanwhile."""
         if len(self.steps) >= self.depth:
             self.steps[0].event.synchronize()
             return
-        dt = 0.00005
-        if until is not None:
-            dt = max(0.0, min(dt, until - time.perf_counter()))
         if self.draining and not self.steps and until is None:
             self.draining[0].d2h_event.synchronize()
-        elif dt > 0:
-            time.sleep(dt)
+            return
+        end = time.perf_counter() + 0.00005
+        if until is not None:
+            end = min(end, until)
+        while time.perf_counter() < end:
+            pass
 
     def run_until_idle(self) -> list:
         """Drive steps until every submitted request has completed."""
@@ -858,19 +870,30 @@ def poisson_trace(n_requests: int, rate: float, seed: int = 0) -> np.ndarray:
     return np.cumsum(rng.exponential(1.0 / rate, n_requests))
 
 
-def serve_trace(server, requests, offsets) -> list:
+def serve_trace(server, requests, offsets, keep_outputs: bool = True) -> list:
     """Offer ``requests[k]`` at ``offsets[k]`` seconds after the start (real time) and run the
     server until all have completed.  Works with :class:`TransitServer` and
-    :class:`PlainServer`; returns the results in completion order."""
+    :class:`PlainServer`; returns the results in completion order.  With ``keep_outputs``
+    false each result's arrays are released as soon as it arrives (``outputs`` = None), as a
+    client that consumes its results does: the server's pinned result blocks then return to
+    the pinned-memory cache for later steps instead of every step allocating a new one."""
     t0 = time.perf_counter()
     k = 0
     out = []
+
+    def take(results):
+        if not keep_outputs:
+            for r in results:
+                r.nbytes = output_nbytes(r.outputs)
+                r.outputs = None
+        out.extend(results)
+
     if isinstance(server, PlainServer):
         for k, req in enumerate(requests):
             arr = t0 + offsets[k]
             while time.perf_counter() < arr:
                 pass
-            out.append(server.process(req, arr))
+            take([server.process(req, arr)])
         return out
     n = len(requests)
     while k < n or not server.idle:
@@ -880,7 +903,7 @@ def serve_trace(server, requests, offsets) -> list:
             k += 1
         n0 = server.step_count
         got = server.step(now)
-        out += got
+        take(got)
         if server.step_count == n0 and not got:
             server.wait(t0 + offsets[k] if k < n else None)
     return out
