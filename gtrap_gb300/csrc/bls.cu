@@ -10,22 +10,25 @@
 // GB300 design:
 //  * prep: the [n, nq] time-major image is transposed once into curve-major arrays so
 //    every later read is coalesced.  Flux is quantised to a per-curve power-of-two fixed
-//    point (|x| < 2^30) and packed with a count of one into a 64-bit word, so a single
-//    integer shared atomic updates both the bin sum and the bin count; integer sums are
-//    exact and order independent, so every result is deterministic (a curve gives the
-//    same bits alone or batched).  Phases are exact: frac(t*fmin) and frac(t*df) of the
-//    float32 inputs are formed as 64-bit fixed-point fractions (the float products are
-//    exact in 48 bits), and frac(t*(fmin + j*df)) = A + j*B mod 2^64 with no rounding at
-//    all; the bin is the top log2(nb) bits.  This removes the FP32 phase drift of the
-//    reference (about 1e-5 cycles at t*f ~ 170) without any FP64 arithmetic in the fold.
+//    point (|x| < 2^30); integer bin sums are exact and order independent, so every result
+//    is deterministic (a curve gives the same bits alone or batched).  Phases are exact:
+//    frac(t*fmin) and frac(t*df) of the float32 inputs are formed as 64-bit fixed-point
+//    fractions (the float products are exact in 48 bits), and frac(t*(fmin + j*df)) =
+//    A + j*B mod 2^64 with no rounding at all; the bin is the top log2(nb) bits.  This
+//    removes the FP32 phase drift of the reference (about 1e-5 cycles at t*f ~ 170) without
+//    any FP64 arithmetic in the fold.
 //  * fold: one CTA per (curve, tile of F consecutive frequencies); every loaded sample is
-//    binned for all F frequencies (phase step = one 64-bit add).
-//  * scan: groups of Tg threads turn a histogram into exact integer prefix sums (rounded
-//    once to float), then each thread evaluates R consecutive start bins against every
-//    end bin with one padded, conflict-free 8-byte shared load per R candidates.  A
-//    division-free pre-test s^2 >= best' * den (best' = best*(1 - 2^-20)) admits every
-//    candidate that can tie or beat the running best; admitted candidates are compared
-//    exactly with a correctly rounded quotient and a lowest-(start, end) tie-break.
+//    binned for all F frequencies (phase step = one 64-bit add) with two 32-bit shared
+//    atomics per update, re-folded in a 64-bit format when a bin could overflow.
+//  * prefix: groups of Tg threads turn a histogram into exact integer prefix sums, rounded
+//    to float (correctly below 2^31 in magnitude, within one ulp above), plus the maximum
+//    and minimum of the flux prefix per 32-entry chunk.
+//  * scan: every frequency's running best is seeded from real windows; bound groups of
+//    starts against chunks of ends are dropped when their bound falls below it, rows of the
+//    surviving groups are bounded again, and only rows that pass run a division-free
+//    per-start pre-test and then the exact correctly rounded power with a lowest-(start, end)
+//    tie-break.  Every bound is conservative under float rounding, so the outputs equal an
+//    exhaustive scan of the same prefix arrays.
 #include <atomic>
 #include <type_traits>
 
@@ -356,6 +359,18 @@ __device__ __forceinline__ unsigned long long pack_key(float pw, int i, int e) {
 // while 32 consecutive entries still map onto the same aligned 32-entry block.
 __device__ __forceinline__ int swz(int e) { return e ^ ((e >> 4) & 7); }
 
+// int64 -> float off the FP64 pipe (the 64-bit conversion issues there, and that pipe is
+// narrow on this part): x = h * 2^32 + l with l the signed low word, so float(l) is correctly
+// rounded, h * 2^32 is exact (|x| < 2^56) and one FMA rounds the sum.  Correctly rounded when
+// |x| < 2^31 (h = 0), within one ulp above.  The prefix pass converts every entry with it
+// (BLS kernel 0.8 % faster than __ll2float_rn on the uneven mix); the scan reads only these
+// floats, so every bound and the exact comparison stay consistent with each other.
+__device__ __forceinline__ float ll2float_fast(long long x) {
+  const int l = (int)(unsigned)(x & 0xffffffffull);
+  const int h = (int)((x - (long long)l) >> 32);
+  return __fmaf_rn(__int2float_rn(h), 4294967296.0f, __int2float_rn(l));
+}
+
 constexpr int kSeedStride = 4;  // starts seeded per frequency: every fourth
 
 __device__ __forceinline__ void group_bar(int id, int nthreads) {
@@ -617,15 +632,15 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
     }
     // P[e] = (flux prefix, count prefix) over bins [0, e) of the wrapped axis, e <= nb + kma
     if (gtid == 0) P[0] = make_float2(0.0f, 0.0f);
-    float vmx = __ll2float_rn(ex), vmn = vmx;  // flux prefix over entries i0 .. i0 + R - 1
+    float vmx = ll2float_fast(ex), vmn = vmx;  // flux prefix over entries i0 .. i0 + R - 1
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       const int e = i0 + r + 1;
-      const float v = __ll2float_rn(ex + px[r]);
+      const float v = ll2float_fast(ex + px[r]);
       if (r < R - 1) { vmx = fmaxf(vmx, v); vmn = fminf(vmn, v); }
       if (e <= nb) {
         P[swz(e)] = make_float2(v, (float)(ec + pc[r]));
-        if (e <= kma) P[swz(nb + e)] = make_float2(__ll2float_rn(tx + ex + px[r]), (float)(tc + ec + pc[r]));
+        if (e <= kma) P[swz(nb + e)] = make_float2(ll2float_fast(tx + ex + px[r]), (float)(tc + ec + pc[r]));
       }
     }
     // chunk statistics of the chunks below nb (entries 32c .. 32c + 31 < nb) from the 32 / R
