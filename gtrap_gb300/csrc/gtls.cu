@@ -127,8 +127,20 @@ __device__ __forceinline__ void gtls_tile(const TlsArgs &a, const int e0) {
   float *pxl = pxh + S + 1;
   float *pqh = pxl + S + 1;              // [S+1] prefix of x^2 (hi, lo)
   float *pql = pqh + S + 1;
+  float *dlw = pql + S + 1;              // [nw] ingress step L / mm of each width
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+  // ---- the ingress step of every width, in the reference's double arithmetic (double
+  //      literals, include/gtls_simple.h:68; include/gtls_absolute.h:68): once per tile
+  //      instead of once per (epoch, width), which keeps the narrow FP64 pipe out of the loop
+  for (int wi = tid; wi < a.nw; wi += kTlsThreads) {
+    const float wf = (float)wi;
+    const float W = a.w_fma ? __fmaf_rn(-a.dw, wf, a.wmax) : __fsub_rn(a.wmax, __fmul_rn(a.dw, wf));
+    const double Wd = (double)W;
+    dlw[wi] = a.mode ? __double2float_rn(Wd / 4.0 / (double)a.nl)
+                     : __double2float_rn(Wd * 0.45 / (double)a.nl);
+  }
 
   // ---- stage the scoop union: (t + 1000) - 1000 rounding (include/gtls_simple.h:54-65)
   for (int s = tid; s < S; s += kTlsThreads) {
@@ -305,9 +317,7 @@ __device__ __forceinline__ void gtls_tile(const TlsArgs &a, const int e0) {
     const float m = Nw > 0 ? __fdiv_rn(df_diff(pxh[ubE], pxl[ubE], pxh[lbS], pxl[lbS]), (float)Nw) : 0.0f;
     const float SxAE = df_diff(pxh[ubE], pxl[ubE], pxh[ubS], pxl[ubS]);
     const float SSf = df_sumsq(pqh[ubE], pql[ubE], pqh[ubS], pql[ubS], m, SxAE, N);
-    const double Wd = (double)W;
-    const float dl = a.mode ? __double2float_rn(Wd / 4.0 / (double)nl)
-                            : __double2float_rn(Wd * 0.45 / (double)nl);
+    const float dl = dlw[wi];
     const float Wq = 0.25f * W;  // exact
     int bL = ub(-Wq), bR = bL;
     int dL = ub(Wq), dR = dL;
@@ -482,9 +492,9 @@ __global__ void __launch_bounds__(kTlsThreads, GTRAP_TLS_MINB) gtls_queue_kernel
   }
 }
 
-size_t tls_smem(int nsc) {
+size_t tls_smem(int nsc, int nw) {
   const int S = nsc + kTE - 1;
-  return (size_t)S * 8 + (size_t)(S + 1) * 20 + 64;
+  return (size_t)S * 8 + (size_t)(S + 1) * 20 + (size_t)nw * 4 + 64;
 }
 
 }  // namespace
@@ -508,7 +518,7 @@ int gtrap_gtls(float *tlssn, float *tlsw, float *tlst0, float *tlsl, float *tlsh
   if (!(deltat > 0.0f)) return fail(GTRAP_ERR_INVALID_ARG, "gtls: deltat must be positive");
   const long long tiles = ((long long)nt + kTE - 1) / kTE;
   if (tiles * nq >= (1LL << 31)) return fail(GTRAP_ERR_INVALID_ARG, "gtls: grid too large");
-  const size_t smem = tls_smem(nsc);
+  const size_t smem = tls_smem(nsc, nw);
   GTRAP_TRY(gtrap::ensure_smem((const void *)gtls_kernel, smem, "gtls"));
   TlsArgs ta;
   ta.sn = tlssn; ta.w = tlsw; ta.t0 = tlst0; ta.l = tlsl; ta.h = tlshmax;
@@ -536,7 +546,7 @@ int gtrap_gtls_run(const gtrap_tls_curve *curves, const gtrap_tls_segment *segs,
   if (max_nsc < 1 || max_nsc + kTE - 1 > kMaxStage)
     return fail(GTRAP_ERR_INVALID_ARG, "gtls_run: max_nsc=%d must be in [1, %d]", max_nsc, kMaxStage - kTE + 1);
   if (mode != 0 && mode != 1) return fail(GTRAP_ERR_INVALID_ARG, "gtls_run: mode must be 0 or 1");
-  const size_t smem = tls_smem(max_nsc);
+  const size_t smem = tls_smem(max_nsc, nw);
   GTRAP_TRY(gtrap::ensure_smem((const void *)gtls_queue_kernel, smem, "gtls_run"));
   TlsQueue qa;
   qa.curves = curves; qa.segs = segs; qa.cum = cum; qa.nseg = nseg; qa.t = t; qa.x = x;
