@@ -86,3 +86,44 @@ def test_row_addresses_of_statistics_buffers():
     c = torch.zeros((3, 8), dtype=torch.int32)
     p, nb, dt = _row(c, 2)
     assert p == c.data_ptr() + 2 * 32 and nb == 32 and dt == np.int32
+
+
+class _FakeServer:
+    """The step interface serve_trace drives: every submitted request completes at the next
+    step with two output arrays (no device involved)."""
+
+    def __init__(self):
+        self.pending, self.step_count, self.waits = [], 0, 0
+
+    @property
+    def idle(self):
+        return not self.pending
+
+    def submit(self, req, arrival):
+        self.pending.append((req, arrival))
+
+    def step(self, now):
+        from gtrap_gb300.serve import Result
+        if not self.pending:
+            return []
+        self.step_count += 1
+        out = [Result(k, "bls", arr, now, now, (np.zeros(req, np.float32), np.zeros(req, np.int32)), req)
+               for k, (req, arr) in enumerate(self.pending)]
+        self.pending = []
+        return out
+
+    def wait(self, until=None):
+        self.waits += 1
+
+
+def test_serve_trace_keeps_or_releases_outputs():
+    from gtrap_gb300.serve import output_nbytes, serve_trace
+    reqs = [3, 5, 8]
+    kept = serve_trace(_FakeServer(), reqs, np.zeros(3))
+    assert [r.outputs[0].size for r in kept] == reqs and all(r.nbytes == -1 for r in kept)
+    srv = _FakeServer()
+    rel = serve_trace(srv, reqs, np.array([0.0, 0.001, 0.002]), keep_outputs=False)
+    assert len(rel) == 3 and all(r.outputs is None for r in rel)
+    assert sorted(r.nbytes for r in rel) == [8 * n for n in reqs]   # float32 + int32 per element
+    assert srv.waits > 0   # idle gaps between arrivals go through the server's wait
+    assert output_nbytes(np.zeros((), np.dtype([("a", np.float64), ("b", np.int32)]))) == 12
