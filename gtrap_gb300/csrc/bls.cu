@@ -84,7 +84,7 @@ __device__ __forceinline__ bool sample_valid(const PrepArgs &a, uint32_t i, floa
   if (!isfinite(x)) return false;
   if (a.full && !(t >= 0.0f)) return false;  // include/geebls.h:67, INVT = 0.0
   if (!isfinite(t)) return false;
-  return isfinite((double)x - off);
+  return isfinite(off);  // (double)x - off is finite for finite x exactly when off is
 }
 
 // Per-curve power-of-two scale: 2^sx * max|x - offset| < xq_max.  Only the exponent of the
@@ -219,12 +219,13 @@ __global__ void __launch_bounds__(256) bls_ragged_scale_kernel(gtrap_bls_curve *
   __shared__ float pm[8];
   __shared__ uint32_t pc[8];
   const gtrap_bls_curve c = curves[blockIdx.x];
-  const double off = (double)c.offset;
+  // (double)xx - offset is finite for finite xx exactly when the offset is: no FP64 per sample
+  const bool off_ok = isfinite(c.offset);
   float amax = 0.0f;
   uint32_t cnt = 0;
   for (uint32_t i = threadIdx.x; i < c.n; i += 256) {
     const float tt = __ldg(t + c.off + i), xx = __ldg(x + c.off + i);
-    if (tt >= 0.0f && isfinite(tt) && isfinite(xx) && isfinite((double)xx - off)) {
+    if (tt >= 0.0f && isfinite(tt) && isfinite(xx) && off_ok) {
       amax = fmaxf(amax, fabsf(__fsub_rz(xx, c.offset)));
       ++cnt;
     }
@@ -248,23 +249,28 @@ __global__ void __launch_bounds__(256) bls_ragged_scale_kernel(gtrap_bls_curve *
 }
 
 // curves[q].offset = sum of resid over samples with t >= 0, divided by n (get_offset).  The
-// summation order is the one of gtrap_offset (lane k sums the samples i = k mod 32 in order
-// with Neumaier compensation; the 32 partials are added in lane order in double), so a packed
-// curve gets the same offset, to the bit, as the same curve in an [n, nq] image.
-__global__ void __launch_bounds__(32) bls_ragged_offset_kernel(gtrap_bls_curve *curves,
-                                                               const float *__restrict__ t,
-                                                               const float *__restrict__ resid) {
+// summation order is the one of gtrap_offset (256 partials, partial p summing the samples
+// i = p mod 256 in order with Neumaier compensation, each rounded to double as sum +
+// compensation; s_r = partials r, r + 32, ..., r + 224 in that order; offset = s_0 + ... +
+// s_31 in that order, over n), so a packed curve gets the same offset, to the bit, as the
+// same curve in an [n, nq] image.  One block of 256 threads per curve, thread p owning
+// partial p: a lone long curve is summed by eight warps with several loads in flight each.
+constexpr int kOffParts = 256;
+
+__global__ void __launch_bounds__(kOffParts) bls_ragged_offset_kernel(gtrap_bls_curve *curves,
+                                                                      const float *__restrict__ t,
+                                                                      const float *__restrict__ resid) {
+  __shared__ double part[kOffParts];
   const gtrap_bls_curve c = curves[blockIdx.x];
+  const uint32_t p = threadIdx.x;
   float sum = 0.0f, comp = 0.0f;
-  // lane k adds samples k, k + 32, ... in order (the image kernel's partition, so the two
-  // offsets agree bit for bit); kU of them are loaded before any is added, which keeps
-  // the loads in flight instead of one memory latency per sample
-  constexpr int kU = 16;
-  for (uint32_t i0 = threadIdx.x; i0 < c.n; i0 += 32 * kU) {
+  // samples p, p + 256, ... in order; kU of them are loaded before any is added
+  constexpr int kU = 8;
+  for (uint32_t i0 = p; i0 < c.n; i0 += kOffParts * kU) {
     float tv[kU], rv[kU];
 #pragma unroll
     for (int u = 0; u < kU; ++u) {
-      const uint32_t i = i0 + 32 * u;
+      const uint32_t i = i0 + kOffParts * u;
       tv[u] = i < c.n ? __ldg(t + c.off + i) : -1.0f;
       rv[u] = i < c.n ? __ldg(resid + c.off + i) : 0.0f;
     }
@@ -278,10 +284,16 @@ __global__ void __launch_bounds__(32) bls_ragged_offset_kernel(gtrap_bls_curve *
       }
     }
   }
-  const double part = (double)sum + (double)comp;
-  double acc = 0.0;
-  for (int k = 0; k < 32; ++k) acc += __shfl_sync(0xffffffffu, part, k);
-  if (threadIdx.x == 0) curves[blockIdx.x].offset = c.n ? (float)(acc / (double)c.n) : 0.0f;
+  part[p] = (double)sum + (double)comp;
+  __syncthreads();
+  if (p < 32) {
+    double sr = 0.0;
+#pragma unroll
+    for (int u = 0; u < kOffParts / 32; ++u) sr += part[p + 32 * u];
+    double acc = 0.0;
+    for (int k = 0; k < 32; ++k) acc += __shfl_sync(0xffffffffu, sr, k);
+    if (p == 0) curves[blockIdx.x].offset = c.n ? (float)(acc / (double)c.n) : 0.0f;
+  }
 }
 
 __global__ void __launch_bounds__(256) bls_ragged_pack_kernel(const gtrap_bls_curve *curves,
@@ -294,7 +306,7 @@ __global__ void __launch_bounds__(256) bls_ragged_pack_kernel(const gtrap_bls_cu
     const double off = (double)c.offset, scale = ldexp(1.0, c.sx);
     for (uint32_t i = blockIdx.x * 256 + threadIdx.x; i < c.n; i += gridDim.x * 256) {
       const float tt = __ldg(t + c.off + i), xx = __ldg(x + c.off + i);
-      const bool ok = tt >= 0.0f && isfinite(tt) && isfinite(xx) && isfinite((double)xx - off);
+      const bool ok = tt >= 0.0f && isfinite(tt) && isfinite(xx) && isfinite(off);
       X[c.off + i] = ok ? (int32_t)__double2ll_rn(((double)xx - off) * scale) : kMasked;
       if (AB) AB[c.off + i] = make_ulonglong2(frac64(tt, c.fmin), frac64(tt, c.df));
     }
@@ -1369,7 +1381,7 @@ int gtrap_bls_offsets(gtrap_bls_curve *curves, uint32_t ncurves, const float *t,
                       gtrap_stream_t stream) {
   if (ncurves == 0) return GTRAP_OK;
   if (!curves || !t || !resid) return fail(GTRAP_ERR_INVALID_ARG, "bls_offsets: null pointer");
-  bls_ragged_offset_kernel<<<ncurves, 32, 0, stream>>>(curves, t, resid);
+  bls_ragged_offset_kernel<<<ncurves, kOffParts, 0, stream>>>(curves, t, resid);
   return gtrap::check_launch("bls_ragged_offset_kernel");
 }
 

@@ -35,9 +35,11 @@ __global__ void __launch_bounds__(256) gfilter_kernel(const float *__restrict__ 
   const long long row1 = min((long long)n, row0 + rows_per_warp);
   const size_t stride = (size_t)nq;
 
-  // Sorted window of the first output row (insertion sort; amortised over the run).
-  for (int k = 0; k < w; ++k) {
-    const float v = load_padded(in, row0 - r + k, n, stride, q, qok);
+  // Sorted window of the first output row (insertion sort; amortised over the run).  The
+  // window's values are loaded first, all loads in flight together, then sorted in place.
+  for (int k = 0; k < w; ++k) S[32 * k] = load_padded(in, row0 - r + k, n, stride, q, qok);
+  for (int k = 1; k < w; ++k) {
+    const float v = S[32 * k];
     int j = k;
     while (j > 0) {
       const float u = S[32 * (j - 1)];
@@ -48,36 +50,44 @@ __global__ void __launch_bounds__(256) gfilter_kernel(const float *__restrict__ 
     S[32 * j] = v;
   }
 
+  // each row's three loads are issued one row ahead, under the previous row's window update
+  float xi = qok ? __ldg(in + (size_t)row0 * stride + q) : 0.0f;
+  float vold = load_padded(in, row0 - r, n, stride, q, qok);
+  float vnew = load_padded(in, row0 + r + 1, n, stride, q, qok);
   for (long long i = row0; i < row1; ++i) {
+    const bool more = i + 1 < row1;
+    const float xn = (qok && more) ? __ldg(in + (size_t)(i + 1) * stride + q) : 0.0f;
+    const float von = more ? load_padded(in, i + 1 - r, n, stride, q, qok) : 0.0f;
+    const float vnn = more ? load_padded(in, i + r + 2, n, stride, q, qok) : 0.0f;
     const float med = S[32 * r];
-    if (qok) out[(size_t)i * stride + q] = __fsub_rn(__ldg(in + (size_t)i * stride + q), med);
-    if (i + 1 >= row1) break;
-    const float vold = load_padded(in, i - r, n, stride, q, qok);
-    const float vnew = load_padded(in, i + r + 1, n, stride, q, qok);
-    if (vnew == vold) continue;
+    if (qok) out[(size_t)i * stride + q] = __fsub_rn(xi, med);
+    if (!more) break;
+    const float vo = vold, vn = vnew;
+    xi = xn; vold = von; vnew = vnn;
+    if (vn == vo) continue;
     // Lowest rank holding the leaving value (present in the window by construction).
     int lo = 0, hi = w - 1;
     while (lo < hi) {
       const int mid = (lo + hi) >> 1;
-      if (S[32 * mid] < vold) lo = mid + 1; else hi = mid;
+      if (S[32 * mid] < vo) lo = mid + 1; else hi = mid;
     }
     int j = lo;
-    if (vnew > vold) {
+    if (vn > vo) {
       while (j + 1 < w) {
         const float u = S[32 * (j + 1)];
-        if (!(u < vnew)) break;
+        if (!(u < vn)) break;
         S[32 * j] = u;
         ++j;
       }
     } else {
       while (j > 0) {
         const float u = S[32 * (j - 1)];
-        if (!(u > vnew)) break;
+        if (!(u > vn)) break;
         S[32 * j] = u;
         --j;
       }
     }
-    S[32 * j] = vnew;
+    S[32 * j] = vn;
   }
 }
 
@@ -102,8 +112,10 @@ __global__ void __launch_bounds__(256) gfilter_packed_kernel(const float *__rest
     if (row0 >= n) continue;
     const long long row1 = min(n, row0 + run);
     auto ld = [&](long long i) -> float { return (i >= 0 && i < n) ? __ldg(x + i) : 0.0f; };
-    for (int k = 0; k < w; ++k) {
-      const float v = ld(row0 - r + k);
+    // the window's values loaded first (all in flight together), then sorted in place
+    for (int k = 0; k < w; ++k) S[32 * k] = ld(row0 - r + k);
+    for (int k = 1; k < w; ++k) {
+      const float v = S[32 * k];
       int j = k;
       while (j > 0) {
         const float u = S[32 * (j - 1)];
@@ -113,52 +125,66 @@ __global__ void __launch_bounds__(256) gfilter_packed_kernel(const float *__rest
       }
       S[32 * j] = v;
     }
+    // each row's three loads are issued one row ahead, under the previous row's update
+    float xi = __ldg(x + row0), vold = ld(row0 - r), vnew = ld(row0 + r + 1);
     for (long long i = row0; i < row1; ++i) {
-      y[i] = __fsub_rn(__ldg(x + i), S[32 * r]);
-      if (i + 1 >= row1) break;
-      const float vold = ld(i - r), vnew = ld(i + r + 1);
-      if (vnew == vold) continue;
+      const bool more = i + 1 < row1;
+      const float xn = more ? __ldg(x + i + 1) : 0.0f;
+      const float von = more ? ld(i + 1 - r) : 0.0f;
+      const float vnn = more ? ld(i + r + 2) : 0.0f;
+      y[i] = __fsub_rn(xi, S[32 * r]);
+      if (!more) break;
+      const float vo = vold, vn = vnew;
+      xi = xn; vold = von; vnew = vnn;
+      if (vn == vo) continue;
       int lo = 0, hi = w - 1;
       while (lo < hi) {
         const int mid = (lo + hi) >> 1;
-        if (S[32 * mid] < vold) lo = mid + 1; else hi = mid;
+        if (S[32 * mid] < vo) lo = mid + 1; else hi = mid;
       }
       int j = lo;
-      if (vnew > vold) {
+      if (vn > vo) {
         while (j + 1 < w) {
           const float u = S[32 * (j + 1)];
-          if (!(u < vnew)) break;
+          if (!(u < vn)) break;
           S[32 * j] = u;
           ++j;
         }
       } else {
         while (j > 0) {
           const float u = S[32 * (j - 1)];
-          if (!(u > vnew)) break;
+          if (!(u > vn)) break;
           S[32 * j] = u;
           --j;
         }
       }
-      S[32 * j] = vnew;
+      S[32 * j] = vn;
     }
   }
 }
 
 // offset[q] = sum of resid over samples whose time is not negative, divided by n.
-// One block per 32 curves; each of the 32 warps sums every 32nd row with Neumaier
-// compensation; the 32 partials are combined in a fixed order (deterministic).
+// The summation order (shared with the packed batches' bls_ragged_offset_kernel, so a curve
+// gets the same offset to the bit in an image and in a packed batch): kOffParts = 256
+// partials, partial p summing the samples i = p mod 256 in order with Neumaier compensation;
+// each partial rounded to double as sum + compensation; s_r = the partials r, r + 32, ...,
+// r + 224 added in that order, and the offset = s_0 + s_1 + ... + s_31 in that order, divided
+// by n.  Here one block takes 32 curves (lane = curve, coalesced rows); thread (row, lane)
+// owns the partials row + 32u, u = 0..7, one load of each in flight per step.
+constexpr int kOffParts = 256;
+
 __global__ void __launch_bounds__(1024) offset_kernel(const float *__restrict__ resid,
                                                       const float *__restrict__ tu,
                                                       float *__restrict__ offset, int n, int nq) {
+  constexpr int kU = kOffParts / 32;
   __shared__ double part[32][33];
   const int lane = threadIdx.x, row = threadIdx.y;
   const int q = blockIdx.x * 32 + lane;
-  float sum = 0.0f, comp = 0.0f;
+  float sum[kU], comp[kU];
+#pragma unroll
+  for (int u = 0; u < kU; ++u) sum[u] = comp[u] = 0.0f;
   if (q < nq) {
-    // rows row, row + 32, ... in order; kU of them loaded before any is added (the loads
-    // stay in flight instead of one memory latency per row)
-    constexpr int kU = 8;
-    for (long long i0 = row; i0 < n; i0 += 32 * kU) {
+    for (long long i0 = row; i0 < n; i0 += kOffParts) {
       float tv[kU], rv[kU];
 #pragma unroll
       for (int u = 0; u < kU; ++u) {
@@ -171,14 +197,17 @@ __global__ void __launch_bounds__(1024) offset_kernel(const float *__restrict__ 
       for (int u = 0; u < kU; ++u) {
         if (!(tv[u] < 0.0f)) {
           const float v = rv[u];
-          const float s = sum + v;
-          comp += (fabsf(sum) >= fabsf(v)) ? ((sum - s) + v) : ((v - s) + sum);
-          sum = s;
+          const float t = sum[u] + v;
+          comp[u] += (fabsf(sum[u]) >= fabsf(v)) ? ((sum[u] - t) + v) : ((v - t) + sum[u]);
+          sum[u] = t;
         }
       }
     }
   }
-  part[row][lane] = (double)sum + (double)comp;
+  double sr = 0.0;
+#pragma unroll
+  for (int u = 0; u < kU; ++u) sr += (double)sum[u] + (double)comp[u];
+  part[row][lane] = sr;
   __syncthreads();
   if (row == 0 && q < nq) {
     double s = 0.0;
