@@ -23,7 +23,9 @@ in the reference's semantics on 4096 TESS-like curves x 18,000 epochs (8 widths 
 widths per epoch).  ``--workload tlsfold``: the folded trapezoid search (an extension) on the
 same curves: 8192 periods (0.5 .. 12 d) x 8 durations (0.5 .. 8 h) x 2048 phase bins.
 ``--workload served``: the continuous-batching server under Poisson arrivals (p50/p99
-latency per offered load).  ``--workload mock``: mock transit injection as the TESS mock driver
+latency per offered load).  ``--workload lone``: single requests (BLS and GTLS of about 5k, 20k
+and 60k samples) through an idle server and through the plain path, the latency floor of
+both.  ``--workload mock``: mock transit injection as the TESS mock driver
 does it (one drawn planet per curve, lc *= 2 - model, plus trends) on 4096 x 18,000 samples.
 ``--workload tlsfit``: the reference's CPU trapezoid fit (gtrap/tls.py tlsfit) on one TESS-like
 curve over 8 widths x 8 ingress lengths x 4320 epochs, in FP64.  ``--tls-kind fold`` sends the
@@ -71,7 +73,8 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="ragged",
-                   choices=["ragged", "masked", "served", "plain", "tls", "tlsfold", "mock", "tlsfit", "epilogue"])
+                   choices=["ragged", "masked", "served", "lone", "plain", "tls", "tlsfold", "mock", "tlsfit",
+                            "epilogue"])
     p.add_argument("--nq", type=int, default=None,
                    help="curves per GPU (default: 10,000 ragged, 1024 masked)")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -1754,6 +1757,66 @@ def run_tlsfit_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_lone(args, rank, world, local_rank):
+    """Lone requests: each of six requests (BLS and GTLS requests of about 5k, 20k and 60k
+    samples from the served pool's distribution) submitted to an idle server and run to
+    completion, ``--steps`` times, beside the plain per-request path on the same requests.
+    ``value`` is the evaluations of the requests over the sum of their median latencies."""
+    import torch
+    from gtrap_gb300 import _build, serve as S, synth
+
+    _build.build()
+    torch.cuda.set_device(local_rank)
+    curves = synth.ragged_mix(400, seed=5000 + 100000 * rank, n_range=(1000, 70000))
+    pool = [S.Request.from_curve(c) for c in curves]
+    srv = S.TransitServer(detrend_r=R_MEDIAN, hbm_budget=100e9)
+    plain = S.PlainServer(detrend_r=R_MEDIAN)
+    for r in pool[:40]:
+        srv.submit(r)
+    srv.run_until_idle()
+    for r in pool[:10]:
+        plain.process(r)
+    torch.cuda.synchronize()
+    picks = []
+    for kind in ("bls", "tls"):
+        for target in (5000, 20000, 60000):
+            picks.append(min((i for i in range(len(pool)) if pool[i].kind == kind),
+                             key=lambda i: abs(pool[i].n - target)))
+    rows, ev_sum, lat_sum = [], 0, 0.0
+    for _ in range(args.warmup):
+        for k in picks:
+            srv.submit(pool[k])
+            srv.run_until_idle()
+            plain.process(pool[k])
+    for k in picks:
+        r = pool[k]
+        lat, plat = [], []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            srv.submit(r, t0)
+            res = srv.run_until_idle()
+            lat.append(1e3 * (res[0].done - t0))
+            t0 = time.perf_counter()
+            pr = plain.process(r, t0)
+            plat.append(1e3 * (pr.done - t0))
+        ev = r.outputs
+        ev_sum += ev
+        lat_sum += float(np.median(lat)) / 1e3
+        rows.append({"kind": r.kind, "n": r.n, "evals": ev, "server_ms_p50": float(np.median(lat)),
+                     "server_ms_min": float(min(lat)), "plain_ms_p50": float(np.median(plat)),
+                     "plain_ms_min": float(min(plat))})
+    if rank != 0:
+        return
+    line = {"metric": METRIC, "value": ev_sum / lat_sum, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * lat_sum, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+i64", "data": "synthetic",
+            "config": {"workload": "lone requests: one BLS or GTLS request at a time (detrended; about 5k, 20k "
+                                   "and 60k samples each) through an idle TransitServer and through PlainServer",
+                       "requests": len(rows)},
+            "requests": rows}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -1777,7 +1840,7 @@ def main():
         torch.cuda.set_device(local_rank)
         dist.init_process_group("nccl")
     try:
-        {"ragged": run_ragged, "masked": run_masked, "served": run_served, "plain": run_image,
+        {"ragged": run_ragged, "masked": run_masked, "served": run_served, "lone": run_lone, "plain": run_image,
          "tls": run_image, "tlsfold": run_tlsfold, "mock": run_mock, "tlsfit": run_tlsfit,
          "epilogue": run_epilogue}[args.workload](
             args, rank, world, local_rank)

@@ -81,3 +81,54 @@ def test_gfilter_packed_bit_exact(cuda, lens, r):
     for x in xs:
         np.testing.assert_array_equal(got[o:o + x.size], oracle.medfilt_residual(x[:, None], r)[:, 0])
         o += x.size
+
+
+def _packed(cuda, xs, r):
+    from gtrap_gb300 import _native as N
+    from gtrap_gb300._dev import as_ptr
+    lens = [x.size for x in xs]
+    flat = torch.from_numpy(np.concatenate(xs)).to(cuda)
+    out = torch.empty_like(flat)
+    off = torch.tensor(np.concatenate([[0], np.cumsum(lens)[:-1]]), dtype=torch.int64, device=cuda)
+    n = torch.tensor(lens, dtype=torch.int32, device=cuda)
+    N.call("gtrap_gfilter_packed", as_ptr(flat), as_ptr(out), as_ptr(off), as_ptr(n), len(lens), max(lens), r,
+           torch.cuda.current_stream().cuda_stream)
+    got = out.cpu().numpy()
+    return np.split(got, np.cumsum(lens)[:-1])
+
+
+@pytest.mark.parametrize("kind", ["duplicates", "signed_zeros", "nan"])
+def test_gfilter_ties_zeros_and_nan(cuda, kind):
+    """Windows full of equal values, of +0 and -0, and with NaN, in the packed detrend (lone
+    curves: short runs) and the image detrend.  Windows that never held a NaN take binary
+    searches and block moves, the others the element-by-element loops.  Equal values: both
+    equal medfilt bit for bit.  Signed zeros: equal medfilt in value (which zero a window
+    holds depends on where its run started, as it always has).  NaN: every row whose window
+    and run have not yet met the first NaN equals medfilt."""
+    rng = np.random.default_rng({"duplicates": 1, "signed_zeros": 2, "nan": 3}[kind])
+    lens = (7000, 300, 41, 2500)
+    xs = []
+    for m in lens:
+        x = rng.integers(-3, 4, size=m).astype(np.float32)
+        if kind == "signed_zeros":
+            x[rng.random(m) < 0.4] = np.float32(-0.0)
+        if kind == "nan":
+            x = rng.normal(size=m).astype(np.float32)
+            x[int(m * 0.6):][rng.random(m - int(m * 0.6)) < 0.01] = np.nan
+        xs.append(x)
+    r = 24
+    got = _packed(cuda, xs, r)
+    for x, g in zip(xs, got):
+        img = api.gfilter(torch.from_numpy(x).to(cuda).view(-1, 1), r).cpu().numpy()[:, 0]
+        ref = oracle.medfilt_residual(np.nan_to_num(x)[:, None], r)[:, 0]
+        if kind == "duplicates":
+            np.testing.assert_array_equal(g, ref)
+            np.testing.assert_array_equal(img, ref)
+        elif kind == "signed_zeros":
+            assert np.array_equal(g, ref) and np.array_equal(img, ref)   # -0 == +0
+        else:
+            nan_at = np.flatnonzero(np.isnan(x))
+            clean = (nan_at[0] if nan_at.size else x.size) - r
+            if clean > 0:
+                np.testing.assert_array_equal(g[:clean], ref[:clean])
+                np.testing.assert_array_equal(img[:clean], ref[:clean])
