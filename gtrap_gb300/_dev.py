@@ -50,14 +50,19 @@ def stream_handle(stream=None) -> int:
     return int(stream)
 
 
-def workspace(nbytes: int, device=None, slot: str = "default") -> torch.Tensor:
-    """A cached device scratch buffer of at least ``nbytes`` (256-byte aligned).
+def workspace(nbytes: int, device=None, slot: str = "default", stream=None) -> torch.Tensor:
+    """A cached device scratch buffer of at least ``nbytes`` (256-byte aligned) for launches on
+    ``stream`` (default: the current stream).
 
-    The buffer is reused by later calls on the same stream order, which is safe because
-    every user of a slot launches on the stream that was current when it was sized.
+    Buffers are cached per (device, slot, launch stream), so calls on one stream reuse a buffer
+    in stream order and calls on different streams never share one.  The buffer is allocated
+    on the current stream: a caller that launches on another stream keeps that stream's work
+    ordered after the current stream's (or makes it current, ``with torch.cuda.stream(s)``),
+    as it must for the output tensors the API functions allocate there too.
     """
     dev = torch.device("cuda", torch.cuda.current_device() if device is None else device)
-    key = (dev.index, slot, torch.cuda.current_stream(dev).cuda_stream)
+    launch = stream_handle(stream) if stream is not None else torch.cuda.current_stream(dev).cuda_stream
+    key = (dev.index, slot, launch)
     with _ws_lock:
         buf = _workspaces.get(key)
         if buf is None or buf.numel() < nbytes:

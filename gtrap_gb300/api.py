@@ -3,6 +3,12 @@
 All functions take and return CUDA tensors, launch on the current PyTorch stream and
 return without synchronising.  Layouts follow the reference: light-curve images are
 ``[n, nq]`` float32 (C order), BLS spectra ``[nq, nf]``, GTLS outputs ``[nt, nq]``.
+
+A function given ``stream=`` launches on that stream, with a scratch workspace of its own
+for that stream, but allocates its outputs (and any contiguous copy of an input) through
+PyTorch on the current stream: make the stream current (``with torch.cuda.stream(s)``), or
+keep the current stream's later work ordered after it, so that freed memory is not reused
+while the launch still reads it.
 """
 from __future__ import annotations
 
@@ -111,7 +117,7 @@ def geebls(lc, tu, offset_, ntrue, nf, nb, kma, kmi, kkmi, fmin, df, *, phase="e
                torch.empty((nq, nf), dtype=torch.int32, device=dev))
     blsp, p1, p2 = out
     need = N.fn("gtrap_geebls_workspace_size")(n, nq, flags)
-    ws = workspace(need, slot="bls")
+    ws = workspace(need, slot="bls", stream=stream)
     N.call("gtrap_geebls", as_ptr(blsp), as_ptr(p1), as_ptr(p2), as_ptr(lc), as_ptr(tu),
            as_ptr(offset_), as_ptr(ntrue), n, nq, int(nf), int(nb), int(kma), int(kmi), int(kkmi),
            float(fmin), float(df), flags, int(ref_nthread), as_ptr(ws), ws.numel(),
@@ -139,7 +145,7 @@ def geebls_simple(lc, tu, nf, nb, kma, kmi, kkmi, fmin, df, *, phase="exact", re
     else:
         blsp, p1, p2 = out
     need = N.fn("gtrap_geebls_simple_workspace_size")(n, nq, flags)
-    ws = workspace(need, slot="bls")
+    ws = workspace(need, slot="bls", stream=stream)
     N.call("gtrap_geebls_simple", as_ptr(blsp), as_ptr(p1), as_ptr(p2), as_ptr(lc), as_ptr(tu),
            n, nq, int(nf), int(nb), int(kma), int(kmi), int(kkmi), float(fmin), float(df), flags,
            int(ref_nthread), as_ptr(ws), ws.numel(), stream_handle(stream))
@@ -204,7 +210,7 @@ def bls_refine(blsp, phase1, phase2, lc, tu, offset_, ntrue, nb, kma, kmi, kkmi,
     nf = blsp.shape[1]
     dev = lc.device
     out = torch.empty(nq * BLS_REFINED.itemsize, dtype=torch.uint8, device=dev)
-    ws = workspace(N.fn("gtrap_bls_refine_workspace_size")(nq, int(K)), slot="refine")
+    ws = workspace(N.fn("gtrap_bls_refine_workspace_size")(nq, int(K)), slot="refine", stream=stream)
     N.call("gtrap_bls_refine", as_ptr(blsp), as_ptr(phase1), as_ptr(phase2), as_ptr(lc), as_ptr(tu),
            as_ptr(_f32(offset_, "offset")), as_ptr(_u32(ntrue, "ntrue")), n, nq, int(nf), int(nb), int(kma),
            int(kmi), int(kkmi), float(fmin), float(df), int(K), int(S), int(M), as_ptr(out), as_ptr(ws),
@@ -221,7 +227,7 @@ def bls_refine_packed(blsp, phase1, phase2, curves, t, x, nb, kma, kmi, *, sel=N
     if count is None:
         count = int(sel.numel()) if sel is not None else curves.numel() // 56
     out = torch.empty(max(count, 1) * BLS_REFINED.itemsize, dtype=torch.uint8, device=dev)
-    ws = workspace(N.fn("gtrap_bls_refine_workspace_size")(max(count, 1), int(K)), slot="refine")
+    ws = workspace(N.fn("gtrap_bls_refine_workspace_size")(max(count, 1), int(K)), slot="refine", stream=stream)
     N.call("gtrap_bls_refine_packed", as_ptr(blsp), as_ptr(phase1), as_ptr(phase2), as_ptr(curves),
            as_ptr(sel) if sel is not None else None, int(count), as_ptr(t), as_ptr(x), int(nb), int(kma), int(kmi),
            int(K), int(S), int(M), as_ptr(out), as_ptr(ws), ws.numel(), stream_handle(stream))
@@ -371,7 +377,7 @@ def tls_fold(lc, tu, offset_, nf, nb, fmin, df, durations, *, lfrac=0.2, dmax=No
                torch.empty((nq, nf), dtype=torch.float32, device=dev))
     tsr, st, du, dep = out
     need = N.fn("gtrap_tls_fold_workspace_size")(n, nq)
-    ws = workspace(need, slot="tls_fold")
+    ws = workspace(need, slot="tls_fold", stream=stream)
     N.call("gtrap_tls_fold", as_ptr(tsr), as_ptr(st), as_ptr(du), as_ptr(dep), as_ptr(lc), as_ptr(tu),
            as_ptr(offset_), n, nq, int(nf), int(nb), float(fmin), float(df),
            w.ctypes.data_as(C.c_void_p), int(w.size), float(lfrac), int(dmax), as_ptr(ws), ws.numel(),

@@ -27,7 +27,7 @@ def _launch(reference_quirks):
         flags = N.BLS_PHASE_FP32_REF if reference_quirks else 0
         ref_nthread = int(block[0]) if reference_quirks else 0
         need = N.fn("gtrap_geebls_simple_workspace_size")(n, nq, flags)
-        ws = workspace(need, slot="bls")
+        ws = workspace(need, slot="bls", stream=stream)
         N.call("gtrap_geebls_simple", as_ptr(blsp), None, None, as_ptr(lc), as_ptr(tu), n, nq, nf,
                int(nb), int(kma), int(kmi), int(kkmi), float(fmin), float(df), flags, ref_nthread,
                as_ptr(ws), ws.numel(), stream_handle(stream))
