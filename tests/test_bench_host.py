@@ -1,6 +1,6 @@
 """Host-side helpers of bench.py (no GPU): the window-sample count behind the tlsfit roofline,
-the folded-search frequency rule of the mixed workloads, the CPU-rate weighting of the mix
-and the command-line defaults."""
+the folded-search frequency rule of the mixed workloads, the CPU-rate weighting of the mix,
+the command-line defaults and the served saturation run."""
 import sys
 
 import numpy as np
@@ -64,3 +64,38 @@ def test_probe_library_is_separate_and_validates_on_the_host():
         assert getattr(lib, name)(None, 10, None, None) == -1
         assert not any("probe" in s for s in _native.exported_symbols())
     assert lib.bench_probe_fp32(C.c_void_p(0), 0, None, None) == -1
+
+
+def test_saturation_offers_every_request_at_once_and_releases_results():
+    """bench.saturation: the whole pool offered at t = 0 through serve_trace, results released
+    as they arrive (byte counts kept) and collected into ``out``."""
+    from gtrap_gb300 import serve as S
+    from gtrap_gb300.serve import Result
+
+    class Fake:
+        def __init__(self):
+            self.pending, self.step_count, self.arrivals = [], 0, []
+
+        @property
+        def idle(self):
+            return not self.pending
+
+        def submit(self, req, arrival):
+            self.pending.append(req)
+            self.arrivals.append(arrival)
+
+        def step(self, now):
+            done = [Result(k, "tls", self.arrivals[k], now, now, (np.zeros(q, np.float32),), q)
+                    for k, q in enumerate(self.pending)]
+            self.step_count += bool(done)
+            self.pending = []
+            return done
+
+        def wait(self, until=None):
+            pass
+
+    srv, out = Fake(), []
+    summ = bench.saturation(S, srv, [4, 6, 9], out)
+    assert len(set(srv.arrivals)) == 1          # every request offered at the same instant
+    assert summ["requests"] == 3 and summ["req_per_s"] > 0
+    assert [r.nbytes for r in out] == [16, 24, 36] and all(r.outputs is None for r in out)
