@@ -87,7 +87,9 @@ int gtrap_gfilter(const float *in, float *out, uint32_t n, uint32_t nq, uint32_t
                   gtrap_stream_t stream);
 
 /* Per-curve offset.  Replaces get_offset (gtrap/gfilter.py:94-101):
- *   offset[q] = sum_{i : !(tu[i,q] < 0)} resid[i, q] / n   (masked samples count as 0). */
+ *   offset[q] = sum_{i : !(tu[i,q] < 0)} resid[i, q] / n   (masked samples count as 0).
+ * The sum has a fixed order (256 compensated partials over i mod 256, combined in double),
+ * shared with gtrap_bls_offsets: deterministic, and equal to the bit between the two. */
 int gtrap_offset(const float *resid, const float *tu, float *offset, uint32_t n, uint32_t nq,
                  gtrap_stream_t stream);
 
@@ -180,7 +182,7 @@ typedef struct {
 int gtrap_gfilter_packed(const float *in, float *out, const uint64_t *off, const uint32_t *n,
                          uint32_t ncurves, uint32_t max_n, uint32_t r, gtrap_stream_t stream);
 /* curves[q].offset = sum of resid over samples with t >= 0, divided by n (get_offset,
- * gtrap/gfilter.py:94-101), for packed curves. */
+ * gtrap/gfilter.py:94-101), for packed curves, in gtrap_offset's summation order. */
 int gtrap_bls_offsets(gtrap_bls_curve *curves, uint32_t ncurves, const float *t, const float *resid,
                       gtrap_stream_t stream);
 /* Frequencies per tile that gtrap_geebls picks for this bin grid on the current device
