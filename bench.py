@@ -1823,6 +1823,12 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
+        if args.workload in ("served", "lone"):
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the reference has no serving loop or "
+                                  "per-request path (its drivers launch one kernel per image); its CPU rate on "
+                                  "the same mix is the default workload's reference arm"}), flush=True)
+            return
         if args.workload == "masked":
             run_masked_reference(args, rank, world)
         elif args.workload == "tlsfold":

@@ -99,3 +99,14 @@ def test_saturation_offers_every_request_at_once_and_releases_results():
     assert len(set(srv.arrivals)) == 1          # every request offered at the same instant
     assert summ["requests"] == 3 and summ["req_per_s"] > 0
     assert [r.nbytes for r in out] == [16, 24, 36] and all(r.outputs is None for r in out)
+
+
+@pytest.mark.parametrize("workload", ["served", "lone"])
+def test_reference_arm_of_served_workloads_is_unavailable(monkeypatch, capsys, workload):
+    """The reference has no serving loop: its arm of the served and lone workloads says so in
+    one JSON line instead of timing another workload."""
+    import json
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--workload", workload])
+    bench.main()
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and "unavailable" in line
