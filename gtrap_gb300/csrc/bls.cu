@@ -389,10 +389,6 @@ __device__ __forceinline__ void group_bar(int id, int nthreads) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
 
-__device__ __forceinline__ bool better(float p, int i, int e, float bp, int bi, int be) {
-  return p > bp || (p == bp && (i < bi || (i == bi && e < be)));
-}
-
 // Fold + scan of one tile by the whole block (blockDim.x == kThreads).
 // MODE 0: exact phase, nb power of two; 1: exact phase, any nb; 2: FP32 reference phase.
 template <int R, int MODE>
@@ -694,9 +690,9 @@ __device__ __forceinline__ void bls_tile(const BlsShape a, const BlsTile &tj) {
     }
     const float clast = __shfl_sync(0xffffffffu, v.y, swz(min(32 * c + 31, elast)) - 32 * c);
     if (lane == 0) {
-      unsigned long long *R = sm + (size_t)f * a.region + lp;
-      reinterpret_cast<float2 *>(R)[c] = make_float2(mx, mn);
-      reinterpret_cast<float *>(R + nchunk)[c] = clast;
+      unsigned long long *Rb = sm + (size_t)f * a.region + lp;
+      reinterpret_cast<float2 *>(Rb)[c] = make_float2(mx, mn);
+      reinterpret_cast<float *>(Rb + nchunk)[c] = clast;
     }
   }
   auto window_power = [&](const float2 *P, int i, int e, float &pw) -> bool {
